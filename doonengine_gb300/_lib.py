@@ -1,0 +1,221 @@
+"""ctypes view of libdoonengine.so: the DN_* API (include/DoonEngine/voxel.h) and the dn_cuda_* C ABI
+(include/dn_cuda.h).  Struct layouts mirror the C headers; ``check_layout()`` compares them with the
+library's own ``DN_abi_layout``."""
+import ctypes
+import os
+from ctypes import (POINTER, Structure, c_bool, c_char_p, c_float, c_int, c_size_t, c_uint8, c_uint32,
+                    c_uint64, c_void_p, c_int32)
+
+from . import build as _build
+
+
+class DNvec2(Structure):
+    _fields_ = [("x", c_float), ("y", c_float)]
+
+
+class DNvec3(Structure):
+    _fields_ = [("x", c_float), ("y", c_float), ("z", c_float)]
+
+    def tolist(self):
+        return [self.x, self.y, self.z]
+
+
+class DNmat4(Structure):
+    _fields_ = [("m", (c_float * 4) * 4)]   # column-major m[col][row]
+
+
+class DNivec3(Structure):
+    _fields_ = [("x", c_int32), ("y", c_int32), ("z", c_int32)]
+
+
+class DNuvec3(Structure):
+    _fields_ = [("x", c_uint32), ("y", c_uint32), ("z", c_uint32)]
+
+
+class DNcolor(Structure):
+    _fields_ = [("r", c_uint8), ("g", c_uint8), ("b", c_uint8)]
+
+
+class DNvoxel(Structure):
+    _fields_ = [("material", c_uint8), ("normal", DNvec3), ("albedo", DNcolor)]
+
+
+class DNcompressedVoxel(Structure):
+    _fields_ = [("normal", c_uint32), ("albedo", c_uint32)]
+
+
+class DNchunk(Structure):
+    _fields_ = [("pos", DNivec3), ("updated", c_bool), ("numVoxels", c_uint32), ("numVoxelsGpu", c_uint32),
+                ("voxels", DNcompressedVoxel * 512)]   # [x][y][z] flattened: x*64 + y*8 + z
+
+
+class DNchunkHandle(Structure):
+    _fields_ = [("flag", c_uint8), ("chunkIndex", c_uint32)]
+
+
+class DNmaterial(Structure):
+    _fields_ = [("padding", DNvec2), ("emissive", c_uint32), ("opacity", c_float), ("refractIndex", c_float),
+                ("specular", c_float), ("reflectType", c_uint32), ("shininess", c_uint32)]
+
+
+class DNvolume(Structure):
+    _fields_ = [
+        ("gpu", c_void_p),
+        ("mapSize", DNuvec3),
+        ("chunkCap", c_size_t), ("nextChunk", c_size_t), ("voxelCap", c_size_t), ("numVoxelNodes", c_size_t),
+        ("numLightingRequests", c_size_t), ("lightingRequestCap", c_size_t),
+        ("map", POINTER(DNchunkHandle)), ("chunks", POINTER(DNchunk)), ("materials", POINTER(DNmaterial)),
+        ("lightingRequests", POINTER(c_uint32)), ("gpuVoxelLayout", c_void_p),
+        ("camPos", DNvec3), ("camOrient", DNvec3), ("camFOV", c_float), ("camViewMode", c_uint32),
+        ("sunDir", DNvec3), ("sunStrength", DNvec3), ("ambientLightStrength", DNvec3),
+        ("diffuseBounceLimit", c_uint32), ("specBounceLimit", c_uint32), ("shadowSoftness", c_float),
+        ("useCubemap", c_bool), ("glCubemapTex", c_uint32), ("skyGradientBot", DNvec3), ("skyGradientTop", DNvec3),
+        ("frameNum", c_uint32), ("lastTime", c_float),
+        ("emissiveStrength", c_float), ("numDirectRays", c_uint32), ("rngMode", c_uint32), ("mapId", c_uint32),
+        ("truncateDispatch", c_uint32), ("deviceBudgetBytes", c_uint64),
+    ]
+
+
+class DNimage(Structure):
+    _fields_ = [("width", c_uint32), ("height", c_uint32), ("color", POINTER(c_float)),
+                ("hitIndex", POINTER(c_uint32)), ("hitFace", POINTER(c_uint8)), ("onDevice", c_int)]
+
+
+class DNstats(Structure):
+    _fields_ = [("rays", c_uint64), ("primaryRays", c_uint64), ("outerSteps", c_uint64), ("chunksEntered", c_uint64),
+                ("innerSteps", c_uint64), ("hits", c_uint64), ("litVoxels", c_uint64)]
+
+
+MESSAGE_CALLBACK = ctypes.CFUNCTYPE(None, c_int, c_int, c_char_p)
+VOLP = POINTER(DNvolume)
+
+# (name, restype, argtypes)
+_SIGS = [
+    ("DN_init", c_bool, []),
+    ("DN_quit", None, []),
+    ("DN_create_volume", VOLP, [DNuvec3, c_uint32]),
+    ("DN_create_volume_cpu", VOLP, [DNuvec3, c_uint32]),
+    ("DN_delete_volume", None, [VOLP]),
+    ("DN_load_volume", VOLP, [c_char_p, c_uint32]),
+    ("DN_save_volume", c_bool, [c_char_p, VOLP]),
+    ("DN_set_view_projection_matrices", None, [VOLP, c_float, c_float, c_float, POINTER(DNmat4), POINTER(DNmat4)]),
+    ("DN_draw", None, [VOLP, POINTER(DNimage), DNmat4, DNmat4, c_int, c_int]),
+    ("DN_update_lighting", None, [VOLP, c_int, c_int, c_float]),
+    ("DN_add_chunk", c_int, [VOLP, DNivec3]),
+    ("DN_remove_chunk", None, [VOLP, DNivec3]),
+    ("DN_sync_gpu", None, [VOLP, c_int, c_int]),
+    ("DN_set_map_size", c_bool, [VOLP, DNuvec3]),
+    ("DN_set_max_chunks", c_bool, [VOLP, c_size_t]),
+    ("DN_set_max_voxels_gpu", c_bool, [VOLP, c_size_t]),
+    ("DN_set_max_lighting_requests", c_bool, [VOLP, c_size_t]),
+    ("DN_in_map_bounds", c_bool, [VOLP, DNivec3]),
+    ("DN_in_chunk_bounds", c_bool, [DNivec3]),
+    ("DN_get_voxel", DNvoxel, [VOLP, DNivec3, DNivec3]),
+    ("DN_get_compressed_voxel", DNcompressedVoxel, [VOLP, DNivec3, DNivec3]),
+    ("DN_set_voxel", None, [VOLP, DNivec3, DNivec3, DNvoxel]),
+    ("DN_set_compressed_voxel", None, [VOLP, DNivec3, DNivec3, DNcompressedVoxel]),
+    ("DN_remove_voxel", None, [VOLP, DNivec3, DNivec3]),
+    ("DN_does_chunk_exist", c_bool, [VOLP, DNivec3]),
+    ("DN_does_voxel_exist", c_bool, [VOLP, DNivec3, DNivec3]),
+    ("DN_step_map", c_bool, [VOLP, DNvec3, DNvec3, c_int, POINTER(DNivec3), POINTER(DNvoxel), POINTER(DNivec3)]),
+    ("DN_separate_position", None, [DNivec3, POINTER(DNivec3), POINTER(DNivec3)]),
+    ("DN_cam_dir", DNvec3, [DNvec3]),
+    ("DN_compress_voxel", DNcompressedVoxel, [DNvoxel]),
+    ("DN_decompress_voxel", DNvoxel, [DNcompressedVoxel]),
+    ("DN_finish", c_bool, [VOLP]),
+    ("DN_image_create", POINTER(DNimage), [c_uint32, c_uint32, c_int, c_int]),
+    ("DN_image_destroy", None, [POINTER(DNimage)]),
+    ("DN_draw_matrices", None, [DNmat4, DNmat4, POINTER(DNmat4), POINTER(DNmat4), POINTER(DNmat4)]),
+    ("DN_get_stats", c_bool, [VOLP, POINTER(DNstats)]),
+    ("DN_reset_stats", None, [VOLP]),
+    ("DN_export_lighting", c_size_t, [VOLP, POINTER(c_uint32), POINTER(c_float), POINTER(c_float), c_size_t]),
+    ("DN_export_tiles", c_bool, [VOLP, POINTER(c_uint8), POINTER(c_uint8), POINTER(c_uint32), POINTER(c_uint32)]),
+    ("DN_export_requests", c_size_t, [VOLP, POINTER(c_uint32), c_size_t]),
+    ("DN_compress_chunk", c_size_t, [VOLP, POINTER(DNchunk), POINTER(c_uint8)]),
+    ("DN_decompress_chunk", c_int, [VOLP, POINTER(c_uint8), c_size_t, POINTER(DNchunk)]),
+    ("DN_abi_layout", c_size_t, [POINTER(c_uint64), c_size_t]),
+    ("DN_set_allocator", None, [c_void_p, c_void_p, c_void_p]),
+    ("DN_mat4_inv", DNmat4, [DNmat4]),
+    ("DN_mat4_mult", DNmat4, [DNmat4, DNmat4]),
+    ("DN_vec3_normalize", DNvec3, [DNvec3]),
+    ("dn_scene_palette", None, [VOLP, c_uint32, c_uint32, c_uint32, c_float, c_float, c_float]),
+    ("dn_scene_terrain", None, [VOLP, c_uint32, c_float, c_float, c_uint32, c_uint32]),
+    ("dn_scene_shapes", None, [VOLP, c_uint32, c_uint32, c_int32, c_int32, c_uint32, c_float, c_float]),
+    ("dn_scene_camera", None, [VOLP, c_float, c_float, c_float, c_float, c_float, c_float]),
+    # C ABI
+    ("dn_cuda_init", c_int, [c_int]),
+    ("dn_cuda_shutdown", None, []),
+    ("dn_cuda_error_string", c_char_p, [c_int]),
+    ("dn_cuda_last_error", c_char_p, []),
+    ("dn_cuda_map_create", c_int, [c_uint32, c_uint32, c_uint32, c_uint32, c_uint64, POINTER(c_void_p)]),
+    ("dn_cuda_map_destroy", None, [c_void_p]),
+    ("dn_cuda_map_resize", c_int, [c_void_p, c_uint32, c_uint32, c_uint32]),
+    ("dn_cuda_reserve", c_int, [c_void_p, c_uint32, c_uint64, c_uint64]),
+    ("dn_cuda_sync", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p, c_uint32, c_void_p, c_uint64]),
+    ("dn_cuda_light", c_int, [c_void_p, c_void_p, c_void_p]),
+    ("dn_cuda_draw", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("dn_cuda_draw_host", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("dn_cuda_finish", c_int, [c_void_p, POINTER(c_uint64)]),
+    ("dn_cuda_stats", c_int, [c_void_p, c_void_p]),
+    ("dn_cuda_reset_stats", c_int, [c_void_p]),
+    ("dn_cuda_stream", c_void_p, [c_void_p]),
+    ("dn_cuda_export_tiles", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("dn_cuda_export_requests", c_int, [c_void_p, c_void_p, c_uint64, POINTER(c_uint64)]),
+    ("dn_cuda_export_lighting", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint64, POINTER(c_uint64)]),
+    ("dn_cuda_malloc", c_int, [POINTER(c_void_p), c_size_t]),
+    ("dn_cuda_free", c_int, [c_void_p]),
+    ("dn_cuda_malloc_host", c_int, [POINTER(c_void_p), c_size_t]),
+    ("dn_cuda_free_host", c_int, [c_void_p]),
+    ("dn_cuda_memcpy_d2h", c_int, [c_void_p, c_void_p, c_size_t]),
+    ("dn_cuda_memcpy_h2d", c_int, [c_void_p, c_void_p, c_size_t]),
+    ("dn_cuda_event_create", c_int, [POINTER(c_void_p)]),
+    ("dn_cuda_event_destroy", c_int, [c_void_p]),
+    ("dn_cuda_event_record", c_int, [c_void_p, c_void_p]),
+    ("dn_cuda_event_elapsed_ms", c_int, [c_void_p, c_void_p, POINTER(c_float)]),
+    ("dn_cuda_stream_sync", c_int, [c_void_p]),
+    ("dn_cuda_device_sync", c_int, []),
+    ("dn_cuda_flush_l2", c_int, [c_void_p, c_size_t]),
+    ("dn_cuda_kernel_names", c_char_p, []),
+]
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libdoonengine.so (building it in-tree when it is missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_missing:
+        _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError("libdoonengine.so is not built (%s); run doonengine_gb300.build.build()" % path)
+    lib = ctypes.CDLL(path)
+    for name, res, args in _SIGS:
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_names():
+    return [n for n, _, _ in _SIGS]
+
+
+def check_layout(lib=None):
+    """Compare the ctypes struct layouts with the library's own sizes / offsets; returns a list of mismatches."""
+    lib = lib or load()
+    buf = (c_uint64 * 32)()
+    n = lib.DN_abi_layout(buf, 32)
+    want = [ctypes.sizeof(DNvolume), DNvolume.mapSize.offset, DNvolume.map.offset, DNvolume.chunks.offset,
+            DNvolume.materials.offset, DNvolume.camPos.offset, DNvolume.sunDir.offset, DNvolume.useCubemap.offset,
+            DNvolume.frameNum.offset, DNvolume.emissiveStrength.offset, DNvolume.deviceBudgetBytes.offset,
+            ctypes.sizeof(DNchunk), ctypes.sizeof(DNmaterial), ctypes.sizeof(DNimage), ctypes.sizeof(DNchunkHandle),
+            ctypes.sizeof(DNstats), DNchunk.voxels.offset, ctypes.sizeof(DNvoxel)]
+    return [(i, int(buf[i]), w) for i, w in enumerate(want[:n]) if int(buf[i]) != w]

@@ -1,0 +1,1046 @@
+/*
+ * voxel.c -- host side of the DoonEngine DN_* API (include/DoonEngine/voxel.h)
+ * on top of the CUDA C ABI (include/dn_cuda.h).
+ *
+ * The CPU-side map (handles + 8x8x8 chunks) and the voxel edit API keep the
+ * reference's semantics (src/DoonEngine/voxel.c:659-714, 1101-1316).  What the
+ * reference does with OpenGL is done here as follows:
+ *   - chunks changed through the API are recorded in a per-volume dirty list;
+ *     DN_sync_gpu packs each changed chunk (surface cull, occupancy mask,
+ *     partial counts, linearised albedo: voxel.c:1391-1461) and stages it in
+ *     the device pool in one batched upload, instead of packing only chunks
+ *     that rays requested (voxel.c:1517-1531).  The device flips a requested
+ *     chunk to "loaded" at the next sync exactly when the reference would
+ *     upload it, so the observable state sequence is unchanged, and no
+ *     per-frame readback of the map is needed (the reference maps the whole
+ *     map buffer every frame, voxel.c:731);
+ *   - device record slots and voxel ranges come from a host-side allocator
+ *     with power-of-two size classes (32..512 voxels) and free lists, in
+ *     place of the linear node scan and bubble-sort defragmentation of
+ *     voxel.c:1554-1695; the pool grows by doubling before a chunk would not
+ *     fit, so every requested chunk loads in the same sync (the reference
+ *     fails the upload, doubles at the end of the sync and loads it a frame
+ *     later, voxel.c:1592-1596, 773-782).
+ */
+#include "DoonEngine/voxel.h"
+#include "dn_cuda.h"
+#include <math.h>
+#include <string.h>
+#include <stdarg.h>
+
+/* ------------------------------------------------------------- globals */
+
+void (*g_DN_message_callback)(DNmessageType, DNmessageSeverity, const char*) = NULL;
+
+static DNmallocFn s_malloc = malloc;
+static DNfreeFn s_free = free;
+static DNreallocFn s_realloc = realloc;
+
+void DN_set_allocator(DNmallocFn m, DNfreeFn f, DNreallocFn r)
+{
+	s_malloc = m ? m : malloc;
+	s_free = f ? f : free;
+	s_realloc = r ? r : realloc;
+}
+void* DN_host_malloc(size_t s) { return s_malloc(s); }
+void DN_host_free(void* p) { if (p) s_free(p); }
+void* DN_host_realloc(void* p, size_t s) { return s_realloc(p, s); }
+
+static void dn_msg(DNmessageType t, DNmessageSeverity s, const char* fmt, ...)
+{
+	if (!g_DN_message_callback) return;
+	char buf[512];
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(buf, sizeof(buf), fmt, ap);
+	va_end(ap);
+	g_DN_message_callback(t, s, buf);
+}
+
+static int s_initialized = 0;
+static uint8_t s_linear[256];   /* sRGB byte -> linear byte, voxel.c:1441-1447 */
+static void init_linear_table(void);
+
+#define GET_MATERIAL_ID(x) ((x) >> 24)
+#define NUM_CLASSES 5           /* voxel ranges of 32, 64, 128, 256, 512 voxels */
+
+/* ----------------------------------------------------- private volume state */
+
+typedef struct u32vec { uint32_t* v; size_t n, cap; } u32vec;
+
+static int u32_push(u32vec* a, uint32_t x)
+{
+	if (a->n == a->cap) {
+		size_t nc = a->cap ? a->cap * 2 : 256;
+		uint32_t* nv = (uint32_t*)DN_REALLOC(a->v, nc * sizeof(uint32_t));
+		if (!nv) return 0;
+		a->v = nv; a->cap = nc;
+	}
+	a->v[a->n++] = x;
+	return 1;
+}
+
+typedef struct DNvolumePriv
+{
+	DNvolume pub;              /* must stay first */
+	uint8_t* dirty;            /* per tile */
+	u32vec dirtyList;
+	uint32_t* tileSlot;        /* per tile: staged record slot or DN_SLOT_NONE */
+	/* record slots */
+	uint32_t slotCap, slotNext;
+	u32vec freeSlots;
+	uint32_t* slotBase;        /* per slot: first voxel */
+	uint8_t* slotClass;        /* per slot: size class */
+	uint32_t* slotGroups;      /* per slot: ceil(nvox/32) */
+	/* voxel ranges */
+	uint64_t poolNext;
+	u32vec freeRanges[NUM_CLASSES];
+	uint64_t groupsStaged;
+	uint64_t stagedChunks;
+	/* sync scratch */
+	dn_tile_op* ops; size_t opsCap;
+	dn_chunk_record* recs; size_t recsCap;
+	uint32_t* vwords; size_t vwordsCap;   /* in uint32 units */
+	u32vec deferredSlots;
+	/* the last view/projection passed to DN_draw */
+	float sphereK; float spherePts[64][3]; uint32_t sphereValid;
+} DNvolumePriv;
+
+static inline DNvolumePriv* priv(DNvolume* v) { return (DNvolumePriv*)v; }
+
+/* ------------------------------------------------------------ init / quit */
+
+bool DN_init(void)
+{
+	int rc = dn_cuda_init(-1);
+	if (rc != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_FATAL, "failed to initialise the CUDA device: %s", dn_cuda_last_error());
+		return false;
+	}
+	init_linear_table();
+	s_initialized = 1;
+	return true;
+}
+
+void DN_quit(void)
+{
+	dn_cuda_shutdown();
+	s_initialized = 0;
+}
+
+/* --------------------------------------------------------- create / delete */
+
+static void clear_chunk(DNvolume* vol, size_t index)
+{
+	/* voxel.c:1353-1363 */
+	DNchunk* c = &vol->chunks[index];
+	c->pos = (DNivec3){-1, -1, -1};
+	c->updated = false;
+	c->numVoxels = 0;
+	c->numVoxelsGpu = 0;
+	for (int x = 0; x < 8; x++)
+		for (int y = 0; y < 8; y++)
+			for (int z = 0; z < 8; z++) c->voxels[x][y][z].normal = UINT32_MAX;
+}
+
+static size_t num_tiles(DNuvec3 s) { return (size_t)s.x * s.y * s.z; }
+
+static void free_priv_arrays(DNvolumePriv* p)
+{
+	DN_FREE(p->dirty); DN_FREE(p->dirtyList.v); DN_FREE(p->tileSlot);
+	DN_FREE(p->freeSlots.v); DN_FREE(p->slotBase); DN_FREE(p->slotClass); DN_FREE(p->slotGroups);
+	for (int c = 0; c < NUM_CLASSES; c++) DN_FREE(p->freeRanges[c].v);
+	DN_FREE(p->ops); DN_FREE(p->recs); DN_FREE(p->vwords); DN_FREE(p->deferredSlots.v);
+}
+
+static bool alloc_tile_arrays(DNvolumePriv* p, size_t tiles)
+{
+	p->dirty = (uint8_t*)DN_MALLOC(tiles ? tiles : 1);
+	p->tileSlot = (uint32_t*)DN_MALLOC(sizeof(uint32_t) * (tiles ? tiles : 1));
+	if (!p->dirty || !p->tileSlot) return false;
+	memset(p->dirty, 0, tiles);
+	for (size_t i = 0; i < tiles; i++) p->tileSlot[i] = DN_SLOT_NONE;
+	return true;
+}
+
+static void init_linear_table(void)
+{
+	for (int b = 0; b < 256; b++) {
+		float l = (float)b * 0.00392156862f;
+		l = powf(l, DN_GAMMA);
+		l = l * 255.0f;
+		s_linear[b] = (uint8_t)l;
+	}
+}
+
+static DNvolume* create_volume(DNuvec3 mapSize, unsigned int minChunks, int withDevice);
+
+DNvolume* DN_create_volume(DNuvec3 mapSize, unsigned int minChunks)
+{
+	if (!s_initialized && !DN_init()) return NULL;
+	return create_volume(mapSize, minChunks, 1);
+}
+
+DNvolume* DN_create_volume_cpu(DNuvec3 mapSize, unsigned int minChunks)
+{
+	init_linear_table();
+	return create_volume(mapSize, minChunks, 0);
+}
+
+static DNvolume* create_volume(DNuvec3 mapSize, unsigned int minChunks, int withDevice)
+{
+	size_t tiles = num_tiles(mapSize);
+	if (tiles == 0 || tiles >= (1u << 28)) {
+		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "invalid map size %ux%ux%u", mapSize.x, mapSize.y, mapSize.z);
+		return NULL;
+	}
+	DNvolumePriv* p = (DNvolumePriv*)DN_MALLOC(sizeof(DNvolumePriv));
+	if (!p) {
+		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_FATAL, "failed to allocate memory for the volume");
+		return NULL;
+	}
+	memset(p, 0, sizeof(*p));
+	DNvolume* vol = &p->pub;
+
+	/* sized from x*y*z (the reference sizes its GPU buffers from x*y*x, voxel.c:173, 184) */
+	size_t numChunks = tiles < minChunks ? tiles : (size_t)minChunks;
+	if (numChunks == 0) numChunks = 1;
+
+	vol->map = (DNchunkHandle*)DN_MALLOC(sizeof(DNchunkHandle) * tiles);
+	if (!vol->map) { dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_FATAL, "failed to allocate memory for map"); goto fail; }
+	memset(vol->map, 0, sizeof(DNchunkHandle) * tiles);
+
+	vol->chunks = (DNchunk*)DN_MALLOC(sizeof(DNchunk) * numChunks);
+	if (!vol->chunks) { dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_FATAL, "failed to allocate memory for chunks"); goto fail; }
+	vol->chunkCap = numChunks;
+	for (size_t i = 0; i < numChunks; i++) clear_chunk(vol, i);
+
+	vol->materials = (DNmaterial*)DN_MALLOC(sizeof(DNmaterial) * DN_MAX_MATERIALS);
+	if (!vol->materials) { dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_FATAL, "failed to allocate memory for materials"); goto fail; }
+	memset(vol->materials, 0, sizeof(DNmaterial) * DN_MAX_MATERIALS);
+
+	if (!alloc_tile_arrays(p, tiles)) { dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_FATAL, "failed to allocate memory for tile state"); goto fail; }
+
+	{
+		uint32_t slotCap = (uint32_t)(numChunks < 64 ? 64 : numChunks);
+		uint64_t voxCap = (uint64_t)DN_CHUNK_LENGTH * numChunks / 2;
+		if (voxCap < 4096) voxCap = 4096;
+		int rc = withDevice ? dn_cuda_map_create(mapSize.x, mapSize.y, mapSize.z, slotCap, voxCap, &vol->gpu) : DN_CUDA_OK;
+		if (rc != DN_CUDA_OK) {
+			dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_FATAL, "failed to create the device map: %s", dn_cuda_last_error());
+			goto fail;
+		}
+		p->slotCap = slotCap;
+		p->slotBase = (uint32_t*)DN_MALLOC(sizeof(uint32_t) * slotCap);
+		p->slotClass = (uint8_t*)DN_MALLOC(slotCap);
+		p->slotGroups = (uint32_t*)DN_MALLOC(sizeof(uint32_t) * slotCap);
+		if (!p->slotBase || !p->slotClass || !p->slotGroups) { dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_FATAL, "failed to allocate slot tables"); goto fail; }
+		vol->voxelCap = voxCap;
+		vol->lightingRequestCap = 1024;   /* the device starts with 1024 request words */
+	}
+
+	vol->mapSize = mapSize;
+	vol->nextChunk = 0;
+	vol->numLightingRequests = 0;
+	vol->lightingRequests = NULL;
+	vol->gpuVoxelLayout = NULL;
+
+	/* defaults, voxel.c:261-278 */
+	vol->camPos = (DNvec3){{0.0f, 0.0f, 0.0f}};
+	vol->camOrient = (DNvec3){{0.0f, 0.0f, 0.0f}};
+	vol->camFOV = 90.0f;
+	vol->camViewMode = 0;
+	vol->sunDir = (DNvec3){{1.0f, 1.0f, 1.0f}};
+	vol->sunStrength = (DNvec3){{0.6f, 0.6f, 0.6f}};
+	vol->ambientLightStrength = (DNvec3){{0.01f, 0.01f, 0.01f}};
+	vol->diffuseBounceLimit = 5;
+	vol->specBounceLimit = 2;
+	vol->shadowSoftness = 10.0f;
+	vol->useCubemap = false;
+	vol->skyGradientBot = (DNvec3){{0.71f, 0.85f, 0.90f}};
+	vol->skyGradientTop = (DNvec3){{0.00f, 0.45f, 0.74f}};
+	vol->frameNum = 0;
+	vol->lastTime = 123.456f;
+	vol->emissiveStrength = 1.0f;
+	vol->numDirectRays = 15;
+	vol->rngMode = 0;
+	vol->mapId = 0;
+	vol->truncateDispatch = 0;
+	vol->deviceBudgetBytes = 0;
+	return vol;
+
+fail:
+	if (vol->gpu) dn_cuda_map_destroy(vol->gpu);
+	DN_FREE(vol->map); DN_FREE(vol->chunks); DN_FREE(vol->materials);
+	free_priv_arrays(p);
+	DN_FREE(p);
+	return NULL;
+}
+
+void DN_delete_volume(DNvolume* vol)
+{
+	if (!vol) return;
+	DNvolumePriv* p = priv(vol);
+	if (vol->gpu) dn_cuda_map_destroy(vol->gpu);
+	DN_FREE(vol->map); DN_FREE(vol->chunks); DN_FREE(vol->materials);
+	free_priv_arrays(p);
+	DN_FREE(p);
+}
+
+/* ------------------------------------------------------------ dirty tiles */
+
+static void mark_dirty(DNvolume* vol, size_t tile)
+{
+	DNvolumePriv* p = priv(vol);
+	if (p->dirty[tile]) return;
+	if (!u32_push(&p->dirtyList, (uint32_t)tile)) {
+		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to record a changed chunk");
+		return;
+	}
+	p->dirty[tile] = 1;
+}
+
+/* marks a chunk read from a file: staged at the next sync, not counted as updated */
+void DN_volume_mark_loaded_chunk(DNvolume* vol, size_t tile) { mark_dirty(vol, tile); }
+
+/* ------------------------------------------------------------ chunk memory */
+
+int DN_add_chunk(DNvolume* vol, DNivec3 pos)
+{
+	/* voxel.c:659-706: ring search from nextChunk for a free chunk, else double the capacity */
+	size_t i = vol->nextChunk;
+	do {
+		if (!DN_in_map_bounds(vol, vol->chunks[i].pos)) {
+			size_t mapIndex = DN_FLATTEN_INDEX(pos, vol->mapSize);
+			vol->map[mapIndex].chunkIndex = (uint32_t)i;
+			vol->map[mapIndex].flag = 1;
+			vol->chunks[i].pos = pos;
+			vol->nextChunk = (i == vol->chunkCap - 1) ? 0 : i + 1;
+			mark_dirty(vol, mapIndex);
+			return (int)i;
+		}
+		i++;
+		if (i >= vol->chunkCap) i = 0;
+	} while (i != vol->nextChunk);
+
+	size_t tiles = num_tiles(vol->mapSize);
+	size_t newCap = vol->chunkCap * 2 < tiles ? vol->chunkCap * 2 : tiles;
+	dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_NOTE, "automatically resizing chunk memory to accomodate %zu chunks (%zu bytes)",
+	       newCap, newCap * sizeof(DNchunk));
+	i = vol->chunkCap;
+	if (newCap <= vol->chunkCap || !DN_set_max_chunks(vol, newCap)) return -1;
+	size_t mapIndex = DN_FLATTEN_INDEX(pos, vol->mapSize);
+	vol->map[mapIndex].chunkIndex = (uint32_t)i;
+	vol->map[mapIndex].flag = 1;
+	vol->chunks[i].pos = pos;
+	vol->nextChunk = (i == vol->chunkCap - 1) ? 0 : i + 1;
+	mark_dirty(vol, mapIndex);
+	return (int)i;
+}
+
+void DN_remove_chunk(DNvolume* vol, DNivec3 pos)
+{
+	/* voxel.c:708-714 */
+	size_t mapIndex = DN_FLATTEN_INDEX(pos, vol->mapSize);
+	vol->map[mapIndex].flag = 0;
+	vol->nextChunk = vol->map[mapIndex].chunkIndex;
+	clear_chunk(vol, vol->map[mapIndex].chunkIndex);
+	mark_dirty(vol, mapIndex);
+}
+
+/* ------------------------------------------------------------- settings */
+
+bool DN_set_max_chunks(DNvolume* vol, size_t num)
+{
+	/* voxel.c:1012-1029 */
+	DNchunk* nc = (DNchunk*)DN_REALLOC(vol->chunks, sizeof(DNchunk) * num);
+	if (!nc) {
+		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to reallocate memory for chunks");
+		return false;
+	}
+	vol->chunks = nc;
+	for (size_t i = vol->chunkCap; i < num; i++) clear_chunk(vol, i);
+	vol->chunkCap = num;
+	return true;
+}
+
+static bool need_device(DNvolume* vol, const char* what)
+{
+	if (vol->gpu) return true;
+	dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "%s: this volume has no device state (created with DN_create_volume_cpu)", what);
+	return false;
+}
+
+static bool ensure_slots(DNvolumePriv* p, uint32_t need)
+{
+	if (need <= p->slotCap) return true;
+	uint32_t nc = p->slotCap;
+	while (nc < need) nc *= 2;
+	uint32_t* b = (uint32_t*)DN_REALLOC(p->slotBase, sizeof(uint32_t) * nc);
+	if (b) p->slotBase = b;
+	uint8_t* c = (uint8_t*)DN_REALLOC(p->slotClass, nc);
+	if (c) p->slotClass = c;
+	uint32_t* g = (uint32_t*)DN_REALLOC(p->slotGroups, sizeof(uint32_t) * nc);
+	if (g) p->slotGroups = g;
+	if (!b || !c || !g) {
+		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to grow the slot tables");
+		return false;
+	}
+	int rc = dn_cuda_reserve(p->pub.gpu, nc, 0, 0);
+	if (rc != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "failed to grow the device chunk records: %s", dn_cuda_last_error());
+		return false;
+	}
+	p->slotCap = nc;
+	return true;
+}
+
+bool DN_set_max_voxels_gpu(DNvolume* vol, size_t num)
+{
+	/* voxel.c:1031-1082: grows the device pool keeping its contents */
+	if (num <= vol->voxelCap) return true;
+	if (!need_device(vol, "DN_set_max_voxels_gpu")) return false;
+	int rc = dn_cuda_reserve(vol->gpu, 0, num, 0);
+	if (rc != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "failed to reallocate voxel buffer: %s", dn_cuda_last_error());
+		return false;
+	}
+	vol->voxelCap = num;
+	return true;
+}
+
+bool DN_set_max_lighting_requests(DNvolume* vol, size_t num)
+{
+	/* voxel.c:1084-1096 (request words now live on the device) */
+	if (num <= vol->lightingRequestCap) return true;
+	if (!need_device(vol, "DN_set_max_lighting_requests")) return false;
+	int rc = dn_cuda_reserve(vol->gpu, 0, 0, num);
+	if (rc != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "failed to resize lighting request buffer: %s", dn_cuda_last_error());
+		return false;
+	}
+	vol->lightingRequestCap = num;
+	return true;
+}
+
+static void release_all_slots(DNvolumePriv* p)
+{
+	p->slotNext = 0;
+	p->freeSlots.n = 0;
+	p->poolNext = 0;
+	for (int c = 0; c < NUM_CLASSES; c++) p->freeRanges[c].n = 0;
+	p->groupsStaged = 0;
+	p->stagedChunks = 0;
+	p->deferredSlots.n = 0;
+}
+
+bool DN_set_map_size(DNvolume* vol, DNuvec3 size)
+{
+	/* voxel.c:957-1010.  The device map restarts with every tile absent and
+	 * every existing chunk is re-staged at the next sync (the reference
+	 * re-creates its GPU buffers from the CPU handle array, which leaves
+	 * them in an undefined state). */
+	DNvolumePriv* p = priv(vol);
+	size_t tiles = num_tiles(size);
+	if (tiles == 0 || tiles >= (1u << 28)) {
+		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "invalid map size");
+		return false;
+	}
+	DNchunkHandle* nm = (DNchunkHandle*)DN_MALLOC(sizeof(DNchunkHandle) * tiles);
+	uint8_t* nd = (uint8_t*)DN_MALLOC(tiles);
+	uint32_t* ns = (uint32_t*)DN_MALLOC(sizeof(uint32_t) * tiles);
+	if (!nm || !nd || !ns) {
+		DN_FREE(nm); DN_FREE(nd); DN_FREE(ns);
+		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to reallocate memory for map");
+		return false;
+	}
+	for (uint32_t z = 0; z < size.z; z++)
+	for (uint32_t y = 0; y < size.y; y++)
+	for (uint32_t x = 0; x < size.x; x++) {
+		DNivec3 pos = {(int32_t)x, (int32_t)y, (int32_t)z};
+		size_t ni = DN_FLATTEN_INDEX(pos, size);
+		if (DN_in_map_bounds(vol, pos)) nm[ni] = vol->map[DN_FLATTEN_INDEX(pos, vol->mapSize)];
+		else { nm[ni].flag = 0; nm[ni].chunkIndex = 0; }
+	}
+	int rc = vol->gpu ? dn_cuda_map_resize(vol->gpu, size.x, size.y, size.z) : DN_CUDA_OK;
+	if (rc != DN_CUDA_OK) {
+		DN_FREE(nm); DN_FREE(nd); DN_FREE(ns);
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "failed to reallocate map buffer: %s", dn_cuda_last_error());
+		return false;
+	}
+	DN_FREE(vol->map); DN_FREE(p->dirty); DN_FREE(p->tileSlot);
+	vol->map = nm; p->dirty = nd; p->tileSlot = ns;
+	vol->mapSize = size;
+	for (size_t i = 0; i < vol->chunkCap; i++)
+		if (!DN_in_map_bounds(vol, vol->chunks[i].pos)) clear_chunk(vol, i);
+	memset(p->dirty, 0, tiles);
+	for (size_t i = 0; i < tiles; i++) p->tileSlot[i] = DN_SLOT_NONE;
+	p->dirtyList.n = 0;
+	release_all_slots(p);
+	for (size_t t = 0; t < tiles; t++) if (vol->map[t].flag) mark_dirty(vol, t);
+	return true;
+}
+
+/* ------------------------------------------------------------ map utility */
+
+bool DN_in_map_bounds(DNvolume* vol, DNivec3 pos)
+{
+	return pos.x >= 0 && pos.y >= 0 && pos.z >= 0 &&
+	       (uint32_t)pos.x < vol->mapSize.x && (uint32_t)pos.y < vol->mapSize.y && (uint32_t)pos.z < vol->mapSize.z;
+}
+
+bool DN_in_chunk_bounds(DNivec3 pos)
+{
+	return pos.x < DN_CHUNK_SIZE && pos.y < DN_CHUNK_SIZE && pos.z < DN_CHUNK_SIZE && pos.x >= 0 && pos.y >= 0 && pos.z >= 0;
+}
+
+DNvoxel DN_get_voxel(DNvolume* vol, DNivec3 mapPos, DNivec3 chunkPos)
+{
+	return DN_decompress_voxel(DN_get_compressed_voxel(vol, mapPos, chunkPos));
+}
+
+DNcompressedVoxel DN_get_compressed_voxel(DNvolume* vol, DNivec3 mapPos, DNivec3 chunkPos)
+{
+	/* voxel.c:1116-1119; a tile without a chunk reads as empty instead of a stale chunk */
+	DNchunkHandle h = vol->map[DN_FLATTEN_INDEX(mapPos, vol->mapSize)];
+	if (!h.flag) { DNcompressedVoxel e = {UINT32_MAX, 0}; return e; }
+	return vol->chunks[h.chunkIndex].voxels[chunkPos.x][chunkPos.y][chunkPos.z];
+}
+
+void DN_set_voxel(DNvolume* vol, DNivec3 mapPos, DNivec3 chunkPos, DNvoxel voxel)
+{
+	DN_set_compressed_voxel(vol, mapPos, chunkPos, DN_compress_voxel(voxel));
+}
+
+void DN_set_compressed_voxel(DNvolume* vol, DNivec3 mapPos, DNivec3 chunkPos, DNcompressedVoxel voxel)
+{
+	/* voxel.c:1126-1161 */
+	size_t mapIndex = DN_FLATTEN_INDEX(mapPos, vol->mapSize);
+	if (vol->map[mapIndex].flag == 0) {
+		if (GET_MATERIAL_ID(voxel.normal) == DN_MATERIAL_EMPTY) return;
+		if (DN_add_chunk(vol, mapPos) < 0) return;
+	}
+	uint32_t chunkIndex = vol->map[mapIndex].chunkIndex;
+	DNchunk* c = &vol->chunks[chunkIndex];
+	uint32_t oldMat = GET_MATERIAL_ID(c->voxels[chunkPos.x][chunkPos.y][chunkPos.z].normal);
+	uint32_t newMat = GET_MATERIAL_ID(voxel.normal);
+	if (oldMat == DN_MATERIAL_EMPTY && newMat != DN_MATERIAL_EMPTY)
+		c->numVoxels++;
+	else if (oldMat != DN_MATERIAL_EMPTY && newMat == DN_MATERIAL_EMPTY) {
+		c->numVoxels--;
+		if (c->numVoxels <= 0) {
+			DN_remove_chunk(vol, mapPos);
+			return;
+		}
+	}
+	c->voxels[chunkPos.x][chunkPos.y][chunkPos.z] = voxel;
+	c->updated = 1;
+	mark_dirty(vol, mapIndex);
+}
+
+void DN_remove_voxel(DNvolume* vol, DNivec3 mapPos, DNivec3 chunkPos)
+{
+	/* voxel.c:1163-1182 (a tile without a chunk is left alone instead of editing a stale chunk) */
+	size_t mapIndex = DN_FLATTEN_INDEX(mapPos, vol->mapSize);
+	if (!vol->map[mapIndex].flag) return;
+	uint32_t chunkIndex = vol->map[mapIndex].chunkIndex;
+	if (DN_does_voxel_exist(vol, mapPos, chunkPos)) {
+		vol->chunks[chunkIndex].numVoxels--;
+		if (vol->chunks[chunkIndex].numVoxels <= 0) {
+			DN_remove_chunk(vol, mapPos);
+			return;
+		}
+	}
+	vol->chunks[chunkIndex].voxels[chunkPos.x][chunkPos.y][chunkPos.z].normal = UINT32_MAX;
+	vol->chunks[chunkIndex].updated = 1;
+	mark_dirty(vol, mapIndex);
+}
+
+bool DN_does_chunk_exist(DNvolume* vol, DNivec3 pos)
+{
+	return vol->map[DN_FLATTEN_INDEX(pos, vol->mapSize)].flag >= 1;
+}
+
+bool DN_does_voxel_exist(DNvolume* vol, DNivec3 mapPos, DNivec3 chunkPos)
+{
+	return GET_MATERIAL_ID(DN_get_compressed_voxel(vol, mapPos, chunkPos).normal) != DN_MATERIAL_EMPTY;
+}
+
+#define SIGNF(n) (((n) > 0) ? 1 : (((n) < 0) ? -1 : 0))
+
+bool DN_step_map(DNvolume* vol, DNvec3 rayDir, DNvec3 rayPos, int maxSteps, DNivec3* hitPos, DNvoxel* hitVoxel, DNivec3* hitNormal)
+{
+	/* CPU picking ray, voxel.c:1195-1272: single-level voxel DDA with strict
+	 * '<' ties; the starting side distances are evaluated in double and
+	 * rounded to float, as the reference's expression does. */
+	*hitNormal = (DNivec3){-1000, -1000, -1000};
+	rayPos = DN_vec3_scale(rayPos, (float)DN_CHUNK_SIZE);
+	DNvec3 inv = {{1 / rayDir.x, 1 / rayDir.y, 1 / rayDir.z}};
+	DNvec3 sgn = {{(float)SIGNF(rayDir.x), (float)SIGNF(rayDir.y), (float)SIGNF(rayDir.z)}};
+	DNivec3 pos = {(int32_t)floor(rayPos.x), (int32_t)floor(rayPos.y), (int32_t)floor(rayPos.z)};
+	DNvec3 delta = {{fabsf(inv.x), fabsf(inv.y), fabsf(inv.z)}};
+	DNivec3 step = {(int32_t)sgn.x, (int32_t)sgn.y, (int32_t)sgn.z};
+	DNvec3 side;
+	side.x = (float)(((double)(sgn.x * ((float)pos.x - rayPos.x)) + (double)sgn.x * 0.5 + 0.5) * (double)delta.x);
+	side.y = (float)(((double)(sgn.y * ((float)pos.y - rayPos.y)) + (double)sgn.y * 0.5 + 0.5) * (double)delta.y);
+	side.z = (float)(((double)(sgn.z * ((float)pos.z - rayPos.z)) + (double)sgn.z * 0.5 + 0.5) * (double)delta.z);
+	for (int n = 0; n < maxSteps; n++) {
+		DNivec3 mp, cp;
+		DN_separate_position(pos, &mp, &cp);
+		if (pos.x < 0) mp.x--;
+		if (pos.y < 0) mp.y--;
+		if (pos.z < 0) mp.z--;
+		if (DN_in_map_bounds(vol, mp) && DN_does_chunk_exist(vol, mp) && DN_does_voxel_exist(vol, mp, cp)) {
+			*hitVoxel = DN_get_voxel(vol, mp, cp);
+			*hitPos = pos;
+			return true;
+		}
+		if (side.x < side.y) {
+			if (side.x < side.z) { side.x += delta.x; pos.x += step.x; *hitNormal = (DNivec3){-step.x, 0, 0}; }
+			else { side.z += delta.z; pos.z += step.z; *hitNormal = (DNivec3){0, 0, -step.z}; }
+		} else {
+			if (side.y < side.z) { side.y += delta.y; pos.y += step.y; *hitNormal = (DNivec3){0, -step.y, 0}; }
+			else { side.z += delta.z; pos.z += step.z; *hitNormal = (DNivec3){0, 0, -step.z}; }
+		}
+	}
+	return false;
+}
+
+void DN_separate_position(DNivec3 pos, DNivec3* mapPos, DNivec3* chunkPos)
+{
+	*mapPos = (DNivec3){pos.x / DN_CHUNK_SIZE, pos.y / DN_CHUNK_SIZE, pos.z / DN_CHUNK_SIZE};
+	*chunkPos = (DNivec3){pos.x % DN_CHUNK_SIZE, pos.y % DN_CHUNK_SIZE, pos.z % DN_CHUNK_SIZE};
+}
+
+DNvec3 DN_cam_dir(DNvec3 orient)
+{
+	DNmat3 r = DN_mat4_top_left(DN_mat4_rotate_euler(orient));
+	return DN_mat3_mult_vec3(r, (DNvec3){{0.0f, 0.0f, 1.0f}});
+}
+
+DNcompressedVoxel DN_compress_voxel(DNvoxel voxel)
+{
+	/* voxel.c:1289-1301 */
+	DNcompressedVoxel res;
+	uint32_t nb[3];
+	for (int i = 0; i < 3; i++) {
+		float n = voxel.normal.v[i];
+		n = n < 1.0f ? n : 1.0f;
+		n = n > -1.0f ? n : -1.0f;
+		nb[i] = (uint32_t)(((int)(n * 255.0f) + 255) / 2);
+	}
+	res.normal = ((uint32_t)voxel.material << 24) | (nb[0] << 16) | (nb[1] << 8) | nb[2];
+	res.albedo = ((uint32_t)voxel.albedo.r << 24) | ((uint32_t)voxel.albedo.g << 16) | ((uint32_t)voxel.albedo.b << 8);
+	return res;
+}
+
+DNvoxel DN_decompress_voxel(DNcompressedVoxel voxel)
+{
+	/* voxel.c:1303-1316 */
+	DNvoxel res;
+	const float inv255 = 1.0f / 255.0f;
+	int32_t nx = (int32_t)((voxel.normal >> 16) & 0xFF) * 2 - 255;
+	int32_t ny = (int32_t)((voxel.normal >> 8) & 0xFF) * 2 - 255;
+	int32_t nz = (int32_t)(voxel.normal & 0xFF) * 2 - 255;
+	res.normal.x = (float)nx * inv255;
+	res.normal.y = (float)ny * inv255;
+	res.normal.z = (float)nz * inv255;
+	res.material = (uint8_t)(voxel.normal >> 24);
+	res.albedo.r = (uint8_t)((voxel.albedo >> 24) & 0xFF);
+	res.albedo.g = (uint8_t)((voxel.albedo >> 16) & 0xFF);
+	res.albedo.b = (uint8_t)((voxel.albedo >> 8) & 0xFF);
+	return res;
+}
+
+/* --------------------------------------------------------------- packing */
+
+static inline int face_visible(const DNvolume* vol, const DNchunk* c, int x, int y, int z)
+{
+	/* voxel.c:1391-1394 */
+	if (x < 0 || y < 0 || z < 0 || x >= 8 || y >= 8 || z >= 8) return 1;
+	uint32_t m = GET_MATERIAL_ID(c->voxels[x][y][z].normal);
+	return m == DN_MATERIAL_EMPTY || vol->materials[m].opacity < 1.0f;
+}
+
+/* surface cull + occupancy mask + partial counts + linear albedo (voxel.c:1397-1461);
+ * writes the voxel words (2 per voxel) to out and returns the voxel count */
+static uint32_t pack_chunk(const DNvolume* vol, const DNchunk* c, dn_chunk_record* rec, uint32_t* out)
+{
+	memset(rec->mask, 0, sizeof(rec->mask));
+	memset(rec->partial, 0, sizeof(rec->partial));
+	uint32_t n = 0;
+	for (int z = 0; z < 8; z++)
+	for (int y = 0; y < 8; y++)
+	for (int x = 0; x < 8; x++) {
+		uint32_t idx = (uint32_t)(x + 8 * (y + 8 * z));
+		if (idx == 128 || idx == 256 || idx == 384) rec->partial[(idx >> 7) - 1] = n;
+		uint32_t nw = c->voxels[x][y][z].normal;
+		if (GET_MATERIAL_ID(nw) == DN_MATERIAL_EMPTY) continue;
+		if (!(face_visible(vol, c, x + 1, y, z) || face_visible(vol, c, x - 1, y, z) ||
+		      face_visible(vol, c, x, y + 1, z) || face_visible(vol, c, x, y - 1, z) ||
+		      face_visible(vol, c, x, y, z + 1) || face_visible(vol, c, x, y, z - 1))) continue;
+		rec->mask[idx >> 5] |= 1u << (idx & 31);
+		uint32_t a = c->voxels[x][y][z].albedo;
+		uint32_t r = s_linear[(a >> 24) & 0xFF], g = s_linear[(a >> 16) & 0xFF], b = s_linear[(a >> 8) & 0xFF];
+		out[2 * n] = nw;
+		out[2 * n + 1] = (r << 24) | (g << 16) | (b << 8);
+		n++;
+	}
+	rec->nvox = n;
+	return n;
+}
+
+/* ---------------------------------------------------- slot / range allocator */
+
+static uint32_t class_of(uint32_t nvox)
+{
+	uint32_t c = 0, s = 32;
+	while (s < nvox) { s <<= 1; c++; }
+	return c;
+}
+
+static bool alloc_slot(DNvolumePriv* p, uint32_t nvox, uint32_t* slotOut)
+{
+	uint32_t slot;
+	if (p->freeSlots.n) slot = p->freeSlots.v[--p->freeSlots.n];
+	else {
+		if (!ensure_slots(p, p->slotNext + 1)) return false;
+		slot = p->slotNext++;
+	}
+	uint32_t cls = class_of(nvox);
+	uint64_t base;
+	if (p->freeRanges[cls].n) base = p->freeRanges[cls].v[--p->freeRanges[cls].n];
+	else {
+		uint64_t size = 32ull << cls;
+		if (p->poolNext + size > p->pub.voxelCap) {
+			uint64_t nc = p->pub.voxelCap ? p->pub.voxelCap : 4096;
+			while (p->poolNext + size > nc) nc *= 2;
+			dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_NOTE, "automatically resizing voxel buffer to accomodate %llu GPU voxels (%llu bytes)",
+			       (unsigned long long)nc, (unsigned long long)(nc * 40));
+			if (!DN_set_max_voxels_gpu(&p->pub, nc)) { u32_push(&p->freeSlots, slot); return false; }
+		}
+		base = p->poolNext;
+		p->poolNext += size;
+	}
+	p->slotBase[slot] = (uint32_t)base;
+	p->slotClass[slot] = (uint8_t)cls;
+	p->slotGroups[slot] = (nvox + 31) / 32;
+	p->groupsStaged += p->slotGroups[slot];
+	p->stagedChunks++;
+	*slotOut = slot;
+	return true;
+}
+
+static void free_slot(DNvolumePriv* p, uint32_t slot)
+{
+	u32_push(&p->freeRanges[p->slotClass[slot]], p->slotBase[slot]);
+	u32_push(&p->freeSlots, slot);
+	p->groupsStaged -= p->slotGroups[slot];
+	p->stagedChunks--;
+}
+
+static bool grow_scratch(void** buf, size_t* cap, size_t need, size_t elem)
+{
+	if (need <= *cap) return true;
+	size_t nc = *cap ? *cap : 64;
+	while (nc < need) nc *= 2;
+	void* nb = DN_REALLOC(*buf, nc * elem);
+	if (!nb) return false;
+	*buf = nb; *cap = nc;
+	return true;
+}
+
+/* ---------------------------------------------------------------- sync */
+
+void DN_sync_gpu(DNvolume* vol, DNmemOp op, int lightingSplit)
+{
+	/* DN_sync_gpu, voxel.c:719-786 */
+	DNvolumePriv* p = priv(vol);
+	if (!need_device(vol, "DN_sync_gpu")) return;
+	if (lightingSplit < 1) lightingSplit = 1;
+	vol->frameNum++;
+	if (vol->frameNum >= (uint32_t)lightingSplit) vol->frameNum = 0;
+
+	size_t nd = p->dirtyList.n;
+	if (!grow_scratch((void**)&p->ops, &p->opsCap, nd ? nd : 1, sizeof(dn_tile_op)) ||
+	    !grow_scratch((void**)&p->recs, &p->recsCap, nd ? nd : 1, sizeof(dn_chunk_record)) ||
+	    !grow_scratch((void**)&p->vwords, &p->vwordsCap, (nd ? nd : 1) * 1024, sizeof(uint32_t))) {
+		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to allocate sync scratch");
+		return;
+	}
+	uint32_t nops = 0, nrecs = 0;
+	uint64_t nvw = 0;
+	p->deferredSlots.n = 0;
+	if (op != DN_READ) {
+		for (size_t k = 0; k < nd; k++) {
+			uint32_t t = p->dirtyList.v[k];
+			p->dirty[t] = 0;
+			dn_tile_op* o = &p->ops[nops++];
+			o->tile = t;
+			o->flags = DN_PEND_VALID;
+			o->slot = DN_SLOT_NONE;
+			o->recordIndex = 0;
+			if (p->tileSlot[t] != DN_SLOT_NONE) u32_push(&p->deferredSlots, p->tileSlot[t]);
+			p->tileSlot[t] = DN_SLOT_NONE;
+			if (vol->map[t].flag) {
+				DNchunk* c = &vol->chunks[vol->map[t].chunkIndex];
+				dn_chunk_record* r = &p->recs[nrecs];
+				uint32_t n = pack_chunk(vol, c, r, &p->vwords[nvw]);
+				uint32_t slot;
+				if (!alloc_slot(p, n, &slot)) {
+					dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "failed to stage a chunk on the device");
+					o->flags = DN_PEND_VALID | DN_PEND_EXISTS | (c->updated ? DN_PEND_UPDATED : 0);
+				} else {
+					r->pos[0] = c->pos.x; r->pos[1] = c->pos.y; r->pos[2] = c->pos.z;
+					r->voxBase = p->slotBase[slot];
+					c->numVoxelsGpu = n;
+					o->flags = DN_PEND_VALID | DN_PEND_EXISTS | DN_PEND_STAGED | (c->updated ? DN_PEND_UPDATED : 0);
+					o->slot = slot;
+					o->recordIndex = nrecs;
+					p->tileSlot[t] = slot;
+					nrecs++;
+					nvw += 2ull * n;
+				}
+				c->updated = false;
+			}
+		}
+		p->dirtyList.n = 0;
+	} else {
+		/* DN_READ: the request filter still sees edited chunks as updated (voxel.c:1470) */
+		for (size_t k = 0; k < nd; k++) {
+			uint32_t t = p->dirtyList.v[k];
+			if (vol->map[t].flag && vol->chunks[vol->map[t].chunkIndex].updated) {
+				dn_tile_op* o = &p->ops[nops++];
+				o->tile = t; o->flags = DN_PEND_UPDATED; o->slot = DN_SLOT_NONE; o->recordIndex = 0;
+			}
+		}
+	}
+	if (p->groupsStaged > vol->lightingRequestCap) DN_set_max_lighting_requests(vol, (size_t)p->groupsStaged * 2);
+
+	dn_sync_params sp;
+	sp.op = (uint32_t)op;
+	sp.split = (uint32_t)lightingSplit;
+	sp.frameNum = vol->frameNum;
+	int rc = dn_cuda_sync(vol->gpu, &sp, p->ops, nops, p->recs, nrecs, p->vwords, nvw / 2);
+	if (rc != DN_CUDA_OK)
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "device sync failed: %s", dn_cuda_last_error());
+	/* slots replaced or removed by this sync are reusable by later uploads (stream order) */
+	for (size_t k = 0; k < p->deferredSlots.n; k++) free_slot(p, p->deferredSlots.v[k]);
+	p->deferredSlots.n = 0;
+	vol->numVoxelNodes = (size_t)p->stagedChunks;
+}
+
+/* ------------------------------------------------------------- drawing */
+
+void DN_set_view_projection_matrices(DNvolume* vol, float aspectRatio, float nearPlane, float farPlane, DNmat4* view, DNmat4* projection)
+{
+	/* voxel.c:788-810 */
+	DNmat3 rotate = DN_mat4_top_left(DN_mat4_rotate_euler(vol->camOrient));
+	DNvec3 camFront;
+	float f = 1.0f / tanf(DN_deg_to_rad(vol->camFOV * 0.5f));
+	if (aspectRatio < 1.0f)
+		camFront = DN_mat3_mult_vec3(rotate, (DNvec3){{0.0f, 0.0f, aspectRatio / tanf(DN_deg_to_rad(vol->camFOV * 0.5f))}});
+	else
+		camFront = DN_mat3_mult_vec3(rotate, (DNvec3){{0.0f, 0.0f, f}});
+	*view = DN_mat4_lookat(vol->camPos, DN_vec3_add(vol->camPos, camFront), (DNvec3){{0.0f, 1.0f, 0.0f}});
+	*projection = DN_mat4_perspective(vol->camFOV, 1.0f / aspectRatio, nearPlane, farPlane);
+}
+
+void DN_draw_matrices(DNmat4 view, DNmat4 projection, DNmat4* invView, DNmat4* invCenteredView, DNmat4* invProjection)
+{
+	/* voxel.c:845-853 */
+	DNmat4 centered = view;
+	centered.m[3][0] = 0.0f; centered.m[3][1] = 0.0f; centered.m[3][2] = 0.0f;
+	*invView = DN_mat4_inv(view);
+	*invCenteredView = DN_mat4_inv(centered);
+	*invProjection = DN_mat4_inv(projection);
+}
+
+void DN_draw(DNvolume* vol, DNimage* output, DNmat4 view, DNmat4 projection, int rasterColorTexture, int rasterDepthTexture)
+{
+	/* DN_draw, voxel.c:812-881 */
+	if (!need_device(vol, "DN_draw")) return;
+	if (!output || !output->color || output->width == 0 || output->height == 0) {
+		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_ERROR, "DN_draw: invalid output image");
+		return;
+	}
+	if (rasterColorTexture >= 0 && rasterDepthTexture >= 0)
+		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_NOTE, "raster composition is not available; drawing without it");
+	if (vol->useCubemap)
+		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_NOTE, "cube-map sky is not available; using the sky gradient");
+	DNmat4 iv, icv, ip;
+	DN_draw_matrices(view, projection, &iv, &icv, &ip);
+	DNmat4 M = DN_mat4_mult(icv, ip);
+	dn_draw_params dp;
+	memset(&dp, 0, sizeof(dp));
+	for (int r = 0; r < 3; r++)
+		dp.origin[r] = iv.m[0][r] * 0.0f + iv.m[1][r] * 0.0f + iv.m[2][r] * 0.0f + iv.m[3][r] * 1.0f;
+	memcpy(dp.dirMat, M.m, sizeof(dp.dirMat));
+	dp.width = output->width;
+	dp.height = output->height;
+	dp.viewMode = vol->camViewMode;
+	dp.truncate16 = vol->truncateDispatch;
+	memcpy(dp.sunStrength, vol->sunStrength.v, 12);
+	memcpy(dp.skyBot, vol->skyGradientBot.v, 12);
+	memcpy(dp.skyTop, vol->skyGradientTop.v, 12);
+	dp.emissiveStrength = vol->emissiveStrength;
+	int rc = output->onDevice
+		? dn_cuda_draw(vol->gpu, &dp, (const dn_material*)vol->materials, output->color, output->hitIndex, output->hitFace)
+		: dn_cuda_draw_host(vol->gpu, &dp, (const dn_material*)vol->materials, output->color, output->hitIndex, output->hitFace);
+	if (rc != DN_CUDA_OK)
+		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_ERROR, "draw failed: %s", dn_cuda_last_error());
+}
+
+static void sphere_points(uint32_t K, float out[64][3])
+{
+	/* golden-angle Fibonacci sphere: y_k = 1 - 2k/(K-1), theta_k = k*pi*(3-sqrt(5)) */
+	const double ga = 3.14159265358979323846 * (3.0 - sqrt(5.0));
+	for (uint32_t k = 0; k < K; k++) {
+		double y = (K > 1) ? 1.0 - 2.0 * (double)k / (double)(K - 1) : 1.0;
+		double r = sqrt(fmax(0.0, 1.0 - y * y));
+		double th = ga * (double)k;
+		out[k][0] = (float)(cos(th) * r);
+		out[k][1] = (float)y;
+		out[k][2] = (float)(sin(th) * r);
+	}
+}
+
+void DN_update_lighting(DNvolume* vol, int numDiffuseSamples, int maxDiffuseSamples, float time)
+{
+	/* DN_update_lighting, voxel.c:883-952 */
+	DNvolumePriv* p = priv(vol);
+	if (!need_device(vol, "DN_update_lighting")) return;
+	if (vol->frameNum == 0) vol->lastTime = time;
+	dn_light_params lp;
+	memset(&lp, 0, sizeof(lp));
+	DNvec3 sd = DN_vec3_normalize(vol->sunDir);
+	memcpy(lp.sunDir, sd.v, 12);
+	memcpy(lp.sunStrength, vol->sunStrength.v, 12);
+	memcpy(lp.ambient, vol->ambientLightStrength.v, 12);
+	memcpy(lp.camPos, vol->camPos.v, 12);
+	memcpy(lp.skyBot, vol->skyGradientBot.v, 12);
+	memcpy(lp.skyTop, vol->skyGradientTop.v, 12);
+	lp.shadowSoftness = vol->shadowSoftness;
+	lp.time = vol->lastTime;
+	lp.emissiveStrength = vol->emissiveStrength;
+	lp.numDiffuse = numDiffuseSamples > 0 ? (uint32_t)numDiffuseSamples : 0u;
+	lp.maxDiffuse = maxDiffuseSamples > 0 ? (uint32_t)maxDiffuseSamples : 0u;
+	lp.diffuseBounceLimit = vol->diffuseBounceLimit;
+	lp.specBounceLimit = vol->specBounceLimit;
+	uint32_t K = vol->numDirectRays;
+	if (K < 1) K = 1;
+	if (K > 64) K = 64;
+	lp.K = K;
+	lp.rngMode = vol->rngMode;
+	lp.mapId = vol->mapId;
+	if (!p->sphereValid || p->sphereK != (float)K) {
+		sphere_points(K, p->spherePts);
+		p->sphereK = (float)K;
+		p->sphereValid = 1;
+	}
+	memcpy(lp.spherePts, p->spherePts, sizeof(lp.spherePts));
+	int rc = dn_cuda_light(vol->gpu, &lp, (const dn_material*)vol->materials);
+	if (rc != DN_CUDA_OK)
+		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_ERROR, "lighting update failed: %s", dn_cuda_last_error());
+}
+
+/* ----------------------------------------------------------- additions */
+
+bool DN_finish(DNvolume* vol)
+{
+	if (!need_device(vol, "DN_finish")) return false;
+	uint64_t nreq = 0;
+	int rc = dn_cuda_finish(vol->gpu, &nreq);
+	vol->numLightingRequests = (size_t)nreq;
+	if (rc != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_ERROR, "device work failed: %s", dn_cuda_last_error());
+		return false;
+	}
+	return true;
+}
+
+DNimage* DN_image_create(uint32_t width, uint32_t height, int onDevice, int withHitInfo)
+{
+	DNimage* img = (DNimage*)DN_MALLOC(sizeof(DNimage));
+	if (!img) return NULL;
+	memset(img, 0, sizeof(*img));
+	img->width = width; img->height = height; img->onDevice = onDevice ? 1 : 0;
+	size_t n = (size_t)width * height;
+	int rc;
+	if (onDevice) {
+		rc = dn_cuda_malloc((void**)&img->color, n * 16);
+		if (rc == DN_CUDA_OK && withHitInfo) rc = dn_cuda_malloc((void**)&img->hitIndex, n * 4);
+		if (rc == DN_CUDA_OK && withHitInfo) rc = dn_cuda_malloc((void**)&img->hitFace, n);
+	} else {
+		rc = dn_cuda_malloc_host((void**)&img->color, n * 16);
+		if (rc == DN_CUDA_OK && withHitInfo) rc = dn_cuda_malloc_host((void**)&img->hitIndex, n * 4);
+		if (rc == DN_CUDA_OK && withHitInfo) rc = dn_cuda_malloc_host((void**)&img->hitFace, n);
+	}
+	if (rc != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "failed to allocate an image: %s", dn_cuda_last_error());
+		DN_image_destroy(img);
+		return NULL;
+	}
+	return img;
+}
+
+void DN_image_destroy(DNimage* img)
+{
+	if (!img) return;
+	if (img->onDevice) { dn_cuda_free(img->color); dn_cuda_free(img->hitIndex); dn_cuda_free(img->hitFace); }
+	else { dn_cuda_free_host(img->color); dn_cuda_free_host(img->hitIndex); dn_cuda_free_host(img->hitFace); }
+	DN_FREE(img);
+}
+
+bool DN_get_stats(DNvolume* vol, DNstats* out)
+{
+	if (!need_device(vol, "DN_get_stats")) return false;
+	dn_stats s;
+	if (dn_cuda_stats(vol->gpu, &s) != DN_CUDA_OK) return false;
+	out->rays = s.rays; out->primaryRays = s.primary; out->outerSteps = s.outerSteps;
+	out->chunksEntered = s.chunksEntered; out->innerSteps = s.innerSteps; out->hits = s.hits;
+	out->litVoxels = s.litVoxels;
+	return true;
+}
+
+void DN_reset_stats(DNvolume* vol) { if (vol->gpu) dn_cuda_reset_stats(vol->gpu); }
+
+size_t DN_export_lighting(DNvolume* vol, uint32_t* index, float* diffuse, float* specular, size_t capacity)
+{
+	uint64_t n = 0;
+	if (!need_device(vol, "DN_export_lighting")) return 0;
+	if (dn_cuda_export_lighting(vol->gpu, index, diffuse, specular, capacity, &n) != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "lighting export failed: %s", dn_cuda_last_error());
+		return 0;
+	}
+	return (size_t)n;
+}
+
+bool DN_export_tiles(DNvolume* vol, uint8_t* state, uint8_t* visible, uint32_t* lastUsed, uint32_t* samples)
+{
+	if (!need_device(vol, "DN_export_tiles")) return false;
+	return dn_cuda_export_tiles(vol->gpu, state, visible, lastUsed, samples) == DN_CUDA_OK;
+}
+
+size_t DN_export_requests(DNvolume* vol, uint32_t* out, size_t capacity)
+{
+	uint64_t n = 0;
+	if (!need_device(vol, "DN_export_requests")) return 0;
+	if (dn_cuda_export_requests(vol->gpu, out, capacity, &n) != DN_CUDA_OK) return 0;
+	return (size_t)n;
+}
+
+/* addition: struct sizes and field offsets, for language bindings that mirror these structs */
+size_t DN_abi_layout(uint64_t* out, size_t n)
+{
+	const uint64_t v[] = {
+		sizeof(DNvolume), offsetof(DNvolume, mapSize), offsetof(DNvolume, map), offsetof(DNvolume, chunks),
+		offsetof(DNvolume, materials), offsetof(DNvolume, camPos), offsetof(DNvolume, sunDir),
+		offsetof(DNvolume, useCubemap), offsetof(DNvolume, frameNum), offsetof(DNvolume, emissiveStrength),
+		offsetof(DNvolume, deviceBudgetBytes), sizeof(DNchunk), sizeof(DNmaterial), sizeof(DNimage),
+		sizeof(DNchunkHandle), sizeof(DNstats), offsetof(DNchunk, voxels), sizeof(DNvoxel)
+	};
+	size_t k = sizeof(v) / sizeof(v[0]);
+	for (size_t i = 0; i < n && i < k; i++) out[i] = v[i];
+	return k;
+}

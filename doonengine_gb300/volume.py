@@ -1,0 +1,236 @@
+"""Python mirror of the DN_* API: a thin object wrapper over libdoonengine.so for tests, benchmarks and
+tools.  Every call goes through the C ABI; nothing here computes lighting or traverses rays."""
+import ctypes
+from ctypes import POINTER, byref, c_float, c_uint8, c_uint32, c_uint64, c_void_p
+
+import numpy as np
+
+from . import _lib as L
+
+DN_READ, DN_WRITE, DN_READ_WRITE = 0, 1, 2
+
+_callback_keepalive = []
+_messages = []
+
+
+def install_message_callback(store=True, echo=False):
+    """Set g_DN_message_callback to collect (type, severity, text) tuples in ``messages()``."""
+    lib = L.load()
+
+    def cb(t, s, m):
+        txt = m.decode(errors="replace") if m else ""
+        if store:
+            _messages.append((t, s, txt))
+        if echo:
+            print("[DN %d/%d] %s" % (t, s, txt))
+
+    f = L.MESSAGE_CALLBACK(cb)
+    _callback_keepalive.append(f)
+    ptr = ctypes.c_void_p.in_dll(lib, "g_DN_message_callback")
+    ptr.value = ctypes.cast(f, ctypes.c_void_p).value
+    return f
+
+
+def messages():
+    return _messages
+
+
+def init():
+    lib = L.load()
+    if not lib.DN_init():
+        raise RuntimeError("DN_init failed: %s" % lib.dn_cuda_last_error().decode())
+    return lib
+
+
+def mat_to_np(m):
+    """DNmat4 -> 4x4 numpy array indexed [col][row]."""
+    return np.array([[m.m[c][r] for r in range(4)] for c in range(4)], dtype=np.float32)
+
+
+class Image:
+    """A DNimage (device or pinned host memory)."""
+
+    def __init__(self, width, height, on_device=True, hit_info=True):
+        self.lib = L.load()
+        self.ptr = self.lib.DN_image_create(width, height, 1 if on_device else 0, 1 if hit_info else 0)
+        if not self.ptr:
+            raise RuntimeError("DN_image_create failed")
+        self.width, self.height, self.on_device = width, height, on_device
+
+    def close(self):
+        if self.ptr:
+            self.lib.DN_image_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def numpy(self):
+        """(color [h,w,4] float32, hit [h,w] uint32, face [h,w] uint8) copied to the host."""
+        n = self.width * self.height
+        img = self.ptr.contents
+        color = np.empty((self.height, self.width, 4), np.float32)
+        hit = np.empty((self.height, self.width), np.uint32)
+        face = np.empty((self.height, self.width), np.uint8)
+        if self.on_device:
+            self.lib.dn_cuda_memcpy_d2h(color.ctypes.data, ctypes.cast(img.color, c_void_p), n * 16)
+            if img.hitIndex:
+                self.lib.dn_cuda_memcpy_d2h(hit.ctypes.data, ctypes.cast(img.hitIndex, c_void_p), n * 4)
+            if img.hitFace:
+                self.lib.dn_cuda_memcpy_d2h(face.ctypes.data, ctypes.cast(img.hitFace, c_void_p), n)
+        else:
+            ctypes.memmove(color.ctypes.data, img.color, n * 16)
+            if img.hitIndex:
+                ctypes.memmove(hit.ctypes.data, img.hitIndex, n * 4)
+            if img.hitFace:
+                ctypes.memmove(face.ctypes.data, img.hitFace, n)
+        return color, hit, face
+
+
+class Volume:
+    """Owns one DNvolume."""
+
+    def __init__(self, map_size, min_chunks=256, cpu_only=False, _ptr=None):
+        self.lib = L.load()
+        if _ptr is not None:
+            self.ptr = _ptr
+        else:
+            ms = L.DNuvec3(*map_size)
+            self.ptr = (self.lib.DN_create_volume_cpu if cpu_only else self.lib.DN_create_volume)(ms, min_chunks)
+        if not self.ptr:
+            raise RuntimeError("DN_create_volume failed: %s" % self.lib.dn_cuda_last_error().decode())
+
+    @classmethod
+    def load(cls, path, min_chunks=256):
+        lib = L.load()
+        p = lib.DN_load_volume(path.encode(), min_chunks)
+        if not p:
+            raise RuntimeError("DN_load_volume failed for %s" % path)
+        return cls(None, _ptr=p)
+
+    def save(self, path):
+        return bool(self.lib.DN_save_volume(path.encode(), self.ptr))
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            self.lib.DN_delete_volume(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def s(self):
+        return self.ptr.contents
+
+    @property
+    def map_size(self):
+        m = self.s.mapSize
+        return (m.x, m.y, m.z)
+
+    @property
+    def num_tiles(self):
+        x, y, z = self.map_size
+        return x * y * z
+
+    # ---- edits
+    def set_voxel(self, mp, cp, material, normal, albedo):
+        v = L.DNvoxel(material, L.DNvec3(*normal), L.DNcolor(*albedo))
+        self.lib.DN_set_voxel(self.ptr, L.DNivec3(*mp), L.DNivec3(*cp), v)
+
+    def set_compressed(self, mp, cp, normal_word, albedo_word):
+        self.lib.DN_set_compressed_voxel(self.ptr, L.DNivec3(*mp), L.DNivec3(*cp), L.DNcompressedVoxel(normal_word, albedo_word))
+
+    def remove_voxel(self, mp, cp):
+        self.lib.DN_remove_voxel(self.ptr, L.DNivec3(*mp), L.DNivec3(*cp))
+
+    def get_compressed(self, mp, cp):
+        c = self.lib.DN_get_compressed_voxel(self.ptr, L.DNivec3(*mp), L.DNivec3(*cp))
+        return c.normal, c.albedo
+
+    def set_material(self, i, emissive=0, opacity=1.0, refract=1.0, specular=0.0, reflect_type=0, shininess=1):
+        m = self.s.materials[i]
+        m.emissive, m.opacity, m.refractIndex = emissive, opacity, refract
+        m.specular, m.reflectType, m.shininess = specular, reflect_type, shininess
+
+    def nonempty_chunks(self):
+        return sum(1 for t in range(self.num_tiles) if self.s.map[t].flag)
+
+    # ---- frame
+    def view_proj(self, aspect, near=0.1, far=100.0):
+        v, p = L.DNmat4(), L.DNmat4()
+        self.lib.DN_set_view_projection_matrices(self.ptr, aspect, near, far, byref(v), byref(p))
+        return v, p
+
+    def draw(self, image, view, proj):
+        self.lib.DN_draw(self.ptr, image.ptr, view, proj, -1, -1)
+
+    def sync(self, op=DN_READ_WRITE, split=1):
+        self.lib.DN_sync_gpu(self.ptr, op, split)
+
+    def update_lighting(self, num_diffuse=1, max_diffuse=1000, time=0.0):
+        self.lib.DN_update_lighting(self.ptr, num_diffuse, max_diffuse, time)
+
+    def finish(self):
+        return bool(self.lib.DN_finish(self.ptr))
+
+    def stats(self):
+        s = L.DNstats()
+        if not self.lib.DN_get_stats(self.ptr, byref(s)):
+            raise RuntimeError("DN_get_stats failed: %s" % self.lib.dn_cuda_last_error().decode())
+        return {k: int(getattr(s, k)) for k, _ in L.DNstats._fields_}
+
+    def reset_stats(self):
+        self.lib.DN_reset_stats(self.ptr)
+
+    def export_lighting(self):
+        n = self.lib.DN_export_lighting(self.ptr, None, None, None, 0)
+        idx = np.empty(n, np.uint32)
+        diff = np.empty((n, 3), np.float32)
+        spec = np.empty((n, 3), np.float32)
+        if n:
+            got = self.lib.DN_export_lighting(self.ptr, idx.ctypes.data_as(POINTER(c_uint32)),
+                                              diff.ctypes.data_as(POINTER(c_float)), spec.ctypes.data_as(POINTER(c_float)), n)
+            assert got == n
+        return idx, diff, spec
+
+    def export_tiles(self):
+        n = self.num_tiles
+        st = np.empty(n, np.uint8)
+        vis = np.empty(n, np.uint8)
+        lu = np.empty(n, np.uint32)
+        ns = np.empty(n, np.uint32)
+        ok = self.lib.DN_export_tiles(self.ptr, st.ctypes.data_as(POINTER(c_uint8)), vis.ctypes.data_as(POINTER(c_uint8)),
+                                      lu.ctypes.data_as(POINTER(c_uint32)), ns.ctypes.data_as(POINTER(c_uint32)))
+        if not ok:
+            raise RuntimeError("DN_export_tiles failed: %s" % self.lib.dn_cuda_last_error().decode())
+        return st, vis, lu, ns
+
+    def export_requests(self):
+        n = self.lib.DN_export_requests(self.ptr, None, 0)
+        out = np.empty(max(n, 1), np.uint32)
+        if n:
+            self.lib.DN_export_requests(self.ptr, out.ctypes.data_as(POINTER(c_uint32)), n)
+        return out[:n]
+
+    def stream(self):
+        return self.lib.dn_cuda_stream(self.s.gpu)
+
+    # ---- scenes
+    def palette(self, seed, n_materials=16, n_emissive=2, albedo_lo=0.1, albedo_hi=0.9, spec_max=0.5):
+        self.lib.dn_scene_palette(self.ptr, seed, n_materials, n_emissive, albedo_lo, albedo_hi, spec_max)
+
+    def terrain(self, seed, mean_frac, amp_frac, n_materials=16, n_emissive=2):
+        self.lib.dn_scene_terrain(self.ptr, seed, mean_frac, amp_frac, n_materials, n_emissive)
+
+    def shapes(self, seed, n, min_size, max_size, n_materials=14, y_lo=0.0, y_hi=0.5):
+        self.lib.dn_scene_shapes(self.ptr, seed, n, min_size, max_size, n_materials, y_lo, y_hi)
+
+    def camera(self, fx, fy, fz, pitch, yaw, fov=90.0):
+        self.lib.dn_scene_camera(self.ptr, fx, fy, fz, pitch, yaw, fov)

@@ -1,0 +1,162 @@
+/*
+ * dn_cuda.h -- the C ABI between the DN_* host layer and the CUDA kernels
+ * (libdoonengine.so).  Plain C types, pointers and sizes only; every entry
+ * returns an int status (DN_CUDA_OK = 0) and no exception crosses it.
+ *
+ * In the reference these operations are OpenGL calls made from
+ * src/DoonEngine/voxel.c; each entry below names the call sites it replaces.
+ * The device state of one map is an opaque struct DNgpuVolume.
+ */
+#ifndef DN_CUDA_H
+#define DN_CUDA_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+struct DNgpuVolume;
+
+enum {
+    DN_CUDA_OK = 0,
+    DN_CUDA_ERR_ARG = 1,        /* bad argument (size, NULL, out of range) */
+    DN_CUDA_ERR_NOMEM = 2,      /* device or pinned allocation failed */
+    DN_CUDA_ERR_LAUNCH = 3,     /* kernel launch / CUDA runtime error */
+    DN_CUDA_ERR_DEVICE = 4,     /* no usable GPU */
+    DN_CUDA_ERR_KERNEL = 5,     /* a kernel flagged an error status */
+    DN_CUDA_ERR_CAPACITY = 6    /* fixed-size scratch too small for the request */
+};
+
+#define DN_SLOT_NONE 0x3FFFFFFFu
+
+/* material as uploaded with every draw / lighting launch (voxel.h:82-94, 32 B) */
+typedef struct dn_material {
+    float padding[2];
+    uint32_t emissive;
+    float opacity, refractIndex, specular;
+    uint32_t reflectType, shininess;
+} dn_material;
+
+/* one packed chunk (output of the host packing, voxel.c:1397-1461) */
+typedef struct dn_chunk_record {
+    uint32_t mask[16];      /* bit x + 8*(y + 8*z) */
+    uint32_t partial[3];    /* set bits before 128, 256, 384 */
+    uint32_t nvox;          /* set bits */
+    int32_t pos[3];         /* chunk position in the map */
+    uint32_t voxBase;       /* first voxel in the device pool */
+} dn_chunk_record;
+
+/* per-tile pending operation decided by the host at sync (voxel.c:1491-1536) */
+#define DN_PEND_VALID   0x1u   /* the entry carries CPU-side state for the tile */
+#define DN_PEND_EXISTS  0x2u   /* the chunk exists on the CPU (DNchunkHandle.flag != 0) */
+#define DN_PEND_UPDATED 0x4u   /* DNchunk.updated was set */
+#define DN_PEND_STAGED  0x8u   /* a freshly packed record was staged into 'slot' */
+typedef struct dn_tile_op {
+    uint32_t tile;
+    uint32_t flags;
+    uint32_t slot;          /* record slot of the staged chunk (DN_PEND_STAGED) */
+    uint32_t recordIndex;   /* index into the records array of the same call */
+} dn_tile_op;
+
+typedef struct dn_sync_params {
+    uint32_t op;            /* 0 DN_READ, 1 DN_WRITE, 2 DN_READ_WRITE */
+    uint32_t split;         /* lightingSplit >= 1 */
+    uint32_t frameNum;
+} dn_sync_params;
+
+typedef struct dn_light_params {
+    float sunDir[3];        /* normalised (voxel.c:942) */
+    float sunStrength[3], ambient[3], camPos[3], skyBot[3], skyTop[3];
+    float shadowSoftness, time, emissiveStrength;
+    uint32_t numDiffuse, maxDiffuse, diffuseBounceLimit, specBounceLimit;
+    uint32_t K;             /* direct / specular rays, 1..64 */
+    uint32_t rngMode;       /* 0 hash, 1 sin-fract */
+    uint32_t mapId;
+    float spherePts[64][3];
+} dn_light_params;
+
+typedef struct dn_draw_params {
+    float origin[3];        /* invView * (0,0,0,1) */
+    float dirMat[4][4];     /* invCenteredView * invProjection, column-major */
+    uint32_t width, height, viewMode, truncate16;
+    float sunStrength[3], skyBot[3], skyTop[3];
+    float emissiveStrength;
+} dn_draw_params;
+
+typedef struct dn_stats {
+    uint64_t rays, primary, outerSteps, chunksEntered, innerSteps, hits, litVoxels;
+} dn_stats;
+
+/* --- device lifetime: replaces DN_init's buffer / program setup (voxel.c:119-154) and DN_quit (156-163) --- */
+int dn_cuda_init(int device);
+void dn_cuda_shutdown(void);
+const char* dn_cuda_error_string(int code);
+/* last detailed error message of this thread */
+const char* dn_cuda_last_error(void);
+
+/* --- map lifetime: replaces the SSBO creation of DN_create_volume (voxel.c:173-195) and glDeleteBuffers (285-287) --- */
+int dn_cuda_map_create(uint32_t sx, uint32_t sy, uint32_t sz, uint32_t slotCap, uint64_t voxelCap,
+                       struct DNgpuVolume** out);
+void dn_cuda_map_destroy(struct DNgpuVolume* g);
+/* re-creates the tile arrays for a new map size, every tile absent (DN_set_map_size, voxel.c:989-1007) */
+int dn_cuda_map_resize(struct DNgpuVolume* g, uint32_t sx, uint32_t sy, uint32_t sz);
+/* grows the record slots / voxel pool / request capacity, keeping contents
+ * (DN_set_max_voxels_gpu voxel.c:1042-1061; request buffer voxel.c:898-916) */
+int dn_cuda_reserve(struct DNgpuVolume* g, uint32_t slotCap, uint64_t voxelCap, uint64_t requestCap);
+
+/* --- sync: replaces glMapBuffer of the map buffer and the per-tile host loop of DN_sync_gpu
+ *     (voxel.c:729-770), the request build (1463-1489), the chunk / voxel uploads
+ *     (1548-1552, 1636-1637) and the request upload of DN_update_lighting (919).
+ *     ops: pending per-tile CPU-side state; records: packed chunks for the staged ops;
+ *     voxels: 2 words per voxel, record r's voxels at voxels[2*records[r].voxBase ...] are
+ *     taken from 'voxelWords' in record order (concatenated). --- */
+int dn_cuda_sync(struct DNgpuVolume* g, const dn_sync_params* p,
+                 const dn_tile_op* ops, uint32_t nops,
+                 const dn_chunk_record* records, uint32_t nrecords,
+                 const uint32_t* voxelWords, uint64_t nvoxels);
+
+/* --- lighting: replaces glDispatchCompute(numLightingRequests) of DN_update_lighting (voxel.c:950) --- */
+int dn_cuda_light(struct DNgpuVolume* g, const dn_light_params* p, const dn_material* materials);
+
+/* --- draw: replaces glDispatchCompute(w/16, h/16) of DN_draw (voxel.c:879); outputs are device pointers --- */
+int dn_cuda_draw(struct DNgpuVolume* g, const dn_draw_params* p, const dn_material* materials,
+                 float* colorOut, uint32_t* hitOut, uint8_t* faceOut);
+/* draw into host memory: device staging plus asynchronous copies; valid after dn_cuda_finish */
+int dn_cuda_draw_host(struct DNgpuVolume* g, const dn_draw_params* p, const dn_material* materials,
+                      float* colorOut, uint32_t* hitOut, uint8_t* faceOut);
+
+/* --- synchronisation, counters, introspection (additions) --- */
+int dn_cuda_finish(struct DNgpuVolume* g, uint64_t* numRequests);
+int dn_cuda_stats(struct DNgpuVolume* g, dn_stats* out);
+int dn_cuda_reset_stats(struct DNgpuVolume* g);
+void* dn_cuda_stream(struct DNgpuVolume* g);
+int dn_cuda_export_tiles(struct DNgpuVolume* g, uint8_t* state, uint8_t* vis, uint32_t* lastUsed, uint32_t* samples);
+int dn_cuda_export_requests(struct DNgpuVolume* g, uint32_t* out, uint64_t capacity, uint64_t* count);
+/* lighting of every loaded chunk; rows ordered by tile then rank */
+int dn_cuda_export_lighting(struct DNgpuVolume* g, uint32_t* index, float* diff, float* spec,
+                            uint64_t capacity, uint64_t* count);
+
+/* device / pinned memory and event helpers for callers without their own CUDA runtime */
+int dn_cuda_malloc(void** p, size_t bytes);
+int dn_cuda_free(void* p);
+int dn_cuda_malloc_host(void** p, size_t bytes);
+int dn_cuda_free_host(void* p);
+int dn_cuda_memcpy_d2h(void* dst, const void* src, size_t bytes);
+int dn_cuda_memcpy_h2d(void* dst, const void* src, size_t bytes);
+int dn_cuda_event_create(void** ev);
+int dn_cuda_event_destroy(void* ev);
+int dn_cuda_event_record(void* ev, void* stream);
+int dn_cuda_event_elapsed_ms(void* start, void* end, float* ms);
+int dn_cuda_stream_sync(void* stream);
+int dn_cuda_device_sync(void);
+/* writes 'bytes' of a scratch buffer on 'stream' (L2 flush between timed steps) */
+int dn_cuda_flush_l2(void* stream, size_t bytes);
+/* names of the kernels this library launches, ';'-separated */
+const char* dn_cuda_kernel_names(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,223 @@
+/*
+ * dn_oracle.h -- CPU oracle for the DoonEngine per-voxel lighting + draw path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference's
+ * GLSL compute shaders (assets/shaders/voxelShared.comp, voxelLighting.comp,
+ * voxelDraw.comp) and of the host-side packing / sync logic in
+ * src/DoonEngine/voxel.c.  It is the checker that the CUDA path is compared
+ * against and the timed CPU baseline; the product library never links,
+ * loads or calls it.
+ *
+ * Parity status: the reference has no tests and its hot path exists only as
+ * GLSL, which cannot run on these machines.  The host-side pieces (voxel
+ * codec, chunk packing, camera, CPU picking ray) are pinned against the
+ * reference's own C compiled from its sources (oracle/ref/).  The shader
+ * transcription is pinned by running the reference shader text itself as
+ * C++ through a GLSL shim (oracle/ref/glsl_pin), in the reference-faithful
+ * RNG mode.
+ *
+ * Deterministic semantics where the reference races or is undefined
+ * (numbered D1..D15, each applied identically here and in the kernels):
+ *   D1  lighting reads the previous frame's committed lighting; results are
+ *       committed after the whole launch (reference reads/writes in place,
+ *       voxelLighting.comp:113,122 vs 276-278).
+ *   D2  the per-chunk sample count is read once per launch and incremented
+ *       after it (voxelLighting.comp:224 vs 284-285).
+ *   D3  FP32 lighting accumulators (reference quantises to 8/16 bit,
+ *       voxelLighting.comp:266-278).
+ *   D4  visible / requested / touched are per-tile bytes written with
+ *       idempotent stores; visible is cleared when a chunk is taken into the
+ *       lighting request list; "touched" (lastUsed = 0) is recorded when a
+ *       ray enters a loaded chunk (voxelShared.comp:143-144, 464;
+ *       voxelDraw.comp:121; voxelLighting.comp:104-105, 281).
+ *   D5  RNG mode B (default): integer hash of (map, voxel, seed, stream,
+ *       index); mode A: the reference's fract(sin(s)*43758.5453) with a
+ *       project-written deterministic sine (voxelLighting.comp:29-57).
+ *   D6  rand_unit_sphere gives up after 64 tries and returns (0,0,0)
+ *       (voxelLighting.comp:47-57 loops without bound).
+ *   D7  the draw covers every pixel; a flag emulates the reference's
+ *       w/16 x h/16 dispatch truncation (voxel.c:879).
+ *   D8  direct light = mean of K fixed shadow rays along
+ *       normalize(sunDir*softness + P_k) (P_k: K-point golden-angle sphere),
+ *       traced once per voxel and added once per diffuse sample; on the first
+ *       sample one ray along sunDir+EPS (voxelLighting.comp:65-80).  Specular
+ *       uses the same K points (voxelLighting.comp:23, 244-250).
+ *   D9  emissive hits are scaled by a volume-wide emissive strength
+ *       (1.0 = reference; voxelLighting.comp:117,189; voxelDraw.comp:44).
+ *   D10 device voxels are two 32-bit words: the reference's packed normal
+ *       word (material<<24 | n.x<<16 | n.y<<8 | n.z) and the linearised albedo
+ *       word (voxel.c:1438-1452).
+ *   D11 no FMA contraction; IEEE division and square root; GLSL built-ins
+ *       (min, max, clamp, mix, reflect, refract, normalize, sign, fract) follow
+ *       their specification formulas.
+ *   D12 the sky gradient keeps the reference's y*0.5+1 parameter
+ *       (voxelShared.comp:294).
+ *   D13 refraction only in the draw (voxelDraw.comp:65).  The transparency
+ *       state (lastVoxID / lastVoxRefract, voxelShared.comp:321-325) starts
+ *       fresh for every primary ray and every lighting ray job (one shadow
+ *       ray, one specular ray with its bounces, one diffuse path with its
+ *       bounces); the reference carries it across all rays of one shader
+ *       invocation, which makes results depend on ray order.  Mode
+ *       DNO_PERSIST_TRANSPARENCY restores the reference behaviour (pinning
+ *       only).
+ *   D14 face code from the hit normal: 0 +x, 1 -x, 2 +y, 3 -y, 4 +z, 5 -z,
+ *       6 none; hit index = global voxel coordinate x + X*(y + Y*z) in voxels,
+ *       0xFFFFFFFF on a miss.
+ *   D15 the GLSL <= multi-axis tie step (voxelShared.comp:313) is
+ *       authoritative; the CPU picking ray keeps its own strict < (voxel.c:1241).
+ */
+#ifndef DN_ORACLE_H
+#define DN_ORACLE_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- layouts of the reference's public CPU-side structs (voxel.h:35-94) ---- */
+
+typedef struct dno_cvoxel { uint32_t normal, albedo; } dno_cvoxel;      /* DNcompressedVoxel */
+
+typedef struct dno_chunk {                                               /* DNchunk */
+    int32_t pos[3];
+    uint8_t updated;
+    uint32_t numVoxels;
+    uint32_t numVoxelsGpu;
+    dno_cvoxel voxels[8][8][8];   /* [x][y][z] */
+} dno_chunk;
+
+typedef struct dno_handle { uint8_t flag; uint32_t chunkIndex; } dno_handle;   /* DNchunkHandle */
+
+typedef struct dno_material {                                            /* DNmaterial (std140, 32 B) */
+    float padding[2];
+    uint32_t emissive;
+    float opacity;
+    float refractIndex;
+    float specular;
+    uint32_t reflectType;
+    uint32_t shininess;
+} dno_material;
+
+/* ---- packed chunk (restatement of _DN_chunk_to_gpu, voxel.c:1397-1461) ---- */
+typedef struct dno_packed {
+    uint32_t mask[16];
+    uint32_t partial[3];
+    uint32_t nvox;
+    uint32_t vox[512][2];         /* [normal word, linear albedo word] */
+} dno_packed;
+
+void dno_pack_chunk(const dno_chunk* chunk, const dno_material* materials, dno_packed* out);
+
+/* voxel codec restatements (voxel.c:1289-1316) */
+void dno_compress_voxel(uint8_t material, const float normal[3], const uint8_t albedo[3], dno_cvoxel* out);
+void dno_decompress_voxel(dno_cvoxel v, uint8_t* material, float normal[3], uint8_t albedo[3]);
+
+/* ---- oracle map state: the device-side state of one volume ---- */
+typedef struct dno_map dno_map;
+
+dno_map* dno_create(uint32_t sx, uint32_t sy, uint32_t sz);
+void dno_destroy(dno_map* m);
+
+/* modes */
+#define DNO_RNG_HASH 0              /* D5 mode B */
+#define DNO_RNG_SIN  1              /* D5 mode A */
+#define DNO_PERSIST_TRANSPARENCY 2  /* D13: carry lastVoxID across rays (pinning only) */
+
+typedef struct dno_light_params {
+    float sunDir[3];          /* already normalised by the caller (voxel.c:942) */
+    float sunStrength[3];
+    float ambient[3];
+    float camPos[3];
+    float skyBot[3], skyTop[3];
+    float shadowSoftness;
+    float time;               /* latched time (voxel.c:886-887) */
+    float emissiveStrength;   /* D9 */
+    uint32_t numDiffuse, maxDiffuse;
+    uint32_t diffuseBounceLimit, specBounceLimit;
+    uint32_t K;               /* fixed direct / specular ray count (D8), <= 64 */
+    uint32_t flags;           /* DNO_RNG_* | DNO_PERSIST_TRANSPARENCY */
+    uint32_t mapId;           /* hash key component (D5) */
+    uint32_t useSpherePoints; /* 1: use spherePts below verbatim (K entries) */
+    float spherePts[64][3];
+} dno_light_params;
+
+typedef struct dno_draw_params {
+    float invView[4][4];          /* column-major m[col][row] */
+    float invCenteredView[4][4];
+    float invProj[4][4];
+    uint32_t width, height;
+    uint32_t viewMode;
+    uint32_t truncate16;          /* D7 */
+    float sunStrength[3];
+    float skyBot[3], skyTop[3];
+    float emissiveStrength;
+    /* pixel subset (NULL = all pixels): list of pixel indices y*width+x */
+    const uint32_t* pixels;
+    uint32_t npixels;
+} dno_draw_params;
+
+typedef struct dno_counters {
+    uint64_t rays;            /* step_map calls (all kinds) */
+    uint64_t primary;         /* primary rays that entered step_map */
+    uint64_t outerSteps;      /* chunk cells visited (S_chunk) */
+    uint64_t chunksEntered;   /* loaded chunks stepped into (E_chunk) */
+    uint64_t innerSteps;      /* voxel cells visited */
+    uint64_t hits;            /* voxels decompressed (H) */
+    uint64_t litVoxels;       /* voxels whose lighting was computed */
+} dno_counters;
+
+/* Sync: restatement of DN_sync_gpu's per-tile loop (voxel.c:719-786) with the
+ * state machine of _DN_stream_to_gpu (voxel.c:1491-1536) and the request rule
+ * of _DN_request_chunk_lighting (voxel.c:1463-1489).  The CPU map and chunks
+ * are read (not modified; the caller clears 'updated' afterwards as the
+ * product does). op: 0 DN_READ, 1 DN_WRITE, 2 DN_READ_WRITE. */
+void dno_sync(dno_map* m, const dno_handle* cpuMap, const dno_chunk* chunks,
+              const dno_material* materials, int op, int lightingSplit);
+
+/* Lighting update over the current request list (voxelLighting.comp:207-288). */
+void dno_light(dno_map* m, const dno_material* materials, const dno_light_params* p, int nthreads);
+
+/* Draw (voxelDraw.comp:63-147).  color: RGBA floats per pixel (rgb, depth);
+ * hit: global voxel index; face: D14.  With a pixel subset, outputs are
+ * packed in subset order. */
+void dno_draw(dno_map* m, const dno_material* materials, const dno_draw_params* p,
+              float* color, uint32_t* hit, uint8_t* face, int nthreads);
+
+/* Lighting of a subset of requests only (size-independent sampled parity):
+ * computes results for the listed request indices without committing.
+ * out_diff/out_spec: 32*3 floats per listed request; valid: 32 bytes each. */
+void dno_light_requests(dno_map* m, const dno_material* materials, const dno_light_params* p,
+                        const uint32_t* reqIdx, uint32_t n, float* out_diff, float* out_spec,
+                        uint8_t* valid, int nthreads);
+
+/* --- state access for tests --- */
+uint32_t dno_num_requests(const dno_map* m);
+const uint32_t* dno_requests(const dno_map* m);     /* (tile << 4) | group, tile order */
+uint32_t dno_frame_num(const dno_map* m);
+void dno_get_counters(const dno_map* m, dno_counters* out);
+void dno_reset_counters(dno_map* m);
+/* tile state export: state (0 absent, 1 unloaded, 2 loaded, 3 requested), vis, lastUsed */
+void dno_export_tiles(const dno_map* m, uint8_t* state, uint8_t* vis, uint32_t* lastUsed);
+/* lighting export for every loaded chunk: rows (globalVoxelIndex, diff rgb, spec rgb) in
+ * tile order then rank order; returns the number of rows (call with NULL to count). */
+uint64_t dno_export_lighting(const dno_map* m, uint32_t* index, float* diff, float* spec);
+/* per-tile sample counts (0 for tiles that are not loaded) */
+void dno_export_samples(const dno_map* m, uint32_t* samples);
+/* import lighting + samples + vis for loaded chunks from another implementation
+ * (rows as in dno_export_lighting); used by sampled parity at full size. */
+void dno_import_lighting(dno_map* m, uint64_t n, const uint32_t* index, const float* diff, const float* spec);
+void dno_import_samples(dno_map* m, const uint32_t* samples);
+
+/* deterministic sine used by RNG mode A (Cody-Waite reduction + Taylor polynomial) */
+float dno_sin(float x);
+/* RNG mode B hash */
+uint32_t dno_hash32(uint32_t x);
+/* K-point golden-angle sphere, computed in double and rounded to float */
+void dno_sphere_points(uint32_t K, float out[][3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
