@@ -1,0 +1,417 @@
+#!/usr/bin/env python3
+"""Benchmark of the DoonEngine lighting + draw path on GB300.
+
+Workload ("large"): a 64x32x64-chunk map (512x256x512 voxels, ~15% of chunks non-empty; seeded
+heightfield + 2000 boxes and spheres), a fixed camera, 1920x1080 primary rays, lighting with
+1 diffuse path per voxel per frame and K=32 fixed direct / specular rays per voxel.  One step is one
+frame in the reference's order: DN_draw -> DN_sync_gpu -> DN_update_lighting (main.c:503-505).
+Data are synthetic and seeded (the reference publishes no scenes or numbers).
+
+Metric: aggregate rays/s = every traversal segment (primary, shadow, specular, diffuse) counted once by
+device counters, over the summed CUDA-event time of the timed steps (inputs resident in HBM, L2 flushed
+between steps outside the timed events).  ``e2e``: the same frames through the C API drawing into pinned
+host memory, each step ending with the image, hit indices and faces on the host (wall clock).
+
+--impl reference: the reference path runs only as GLSL (no graphics stack here), so the reference arm
+times the CPU restatement of its algorithm (oracle/) on the host cores, on a bounded sample per step.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
+METRIC = "aggregate rays/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    except Exception:
+        return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        finally:
+            os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allreduce_max(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+def workload_desc(cfg, vol=None, nonempty=None):
+    sx, sy, sz = cfg["map"]
+    d = {"workload": "large: %dx%dx%d chunks (%dx%dx%d voxels), heightfield + %d boxes/spheres, %dx%d draw, "
+                     "K=%d direct/specular rays, 1 diffuse path per voxel per frame"
+                     % (sx, sy, sz, sx * 8, sy * 8, sz * 8, cfg["shapes"], cfg["res"][0], cfg["res"][1], cfg["K"]),
+         "map_chunks": [sx, sy, sz], "resolution": list(cfg["res"]), "K": cfg["K"], "diffuse_spp": 1,
+         "seed": cfg["seed"], "frame": "draw -> sync -> lighting",
+         "l2": "flushed between timed steps (256 MiB write, outside the timed events)"}
+    if nonempty is not None:
+        d["nonempty_chunk_frac"] = round(nonempty, 4)
+    return d
+
+
+# ------------------------------------------------------------------ our arm
+
+def run_ours(args):
+    rank, world, local, pg = dist_setup()
+    import doonengine_gb300 as dn
+    from doonengine_gb300 import configs
+    lib = dn.load()
+    if lib.dn_cuda_init(local) != 0:
+        raise RuntimeError("dn_cuda_init(%d): %s" % (local, lib.dn_cuda_last_error().decode()))
+    dn.init()
+    vol, cfg = configs.build_volume(args.config, seed=configs.CONFIGS[args.config]["seed"] + 1000 * rank)
+    vol.s.mapId = rank
+    nonempty = vol.nonempty_chunks() / vol.num_tiles
+    W, H = cfg["res"]
+    img = dn.Image(W, H, on_device=True)
+    view, proj = vol.view_proj(H / W)
+    stream = vol.stream()
+    frame = [0]
+
+    def step(image):
+        t = 1.0 + 0.25 * frame[0]
+        vol.draw(image, view, proj)
+        vol.sync(dn.DN_READ_WRITE, 1)
+        vol.update_lighting(1, 1000, t)
+        frame[0] += 1
+
+    for _ in range(args.warmup):
+        step(img)
+    assert vol.finish(), lib.dn_cuda_last_error().decode()
+
+    K = args.steps
+    evs = []
+    for _ in range(3 * K):
+        e = __import__("ctypes").c_void_p()
+        lib.dn_cuda_event_create(e)
+        evs.append(e)
+    vol.reset_stats()
+    launches0 = lib.dn_cuda_launch_count()
+    clocks = ClockSampler(local)
+    barrier(pg)
+    lib.dn_cuda_device_sync()
+    clocks.start()
+    t0 = time.perf_counter()
+    for k in range(K):
+        lib.dn_cuda_flush_l2(stream, L2_FLUSH_BYTES)
+        lib.dn_cuda_event_record(evs[3 * k], stream)
+        t = 1.0 + 0.25 * frame[0]
+        vol.draw(img, view, proj)
+        vol.sync(dn.DN_READ_WRITE, 1)
+        lib.dn_cuda_event_record(evs[3 * k + 1], stream)
+        vol.update_lighting(1, 1000, t)
+        lib.dn_cuda_event_record(evs[3 * k + 2], stream)
+        frame[0] += 1
+    lib.dn_cuda_device_sync()
+    barrier(pg)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches = lib.dn_cuda_launch_count() - launches0 - K   # minus the L2-flush kernels
+    ms = __import__("ctypes").c_float()
+    dev_ms, light_ms = 0.0, 0.0
+    for k in range(K):
+        lib.dn_cuda_event_elapsed_ms(evs[3 * k], evs[3 * k + 2], ms)
+        dev_ms += ms.value
+        lib.dn_cuda_event_elapsed_ms(evs[3 * k + 1], evs[3 * k + 2], ms)
+        light_ms += ms.value
+    st_all = vol.stats_kind(0)
+    st_light = vol.stats_kind(2)
+    assert vol.finish(), lib.dn_cuda_last_error().decode()
+
+    rays_total = allreduce_sum(pg, st_all["rays"])
+    lit_total = allreduce_sum(pg, st_all["litVoxels"])
+    prim_total = allreduce_sum(pg, st_all["primaryRays"])
+    dev_ms_max = allreduce_max(pg, dev_ms)
+    value = rays_total / (dev_ms_max / 1e3)
+
+    # roofline of the dominant kernel (lighting: k_light + k_commit), algorithmic bytes from exact counters:
+    # 4 B per chunk cell visited, 64 B per chunk mask entered, 28 B per voxel hit, 40 B per lit voxel
+    peaks, peak_kind = load_peaks()
+    peak = float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
+    bytes_light = (4 * st_light["outerSteps"] + 64 * st_light["chunksEntered"] + 28 * st_light["hits"]
+                   + 40 * st_light["litVoxels"])
+    per_launch_bytes = bytes_light / K
+    per_launch_s = (light_ms / K) / 1e3
+    achieved = per_launch_bytes / per_launch_s / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "k_light_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            tj = json.load(open(tpath))
+            # captured DRAM bytes per lit voxel of the profiled launch, scaled to this run's launches
+            traffic = tj["dram_bytes_per_lit_voxel"] * st_light["litVoxels"] / K
+        except Exception:
+            traffic = None
+
+    result = {
+        "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
+        "ms_per_step": dev_ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded heightfield + boxes/spheres; the reference publishes no scenes)",
+        "config": dict(workload_desc(cfg, vol, nonempty), parallelism="replicas: one map per GPU, no collective"),
+        "lit_voxels_per_s": lit_total / (dev_ms_max / 1e3),
+        "primary_rays_per_s": prim_total / (dev_ms_max / 1e3),
+        "rays_per_step": rays_total / K,
+        "wall_s": wall,
+        "gpu_launches": int(allreduce_sum(pg, launches)),
+        "roofline": {"bound": "hbm", "kernel": "k_light+k_commit (DN_update_lighting)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": per_launch_bytes,
+                     "launch_ms": per_launch_s * 1e3},
+        "clocks": clk,
+    }
+
+    # e2e: the same frames through the C API into pinned host memory, host-side wall clock per step
+    if not args.no_e2e:
+        himg = dn.Image(W, H, on_device=False)
+        vol.reset_stats()
+        barrier(pg)
+        lib.dn_cuda_device_sync()
+        t0 = time.perf_counter()
+        for k in range(K):
+            step(himg)
+            assert vol.finish()
+        e2e_s = time.perf_counter() - t0
+        e2e_s = allreduce_max(pg, e2e_s)
+        st_e = vol.stats_kind(0)
+        e_rays = allreduce_sum(pg, st_e["rays"])
+        result["e2e"] = {"value": e_rays / e2e_s, "unit": "rays/s",
+                         "h2d_bytes_per_step": 2 * 256 * 32 + 1024,
+                         "d2h_bytes_per_step": W * H * (16 + 4 + 1) + 8,
+                         "path": "DN_draw(host DNimage) + DN_sync_gpu + DN_update_lighting + DN_finish"}
+        himg.close()
+
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline_sample(vol, view, proj, W, H, args.cpu_seconds)
+    vol.close()
+    img.close()
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+
+
+def cpu_baseline_sample(vol, view, proj, W, H, seconds):
+    """The oracle on the host cores, on this run's own map state: a pixel sample of the draw and a request
+    sample of the lighting, timed with all threads.  Test infrastructure, measured, not shipped."""
+    from oracle import oracle as O
+    import doonengine_gb300 as dn
+    from doonengine_gb300 import _lib
+    lib = dn.load()
+    ncores = os.cpu_count() or 1
+    st, vis, _, _ = vol.export_tiles()
+    reqs = vol.export_requests()
+    om = O.OracleMap(vol.map_size)
+    om.import_state(vol.s, st, vis, vol.s.frameNum)
+    om.set_requests(reqs)
+    params = om.light_params(vol.s, 1, 1000, float(vol.s.lastTime))
+    iv, icv, ip = _lib.DNmat4(), _lib.DNmat4(), _lib.DNmat4()
+    lib.DN_draw_matrices(view, proj, iv, icv, ip)
+    rng = np.random.default_rng(0)
+    order = rng.permutation(len(reqs)).astype(np.uint32)
+    pix = rng.choice(W * H, size=min(W * H, 1 << 16), replace=False).astype(np.uint32)
+    om.reset_counters()
+    t0 = time.perf_counter()
+    om.draw(vol.s, iv, icv, ip, W, H, pixels=pix, nthreads=ncores)
+    n, done, budget = 64, 0, seconds
+    while done < len(order) and time.perf_counter() - t0 < budget:
+        chunk = order[done:done + n]
+        om.light_requests(vol.s, params, chunk, nthreads=ncores)
+        done += len(chunk)
+        n = min(n * 2, 1 << 14)
+    el = time.perf_counter() - t0
+    c = om.counters()
+    om.close()
+    return {"value": c["rays"] / el, "unit": "rays/s", "cores": ncores, "kind": "port",
+            "sample": "%d pixels of the 1920x1080 draw + %d of %d lighting request groups of the last timed frame "
+                      "(%d rays, %.1f s)" % (len(pix), done, len(order), c["rays"], el)}
+
+
+# ------------------------------------------------------------ reference arm
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import doonengine_gb300 as dn
+    from doonengine_gb300 import configs, _lib
+    from oracle import oracle as O
+    lib = dn.load()
+    ncores = os.cpu_count() or 1
+    vol, cfg = configs.build_volume(args.config, cpu_only=True)
+    nonempty = vol.nonempty_chunks() / vol.num_tiles
+    W, H = cfg["res"]
+    view, proj = vol.view_proj(H / W)
+    iv, icv, ip = _lib.DNmat4(), _lib.DNmat4(), _lib.DNmat4()
+    lib.DN_draw_matrices(view, proj, iv, icv, ip)
+    om = O.OracleMap(vol.map_size)
+    rng = np.random.default_rng(0)
+    pix_n = args.ref_pixels if args.ref_pixels > 0 else W * H
+    req_cap = args.ref_requests
+
+    def clear_updated():
+        # the product's DN_sync_gpu clears 'updated' after streaming (voxel.c:1534); the oracle only reads it
+        for i in range(vol.s.chunkCap):
+            if vol.s.chunks[i].updated:
+                vol.s.chunks[i].updated = False
+
+    def frame(f):
+        if pix_n >= W * H:
+            om.draw(vol.s, iv, icv, ip, W, H, nthreads=ncores)
+        else:
+            pix = rng.choice(W * H, size=pix_n, replace=False).astype(np.uint32)
+            om.draw(vol.s, iv, icv, ip, W, H, pixels=pix, nthreads=ncores)
+        om.sync(vol.s, 2, 1)
+        clear_updated()
+        p = om.light_params(vol.s, 1, 1000, 1.0 + 0.25 * f)
+        reqs = om.requests()
+        sel = rng.permutation(len(reqs))[:req_cap].astype(np.uint32)
+        if len(sel):
+            om.light_requests(vol.s, p, sel, nthreads=ncores)
+
+    for f in range(args.warmup):
+        frame(f)
+    om.reset_counters()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        frame(args.warmup + k)
+    el = time.perf_counter() - t0
+    c = om.counters()
+    value = c["rays"] / el
+    sample = ("per step: %d sampled pixels of the %dx%d draw + up to %d sampled lighting request groups, "
+              "the CPU restatement of the reference shaders with OpenMP" % (pix_n, W, H, req_cap))
+    result = {"metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+              "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+              "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+              "data": "synthetic (seeded heightfield + boxes/spheres)", "impl": "reference",
+              "config": workload_desc(cfg, vol, nonempty),
+              "cpu_baseline": {"value": value, "unit": "rays/s", "cores": ncores, "kind": "port", "sample": sample},
+              "e2e": {"value": value, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+              "note": "the reference path runs only as GLSL through OpenGL, which is unavailable on this box; "
+                      "this arm times the CPU restatement of its algorithm"}
+    om.close()
+    vol.close()
+    print(json.dumps(result), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=24)
+    ap.add_argument("--warmup", type=int, default=8)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="large")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-pixels", type=int, default=0, help="pixels per reference step (0 = the full image)")
+    ap.add_argument("--ref-requests", type=int, default=2048, help="lighting request groups per reference step")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warmup raised to 3 (at least three untimed steps)")
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

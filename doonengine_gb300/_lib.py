@@ -157,6 +157,7 @@ _SIGS = [
     ("dn_cuda_draw_host", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("dn_cuda_finish", c_int, [c_void_p, POINTER(c_uint64)]),
     ("dn_cuda_stats", c_int, [c_void_p, c_void_p]),
+    ("dn_cuda_stats_kind", c_int, [c_void_p, c_int, c_void_p]),
     ("dn_cuda_reset_stats", c_int, [c_void_p]),
     ("dn_cuda_stream", c_void_p, [c_void_p]),
     ("dn_cuda_export_tiles", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
@@ -176,6 +177,7 @@ _SIGS = [
     ("dn_cuda_device_sync", c_int, []),
     ("dn_cuda_flush_l2", c_int, [c_void_p, c_size_t]),
     ("dn_cuda_kernel_names", c_char_p, []),
+    ("dn_cuda_launch_count", c_uint64, []),
 ]
 
 _lib = None

@@ -1,19 +1,19 @@
 """Seeded synthetic workloads (the reference publishes no benchmark data; these stand in for its
 scenes with the shapes and sizes of the benchmark configurations).
 
-* ``small``  -- 16x16x16 chunks (128^3 voxels), value-noise heightfield with about a third of the chunks
+* ``small``  -- 16x16x16 chunks (128^3 voxels), value-noise heightfield with about 35% of the chunks
   non-empty, 16 materials (2 emissive), specular U[0,0.5], one lighting update with 1 diffuse sample and
   K=16 direct / specular rays, then a 640x360 draw.
-* ``large``  -- 64x32x64 chunks (512x256x512 voxels), heightfield plus 2000 seeded boxes and spheres
-  (about 15% of chunks non-empty), 1920x1080 draw from a fixed camera, 1 diffuse sample per voxel per
+* ``large``  -- 64x32x64 chunks (512x256x512 voxels), heightfield plus 2000 seeded boxes and spheres of
+  3-10 voxels (about 15% of chunks non-empty), 1920x1080 draw from a fixed camera, 1 diffuse sample per voxel per
   frame, K=32 direct / specular rays, accumulated over 64 frames.
 """
 from .volume import Volume
 
 CONFIGS = {
-    "small": dict(map=(16, 16, 16), seed=1, mean=0.27, amp=0.16, shapes=0, res=(640, 360), K=16,
+    "small": dict(map=(16, 16, 16), seed=1, mean=0.32, amp=0.16, shapes=0, res=(640, 360), K=16,
                   frames=1, cam=(0.1, 0.62, 0.1, 32.0, 42.0)),
-    "large": dict(map=(64, 32, 64), seed=2, mean=0.115, amp=0.07, shapes=2000, res=(1920, 1080), K=32,
+    "large": dict(map=(64, 32, 64), seed=2, mean=0.06, amp=0.04, shapes=2000, shape_max=10, res=(1920, 1080), K=32,
                   frames=64, cam=(0.08, 0.42, 0.08, 24.0, 44.0)),
     # parity-test sizes: the same recipe scaled down
     "tiny": dict(map=(6, 5, 7), seed=3, mean=0.3, amp=0.2, shapes=6, res=(96, 64), K=8,
@@ -33,7 +33,7 @@ def build_volume(name, cpu_only=False, **over):
     vol.palette(seed, 16, 2, 0.1, 0.9, 0.5)
     vol.terrain(seed, cfg["mean"], cfg["amp"], 16, 2)
     if cfg["shapes"]:
-        vol.shapes(seed, cfg["shapes"], 3, 24, 14, 0.05, 0.5)
+        vol.shapes(seed, cfg["shapes"], cfg.get("shape_min", 3), cfg.get("shape_max", 24), 14, 0.05, 0.5)
     fx, fy, fz, pitch, yaw = cfg["cam"]
     vol.camera(fx, fy, fz, pitch, yaw, 90.0)
     vol.s.numDirectRays = cfg["K"]

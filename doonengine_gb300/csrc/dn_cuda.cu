@@ -71,7 +71,8 @@ enum { S_RAYS = 0, S_PRIMARY, S_OUTER, S_ENTERED, S_INNER, S_HITS, S_LIT, S_COUN
 
 struct DevState {
     uint32_t w[4];                      // nreq, work counter, error flags, pad
-    unsigned long long stats[8];
+    unsigned long long stats[8];        // draw kernels
+    unsigned long long lstats[8];       // lighting kernels
 };
 
 struct DNgpuVolume {
@@ -97,6 +98,10 @@ struct DNgpuVolume {
 
 static int g_device = -1;
 static int g_numSMs = 0;
+static unsigned long long g_launches = 0;   // kernels launched by this library (all threads)
+#define COUNT_LAUNCH() __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED)
+
+extern "C" uint64_t dn_cuda_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
 extern "C" int dn_cuda_init(int device)
 {
@@ -695,7 +700,7 @@ __global__ void __launch_bounds__(128) k_light(const __grid_constant__ LightArgs
         a.out[((uint64_t)r * 32u + lane) * 2u] = od;
         a.out[((uint64_t)r * 32u + lane) * 2u + 1u] = os;
     }
-    flush_counters(a.st->stats, L.rc.c, 0, lit);
+    flush_counters(a.st->lstats, L.rc.c, 0, lit);
 }
 
 // D1/D2: commit the new lighting after the whole launch, then count the sample
@@ -879,6 +884,7 @@ extern "C" int dn_cuda_sync(DNgpuVolume* g, const dn_sync_params* p, const dn_ti
         if (bVox) memcpy(g->hstage + oVox, voxelWords, bVox);
         CK(cudaMemcpyAsync(g->dstage, g->hstage, total, cudaMemcpyHostToDevice, g->stream));
         CK(cudaEventRecord(g->stageFree, g->stream));
+        COUNT_LAUNCH();
         k_sync_stage<<<nops < 65535u ? nops : 65535u, 128, 0, g->stream>>>(
             (const dn_tile_op*)g->dstage, nops, (const dn_chunk_record*)(g->dstage + oRec),
             (const uint64_t*)(g->dstage + oOff), (const uint32_t*)(g->dstage + oVox), g->tpend, g->tpendSlot,
@@ -893,8 +899,10 @@ extern "C" int dn_cuda_sync(DNgpuVolume* g, const dn_sync_params* p, const dn_ti
     a.op = p->op; a.split = p->split; a.frameNum = p->frameNum;
     uint64_t blocks = (g->ntiles + 255) / 256;
     uint32_t maxBlocks = (uint32_t)(g->numSMs > 0 ? g->numSMs * 8 : 1024);
+    COUNT_LAUNCH();
     k_compact<<<(uint32_t)(blocks < maxBlocks ? blocks : maxBlocks), 256, 0, g->stream>>>(a);
     CK(cudaGetLastError());
+    COUNT_LAUNCH();
     k_clamp_requests<<<1, 1, 0, g->stream>>>(g->st, g->reqCap);
     CK(cudaGetLastError());
     return DN_CUDA_OK;
@@ -924,8 +932,10 @@ extern "C" int dn_cuda_light(DNgpuVolume* g, const dn_light_params* p, const dn_
     int perSM = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light, 128, 0));
     if (perSM < 1) perSM = 1;
+    COUNT_LAUNCH();
     k_light<<<g->numSMs * perSM, 128, 0, g->stream>>>(*a);
     CK(cudaGetLastError());
+    COUNT_LAUNCH();
     k_commit<<<g->numSMs * 4, 256, 0, g->stream>>>(a->m, g->reqs, g->st, g->lightOut, g->diff, g->spec, g->nsamples);
     CK(cudaGetLastError());
     return DN_CUDA_OK;
@@ -942,6 +952,7 @@ static int launch_draw(DNgpuVolume* g, const dn_draw_params* p, const dn_materia
     memcpy(a->mats, materials, sizeof(a->mats));
     dim3 block(8, 32);
     dim3 grid((p->width + 7) / 8, (p->height + 31) / 32);
+    COUNT_LAUNCH();
     k_draw<<<grid, block, 0, g->stream>>>(*a);
     CK(cudaGetLastError());
     return DN_CUDA_OK;
@@ -995,22 +1006,26 @@ extern "C" int dn_cuda_finish(DNgpuVolume* g, uint64_t* numRequests)
     return DN_CUDA_OK;
 }
 
-extern "C" int dn_cuda_stats(DNgpuVolume* g, dn_stats* out)
+extern "C" int dn_cuda_stats_kind(DNgpuVolume* g, int kind, dn_stats* out)
 {
-    if (!g || !out) return set_err(DN_CUDA_ERR_ARG, "null argument");
+    if (!g || !out || kind < 0 || kind > 2) return set_err(DN_CUDA_ERR_ARG, "bad argument");
     int rc = dn_cuda_finish(g, nullptr);
     if (rc && rc != DN_CUDA_ERR_KERNEL) return rc;
-    const unsigned long long* s = g->hst->stats;
+    unsigned long long s[8];
+    for (int k = 0; k < 8; k++)
+        s[k] = (kind != 2 ? g->hst->stats[k] : 0ull) + (kind != 1 ? g->hst->lstats[k] : 0ull);
     out->rays = s[S_RAYS]; out->primary = s[S_PRIMARY]; out->outerSteps = s[S_OUTER];
     out->chunksEntered = s[S_ENTERED]; out->innerSteps = s[S_INNER]; out->hits = s[S_HITS]; out->litVoxels = s[S_LIT];
     return rc;
 }
 
+extern "C" int dn_cuda_stats(DNgpuVolume* g, dn_stats* out) { return dn_cuda_stats_kind(g, 0, out); }
+
 extern "C" int dn_cuda_reset_stats(DNgpuVolume* g)
 {
     if (!g) return set_err(DN_CUDA_ERR_ARG, "null volume");
     CK(cudaSetDevice(g->device));
-    CK(cudaMemsetAsync(g->st->stats, 0, sizeof(g->st->stats), g->stream));
+    CK(cudaMemsetAsync(g->st->stats, 0, sizeof(g->st->stats) + sizeof(g->st->lstats), g->stream));
     return DN_CUDA_OK;
 }
 
@@ -1130,6 +1145,7 @@ extern "C" int dn_cuda_flush_l2(void* stream, size_t bytes)
         CK(cudaMalloc((void**)&buf, n * 16));
         cap = n;
     }
+    COUNT_LAUNCH();
     k_flush<<<g_numSMs > 0 ? g_numSMs * 4 : 256, 256, 0, (cudaStream_t)stream>>>(buf, n, tick++);
     CK(cudaGetLastError());
     return DN_CUDA_OK;

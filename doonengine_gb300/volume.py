@@ -72,6 +72,8 @@ class Image:
         """(color [h,w,4] float32, hit [h,w] uint32, face [h,w] uint8) copied to the host."""
         n = self.width * self.height
         img = self.ptr.contents
+        # device work runs on per-volume non-blocking streams: wait for it before reading the image
+        self.lib.dn_cuda_device_sync()
         color = np.empty((self.height, self.width, 4), np.float32)
         hit = np.empty((self.height, self.width), np.uint32)
         face = np.empty((self.height, self.width), np.uint8)
@@ -184,6 +186,13 @@ class Volume:
         s = L.DNstats()
         if not self.lib.DN_get_stats(self.ptr, byref(s)):
             raise RuntimeError("DN_get_stats failed: %s" % self.lib.dn_cuda_last_error().decode())
+        return {k: int(getattr(s, k)) for k, _ in L.DNstats._fields_}
+
+    def stats_kind(self, kind):
+        """kind 0: all kernels, 1: draw, 2: lighting (k_light + k_commit)."""
+        s = L.DNstats()
+        if self.lib.dn_cuda_stats_kind(self.s.gpu, kind, ctypes.byref(s)) != 0:
+            raise RuntimeError("dn_cuda_stats_kind failed: %s" % self.lib.dn_cuda_last_error().decode())
         return {k: int(getattr(s, k)) for k, _ in L.DNstats._fields_}
 
     def reset_stats(self):

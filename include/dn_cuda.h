@@ -130,6 +130,8 @@ int dn_cuda_draw_host(struct DNgpuVolume* g, const dn_draw_params* p, const dn_m
 /* --- synchronisation, counters, introspection (additions) --- */
 int dn_cuda_finish(struct DNgpuVolume* g, uint64_t* numRequests);
 int dn_cuda_stats(struct DNgpuVolume* g, dn_stats* out);
+/* kind 0: all kernels, 1: draw, 2: lighting */
+int dn_cuda_stats_kind(struct DNgpuVolume* g, int kind, dn_stats* out);
 int dn_cuda_reset_stats(struct DNgpuVolume* g);
 void* dn_cuda_stream(struct DNgpuVolume* g);
 int dn_cuda_export_tiles(struct DNgpuVolume* g, uint8_t* state, uint8_t* vis, uint32_t* lastUsed, uint32_t* samples);
@@ -153,6 +155,8 @@ int dn_cuda_stream_sync(void* stream);
 int dn_cuda_device_sync(void);
 /* writes 'bytes' of a scratch buffer on 'stream' (L2 flush between timed steps) */
 int dn_cuda_flush_l2(void* stream, size_t bytes);
+/* number of kernels this library has launched since load (all volumes) */
+uint64_t dn_cuda_launch_count(void);
 /* names of the kernels this library launches, ';'-separated */
 const char* dn_cuda_kernel_names(void);
 

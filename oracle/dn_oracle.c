@@ -1138,3 +1138,27 @@ void dno_import_samples(dno_map* m, const uint32_t* samples)
 {
     for (uint64_t t = 0; t < m->ntiles; t++) if (m->state[t] == 2) m->rec[t].samples = samples[t];
 }
+
+void dno_import_state(dno_map* m, const dno_handle* cpuMap, const dno_chunk* chunks, const dno_material* mats,
+                      const uint8_t* state, const uint8_t* vis, uint32_t frameNum)
+{
+    for (uint64_t t = 0; t < m->ntiles; t++) {
+        uint8_t st = state[t];
+        if (st == 2) {
+            if (m->state[t] != 2 && cpuMap[t].flag) rec_load(&m->rec[t], &chunks[cpuMap[t].chunkIndex], mats);
+            if (!cpuMap[t].flag) st = 0;
+        } else if (m->state[t] == 2) {
+            rec_free(&m->rec[t]);
+        }
+        m->state[t] = st;
+        m->vis[t] = vis ? vis[t] : 0;
+        m->touch[t] = 0;
+    }
+    m->frameNum = frameNum;
+}
+
+void dno_set_requests(dno_map* m, const uint32_t* words, uint32_t n)
+{
+    m->nreq = 0;
+    for (uint32_t i = 0; i < n; i++) push_req(m, words[i]);
+}

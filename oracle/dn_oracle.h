@@ -210,6 +210,13 @@ void dno_export_samples(const dno_map* m, uint32_t* samples);
 void dno_import_lighting(dno_map* m, uint64_t n, const uint32_t* index, const float* diff, const float* spec);
 void dno_import_samples(dno_map* m, const uint32_t* samples);
 
+/* adopt another implementation's tile states (0..3) and visible flags; loaded tiles are packed
+ * from the CPU chunks by this oracle's own packing.  Used to time / check a sample of one frame of
+ * a large workload without replaying every earlier frame. */
+void dno_import_state(dno_map* m, const dno_handle* cpuMap, const dno_chunk* chunks, const dno_material* materials,
+                      const uint8_t* state, const uint8_t* vis, uint32_t frameNum);
+void dno_set_requests(dno_map* m, const uint32_t* words, uint32_t n);
+
 /* deterministic sine used by RNG mode A (Cody-Waite reduction + Taylor polynomial) */
 float dno_sin(float x);
 /* RNG mode B hash */

@@ -84,6 +84,8 @@ def load():
         ("dno_import_lighting", None, [c_void_p, c_uint64, c_void_p, c_void_p, c_void_p]),
         ("dno_import_samples", None, [c_void_p, c_void_p]),
         ("dno_pack_chunk", None, [c_void_p, c_void_p, c_void_p]),
+        ("dno_import_state", None, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_uint32]),
+        ("dno_set_requests", None, [c_void_p, c_void_p, c_uint32]),
         ("dno_compress_voxel", None, [c_uint8, c_void_p, c_void_p, c_void_p]),
         ("dno_decompress_voxel", None, [c_uint64, c_void_p, c_void_p, c_void_p]),
         ("dno_sin", c_float, [c_float]),
@@ -253,6 +255,18 @@ class OracleMap:
         diff = np.ascontiguousarray(diff, np.float32)
         spec = np.ascontiguousarray(spec, np.float32)
         self.lib.dno_import_lighting(self.ptr, len(idx), idx.ctypes.data, diff.ctypes.data, spec.ctypes.data)
+
+    def import_state(self, vol_s, state, vis, frame_num):
+        state = np.ascontiguousarray(state, np.uint8)
+        vis = np.ascontiguousarray(vis, np.uint8)
+        self.lib.dno_import_state(self.ptr, ctypes.cast(vol_s.map, c_void_p), ctypes.cast(vol_s.chunks, c_void_p),
+                                  ctypes.cast(vol_s.materials, c_void_p), state.ctypes.data, vis.ctypes.data, frame_num)
+        self.frame = frame_num
+        self.last_time = float(vol_s.lastTime)
+
+    def set_requests(self, words):
+        words = np.ascontiguousarray(words, np.uint32)
+        self.lib.dno_set_requests(self.ptr, words.ctypes.data, len(words))
 
     def import_samples(self, samples):
         samples = np.ascontiguousarray(samples, np.uint32)
