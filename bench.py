@@ -258,6 +258,7 @@ def run_ours(args):
                      "traffic": traffic, "algorithmic_bytes_per_launch": per_launch_bytes,
                      "launch_ms": per_launch_s * 1e3},
         "clocks": clk,
+        "light_counters_per_step": {k: v / K for k, v in st_light.items()},
     }
 
     # e2e: the same frames through the C API into pinned host memory, host-side wall clock per step

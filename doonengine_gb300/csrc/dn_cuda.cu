@@ -13,6 +13,8 @@
  */
 #include "dn_cuda.h"
 #include "dn_device.cuh"
+#include "dn_light.cuh"
+#include "dn_light_stream.cuh"
 #include <cuda_runtime.h>
 #include <stdio.h>
 #include <string.h>
@@ -81,6 +83,7 @@ struct DNgpuVolume {
     uint32_t sx, sy, sz;
     uint64_t ntiles;
     uint32_t* tword; uint8_t* treq; uint8_t* tvis; uint8_t* ttouch;
+    uint32_t* tbits;                    // 2 bits per tile: 0 absent, 1 unloaded, 2 loaded (16 tiles per word)
     uint32_t* tlast; uint32_t* tpend; uint32_t* tpendSlot;
     ChunkRec* rec; uint32_t* nsamples; uint32_t slotCap;
     uint2* vox; float4* diff; float4* spec; uint64_t voxCap;
@@ -103,8 +106,18 @@ static unsigned long long g_launches = 0;   // kernels launched by this library 
 
 extern "C" uint64_t dn_cuda_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
+// lighting kernel selection and stream batch threshold (DN_LIGHT_KERNEL=0 lockstep, 1 streams;
+// DN_STREAM_BATCH lanes, 1..32), read once at init
+static int g_lightKernel = 1;
+static uint32_t g_streamBatch = 24;
+
 extern "C" int dn_cuda_init(int device)
 {
+    if (const char* e = getenv("DN_LIGHT_KERNEL")) g_lightKernel = atoi(e);
+    if (const char* e = getenv("DN_STREAM_BATCH")) {
+        int b = atoi(e);
+        g_streamBatch = (uint32_t)(b < 1 ? 1 : (b > 32 ? 32 : b));
+    }
     int n = 0;
     cudaError_t e = cudaGetDeviceCount(&n);
     if (e != cudaSuccess || n == 0) {
@@ -136,10 +149,12 @@ static int alloc_tiles(DNgpuVolume* g)
     uint64_t n = g->ntiles;
     int rc;
     if ((rc = dalloc(&g->tword, n)) || (rc = dalloc(&g->treq, n)) || (rc = dalloc(&g->tvis, n)) ||
+        (rc = dalloc(&g->tbits, (n + 31) / 32 * 2)) ||
         (rc = dalloc(&g->ttouch, n)) || (rc = dalloc(&g->tlast, n)) || (rc = dalloc(&g->tpend, n)) ||
         (rc = dalloc(&g->tpendSlot, n)))
         return rc;
     CK(cudaMemsetAsync(g->tword, 0, n * 4, g->stream));
+    CK(cudaMemsetAsync(g->tbits, 0, (n + 31) / 32 * 8, g->stream));
     CK(cudaMemsetAsync(g->treq, 0, n, g->stream));
     CK(cudaMemsetAsync(g->tvis, 0, n, g->stream));
     CK(cudaMemsetAsync(g->ttouch, 0, n, g->stream));
@@ -150,7 +165,7 @@ static int alloc_tiles(DNgpuVolume* g)
 
 static void free_tiles(DNgpuVolume* g)
 {
-    dfree(g->tword); dfree(g->treq); dfree(g->tvis); dfree(g->ttouch); dfree(g->tlast); dfree(g->tpend); dfree(g->tpendSlot);
+    dfree(g->tword); dfree(g->tbits); dfree(g->treq); dfree(g->tvis); dfree(g->ttouch); dfree(g->tlast); dfree(g->tpend); dfree(g->tpendSlot);
 }
 
 extern "C" void dn_cuda_map_destroy(DNgpuVolume* g)
@@ -430,228 +445,6 @@ struct LightArgs {
     Material mats[256];
 };
 
-struct LightCtx {
-    RayCtx rc;
-    const dn_light_params* p;
-    f3 sunDir, ambient, camPos, skyBot, skyTop;
-    bool firstSample, rngSin;
-    uint32_t key, sample;
-};
-
-// specular_ray, voxelLighting.comp:83-146
-__device__ __noinline__ void specular_ray(LightCtx& L, f3 rayPos, f3 rayDir, f3 albedo, uint32_t reflectType, f3& color)
-{
-    RayCtx& c = L.rc;
-    const DevMap& m = *c.m;
-    f3 lastPos = rayPos;
-    f3 mult = albedo;
-    Voxel hv;
-    hv.normal = mk(0.0f, 0.0f, 0.0f); hv.material = 0; hv.albedo = hv.normal; hv.spec = hv.normal; hv.diff = hv.normal;
-    TState ts{255u, 1.0f};   // D13: fresh per ray job
-    for (uint32_t i = 0; i < L.p->specBounceLimit; i++) {
-        f3 cadd; float cmul; f3 tn = mk(0.0f, 0.0f, 0.0f); HitInfo hi;
-        f3 inv = mk(1.0f / rayDir.x, 1.0f / rayDir.y, 1.0f / rayDir.z);
-        if (step_map(c, ts, rayDir, inv, rayPos, true, -1.0f, tn, hv, cadd, cmul, hi)) {
-            i3 hp{f2i(truncf(rayPos.x)), f2i(truncf(rayPos.y)), f2i(truncf(rayPos.z))};
-            if (in_map(m, hp)) {   // D4: the lit chunk was visible when requested
-                uint8_t* vp = &m.tvis[map_index(m, hp)];
-                if (*vp == 0) *vp = 1;
-            }
-            f3 d = vabs(sub(vfloor(muls(rayPos, 8.0f)), vfloor(muls(lastPos, 8.0f))));
-            if (dot(d, d) <= 1.0f) return;
-            const Material& hm = c.mats[hv.material];
-            hv.diff = muls(hv.diff, 1.0f - hm.specular);
-            if (hm.emissive) {
-                color.x = color.x + ((hv.albedo.x * c.emissive * cmul + cadd.x) * mult.x) * albedo.x;
-                color.y = color.y + ((hv.albedo.y * c.emissive * cmul + cadd.y) * mult.y) * albedo.y;
-                color.z = color.z + ((hv.albedo.z * c.emissive * cmul + cadd.z) * mult.z) * albedo.z;
-                return;
-            }
-            f3 hc = mul(hv.diff, hv.albedo);
-            color.x = color.x + (hc.x * cmul + cadd.x) * mult.x;
-            color.y = color.y + (hc.y * cmul + cadd.y) * mult.y;
-            color.z = color.z + (hc.z * cmul + cadd.z) * mult.z;
-            if (hm.specular == 0.0f) return;
-            mult.x = mult.x * (hv.albedo.x * cmul * hm.specular);
-            mult.y = mult.y * (hv.albedo.y * cmul * hm.specular);
-            mult.z = mult.z * (hv.albedo.z * cmul * hm.specular);
-            reflectType = hm.reflectType;
-            lastPos = rayPos;
-            rayDir = reflect(rayDir, hv.normal);
-        } else if (dot(rayDir, L.sunDir) > 0.99f) {
-            color.x = color.x + (c.sunStrength.x * cmul + cadd.x);
-            color.y = color.y + (c.sunStrength.y * cmul + cadd.y);
-            color.z = color.z + (c.sunStrength.z * cmul + cadd.z);
-            return;
-        } else {
-            f3 s = (reflectType == 1u) ? sky_color(L.skyBot, L.skyTop, rayDir) : c.sunStrength;
-            color.x = color.x + (s.x * cmul + cadd.x) * mult.x;
-            color.y = color.y + (s.y * cmul + cadd.y) * mult.y;
-            color.z = color.z + (s.z * cmul + cadd.z) * mult.z;
-            return;
-        }
-    }
-}
-
-// diffuse_ray, voxelLighting.comp:149-203
-__device__ __noinline__ void diffuse_ray(LightCtx& L, f3 normal, f3 rayPos, const Voxel& initial, float seed, f3& color)
-{
-    RayCtx& c = L.rc;
-    const dn_light_params* p = L.p;
-    Voxel hv = initial;
-    f3 hitNormal = normal;
-    uint32_t hmat = initial.material;
-    f3 nc = mk(1.0f, 1.0f, 1.0f);
-    const f3 lastPos = rayPos;
-    f3 lastDir = mk(0.0f, 0.0f, 0.0f);
-    TState ts{255u, 1.0f};   // D13
-    for (uint32_t i = 0; i < p->diffuseBounceLimit; i++) {
-        f3 dir;
-        bool lobe = false;
-        const Material& hm0 = c.mats[hmat];
-        if (i > 0) {
-            float r = L.rngSin ? srand1(seed + (float)p->diffuseBounceLimit + (float)i)
-                               : hrand(L.key, 2u, (L.sample * 16u + i) << 8);
-            lobe = (r + 1.0f) * 0.5f < hm0.specular;
-        }
-        if (lobe) {
-            f3 rs = L.rngSin ? sphere_sin(p->time + (float)i) : sphere_hash(L.key, 3u, L.sample * 16u + i);
-            dir = normalize(add(muls(reflect(lastDir, hitNormal), (float)hm0.shininess), rs));
-        } else if (L.firstSample) {
-            dir = adds(normalize(hitNormal), EPS);
-        } else {
-            f3 rs = L.rngSin ? sphere_sin(seed + (float)i) : sphere_hash(L.key, 1u, L.sample * 16u + i);
-            dir = adds(normalize(add(hitNormal, rs)), EPS);
-        }
-        f3 cadd; float cmul; f3 tn = mk(0.0f, 0.0f, 0.0f); HitInfo hi;
-        f3 inv = mk(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
-        f3 pos = rayPos;
-        bool hit = step_map(c, ts, dir, inv, pos, true, -1.0f, tn, hv, cadd, cmul, hi);
-        rayPos = pos;
-        hitNormal = hv.normal;
-        hmat = hv.material;
-        const Material& hm = c.mats[hmat];
-        if (hit) {
-            f3 d = vabs(sub(vfloor(muls(lastPos, 8.0f)), vfloor(muls(rayPos, 8.0f))));
-            if (dot(d, d) < 1.0f) return;
-            if (hm.emissive) {
-                color.x = color.x + nc.x * (hv.albedo.x * c.emissive * cmul + cadd.x);
-                color.y = color.y + nc.y * (hv.albedo.y * c.emissive * cmul + cadd.y);
-                color.z = color.z + nc.z * (hv.albedo.z * c.emissive * cmul + cadd.z);
-                return;
-            }
-            nc.x = nc.x * (hv.albedo.x * cmul + cadd.x);
-            nc.y = nc.y * (hv.albedo.y * cmul + cadd.y);
-            nc.z = nc.z * (hv.albedo.z * cmul + cadd.z);
-        } else {
-            float k = gmax(dot(dir, L.sunDir), 0.0f);
-            color.x = color.x + (nc.x * k * c.sunStrength.x * cmul + cadd.x);
-            color.y = color.y + (nc.y * k * c.sunStrength.y * cmul + cadd.y);
-            color.z = color.z + (nc.z * k * c.sunStrength.z * cmul + cadd.z);
-            return;
-        }
-        lastDir = dir;
-    }
-}
-
-// one shadow ray, voxelLighting.comp:65-80
-__device__ __forceinline__ void shadow_ray(LightCtx& L, f3 rayPos, f3 dir, f3& color)
-{
-    RayCtx& c = L.rc;
-    Voxel hv; f3 cadd; float cmul; f3 tn = mk(0.0f, 0.0f, 0.0f); HitInfo hi;
-    TState ts{255u, 1.0f};   // D13
-    f3 inv = mk(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
-    if (!step_map(c, ts, dir, inv, rayPos, true, -1.0f, tn, hv, cadd, cmul, hi)) {
-        color.x = color.x + (c.sunStrength.x * cmul + cadd.x);
-        color.y = color.y + (c.sunStrength.y * cmul + cadd.y);
-        color.z = color.z + (c.sunStrength.z * cmul + cadd.z);
-    }
-}
-
-// voxelLighting.comp:207-288 for one voxel
-__device__ __noinline__ void light_voxel(LightCtx& L, i3 mp, i3 cp, const Voxel& tv, uint32_t samples,
-                                         float4& outD, float4& outS)
-{
-    RayCtx& c = L.rc;
-    const DevMap& m = *c.m;
-    const dn_light_params* p = L.p;
-    const Material& tm = c.mats[tv.material];
-    const uint32_t ns = samples < p->maxDiffuse ? samples : p->maxDiffuse;
-    const float indirect = (float)ns;
-    L.firstSample = (indirect == 0.0f);
-    const uint32_t gx = (uint32_t)(mp.x * 8 + cp.x), gy = (uint32_t)(mp.y * 8 + cp.y), gz = (uint32_t)(mp.z * 8 + cp.z);
-    const uint32_t gidx = gx + (m.sx * 8u) * (gy + (m.sy * 8u) * gz);
-    L.key = rng_key(__float_as_uint(p->time), p->mapId, gidx);
-
-    f3 rayPos;
-    rayPos.x = INV_CHUNK * (float)cp.x + (float)mp.x + HALF_INV_CHUNK;
-    rayPos.y = INV_CHUNK * (float)cp.y + (float)mp.y + HALF_INV_CHUNK;
-    rayPos.z = INV_CHUNK * (float)cp.z + (float)mp.z + HALF_INV_CHUNK;
-    const float off = HALF_INV_CHUNK - EPS;
-    rayPos = add(rayPos, muls(tv.normal, off));
-
-    f3 spec = mk(0.0f, 0.0f, 0.0f), diff = mk(0.0f, 0.0f, 0.0f);
-    const uint32_t K = p->K;
-    f3 viewDir = sub(rayPos, L.camPos);
-    if (tm.specular > 0.0f && dot(viewDir, tv.normal) < 0.0f && tm.reflectType <= 1u) {
-        f3 refl = reflect(normalize(viewDir), tv.normal);
-        for (uint32_t k = 0; k < K; k++) {
-            f3 P = mk(p->spherePts[k][0], p->spherePts[k][1], p->spherePts[k][2]);
-            f3 sd = adds(normalize(add(muls(refl, (float)tm.shininess), P)), EPS);
-            specular_ray(L, rayPos, sd, tv.albedo, tm.reflectType, spec);
-        }
-        spec = divs(spec, (float)K);
-    }
-    if (tm.specular < 1.0f) {
-        // D8: K fixed shadow rays traced once, averaged, added once per sample
-        f3 sum = mk(0.0f, 0.0f, 0.0f);
-        f3 direct;
-        if (L.firstSample) {
-            shadow_ray(L, rayPos, adds(L.sunDir, EPS), sum);
-            direct = divs(sum, 1.0f);
-        } else {
-            for (uint32_t k = 0; k < K; k++) {
-                f3 P = mk(p->spherePts[k][0], p->spherePts[k][1], p->spherePts[k][2]);
-                f3 d = adds(normalize(add(muls(L.sunDir, p->shadowSoftness), P)), EPS);
-                shadow_ray(L, rayPos, d, sum);
-            }
-            direct = divs(sum, (float)K);
-        }
-        for (uint32_t i = 0; i < p->numDiffuse; i++) {
-            L.sample = i;
-            diff = add(diff, L.ambient);
-            diffuse_ray(L, adds(tv.normal, EPS), rayPos, tv, p->time * (float)(i + 1u), diff);
-            diff = add(diff, direct);
-        }
-        const float den = indirect + (float)p->numDiffuse;
-        diff.x = (tv.diff.x * indirect + diff.x) / den;
-        diff.y = (tv.diff.y * indirect + diff.y) / den;
-        diff.z = (tv.diff.z * indirect + diff.z) / den;
-    }
-    outS = make_float4(gmin(gmax(spec.x, 0.0f), 1.0f), gmin(gmax(spec.y, 0.0f), 1.0f), gmin(gmax(spec.z, 0.0f), 1.0f), 0.0f);
-    outD = make_float4(gmin(gmax(diff.x, 0.0f), 1.0f), gmin(gmax(diff.y, 0.0f), 1.0f), gmin(gmax(diff.z, 0.0f), 1.0f), 0.0f);
-}
-
-// n-th set bit of a chunk mask -> local position; false if n >= popcount
-__device__ __forceinline__ bool select_voxel(const ChunkRec* r, uint32_t n, i3& out, uint32_t& li)
-{
-    uint32_t count = 0;
-    for (uint32_t w = 0; w < 16; w++) {
-        uint32_t bits = __ldg(&r->mask[w]);
-        uint32_t c = __popc(bits);
-        if (count + c > n) {
-            for (uint32_t k = n - count; k > 0; k--) bits &= bits - 1u;   // drop the k lowest set bits
-            uint32_t b = (uint32_t)(__ffs(bits) - 1);
-            uint32_t pos = w * 32u + b;
-            li = pos;
-            out.x = (int32_t)(pos & 7u); out.y = (int32_t)((pos >> 3) & 7u); out.z = (int32_t)(pos >> 6);
-            return true;
-        }
-        count += c;
-    }
-    return false;
-}
-
 __global__ void __launch_bounds__(128) k_light(const __grid_constant__ LightArgs a)
 {
     __shared__ Material smat[256];
@@ -683,24 +476,114 @@ __global__ void __launch_bounds__(128) k_light(const __grid_constant__ LightArgs
         const uint32_t word = a.reqs[r];
         const uint32_t tile = word >> 4, group = word & 15u;
         const uint32_t tw = __ldg(&a.m.tword[tile]);
-        float4 od = make_float4(0.0f, 0.0f, 0.0f, 0.0f), os = od;
+        // every lane of the warp takes part (the phases use warp votes); lanes without a voxel idle
+        bool active = false;
+        i3 cp{0, 0, 0}, mp{0, 0, 0};
+        uint32_t samples = 0;
+        Voxel tv;
+        tv.normal = mk(0.0f, 1.0f, 0.0f); tv.material = 0; tv.albedo = mk(0.0f, 0.0f, 0.0f);
+        tv.spec = tv.albedo; tv.diff = tv.albedo;
         if ((tw >> 30) == 2u) {
             const uint32_t slot = tw & SLOT_MASK;
             const ChunkRec* rc = &a.m.rec[slot];
             const uint32_t vn = group * 32u + lane;
-            i3 cp; uint32_t li;
+            uint32_t li;
             if (vn < __ldg(&rc->nvox) && select_voxel(rc, vn, cp, li)) {
-                i3 mp{__ldg(&rc->pos[0]), __ldg(&rc->pos[1]), __ldg(&rc->pos[2])};
-                Voxel tv;
+                mp = i3{__ldg(&rc->pos[0]), __ldg(&rc->pos[1]), __ldg(&rc->pos[2])};
                 decompress(a.m, __ldg(&rc->voxBase) + vn, tv);
-                light_voxel(L, mp, cp, tv, __ldg(&a.nsamples[slot]), od, os);
-                lit++;
+                samples = __ldg(&a.nsamples[slot]);
+                active = true;
             }
         }
+        float4 od = make_float4(0.0f, 0.0f, 0.0f, 0.0f), os = od;
+        light_voxel(L, active, mp, cp, tv, samples, od, os);
+        if (!active) { od = make_float4(0.0f, 0.0f, 0.0f, 0.0f); os = od; }
+        lit += active ? 1u : 0u;
         a.out[((uint64_t)r * 32u + lane) * 2u] = od;
         a.out[((uint64_t)r * 32u + lane) * 2u + 1u] = os;
     }
     flush_counters(a.st->lstats, L.rc.c, 0, lit);
+}
+
+#ifndef DN_STREAM_MIN_BLOCKS
+#define DN_STREAM_MIN_BLOCKS 4   // 4 blocks of 4 warps per SM (measured best: leaves L1 room for the tile map)
+#endif
+
+// The lighting launch as persistent per-lane ray streams (dn_light_stream.cuh).
+__global__ void __launch_bounds__(128, DN_STREAM_MIN_BLOCKS) k_light_stream(const __grid_constant__ StreamArgs a)
+{
+    __shared__ StreamShared sh;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) sh.mats[i] = a.mats[i];
+    {
+        // shadow directions: normalize(sunDir * softness + P_k) + EPS and their reciprocals (identical for every voxel)
+        const dn_light_params& p = a.p;
+        const f3 sd = mk(p.sunDir[0], p.sunDir[1], p.sunDir[2]);
+        for (int k = threadIdx.x; k < 65; k += blockDim.x) {
+            f3 d;
+            if (k == 64) d = adds(sd, EPS);
+            else if ((uint32_t)k < p.K) {
+                const f3 P = mk(p.spherePts[k][0], p.spherePts[k][1], p.spherePts[k][2]);
+                d = adds(normalize(add(muls(sd, p.shadowSoftness), P)), EPS);
+            } else d = mk(1.0f, 1.0f, 1.0f);
+            sh.sdir[k][0] = d.x; sh.sdir[k][1] = d.y; sh.sdir[k][2] = d.z;
+            sh.sinv[k][0] = __frcp_rn(d.x); sh.sinv[k][1] = __frcp_rn(d.y); sh.sinv[k][2] = __frcp_rn(d.z);
+        }
+    }
+    __syncthreads();
+    const uint32_t lane = lane_id();
+    const uint32_t nreq = *(volatile const uint32_t*)a.nreqPtr;
+    const f3 sun = mk(a.p.sunStrength[0], a.p.sunStrength[1], a.p.sunStrength[2]);
+    const uint32_t batch = a.batch;
+    uint32_t winReq = 0, winNext = 32;     // warp-uniform voxel window: request index, next lane in it
+    bool exhausted = false;
+    // per-voxel job state lives in shared memory: it is touched only when a segment ends
+    __shared__ Job jobs[128];
+    Job& j = jobs[threadIdx.x];
+    j.phase = PH_FETCH;
+    Seg s;
+    bool rayActive = false;
+    uint32_t hitState = 0, hitIdx = 0;
+    Counters c{0, 0, 0, 0, 0};
+    uint32_t lit = 0;
+    while (true) {
+        const unsigned waiting = __ballot_sync(0xFFFFFFFFu, !rayActive && j.phase != PH_DONE);
+        const unsigned stepping = __ballot_sync(0xFFFFFFFFu, rayActive);
+        if (waiting == 0u && stepping == 0u) break;
+        if (stepping == 0u || (uint32_t)__popc(waiting) >= batch) {
+            for (int round = 0; round < 4; round++) {
+                // warp-cooperative voxel fetch for lanes whose voxel is done
+                for (int guard = 0; guard < 64; guard++) {
+                    const unsigned need = __ballot_sync(0xFFFFFFFFu, j.phase == PH_FETCH);
+                    if (need == 0u) break;
+                    if (winNext >= 32u) {
+                        uint32_t r = 0;
+                        if (!exhausted && lane == 0) r = atomicAdd(a.workCounter, 1u);
+                        r = __shfl_sync(0xFFFFFFFFu, r, 0);
+                        if (exhausted || r >= nreq) {
+                            exhausted = true;
+                            if (j.phase == PH_FETCH) j.phase = PH_DONE;
+                            break;
+                        }
+                        winReq = r;
+                        winNext = 0;
+                    }
+                    const uint32_t rank = __popc(need & ((1u << lane) - 1u));
+                    if (j.phase == PH_FETCH && winNext + rank < 32u) voxel_setup(j, winReq, winNext + rank, a, sh);
+                    const uint32_t took = (uint32_t)__popc(need) < 32u - winNext ? (uint32_t)__popc(need) : 32u - winNext;
+                    winNext += took;
+                }
+                // shade the finished segment and set up the next one (or finish the voxel)
+                if (!rayActive && j.phase != PH_DONE && j.phase != PH_FETCH)
+                    rayActive = advance(j, s, hitState, hitIdx, a, sh, c, lit);
+                if (__ballot_sync(0xFFFFFFFFu, j.phase == PH_FETCH) == 0u) break;
+            }
+        }
+        if (rayActive) {
+            const uint32_t r = seg_step(s, a.m, sh.mats, sun, c, hitIdx);
+            if (r) { rayActive = false; hitState = r; }
+        }
+    }
+    flush_counters(a.stats, c, 0, lit);
 }
 
 // D1/D2: commit the new lighting after the whole launch, then count the sample
@@ -763,8 +646,20 @@ __global__ void k_sync_stage(const dn_tile_op* ops, uint32_t nops, const dn_chun
     }
 }
 
+// spreads the 16 low bits of x to the even bit positions of a word
+__device__ __forceinline__ uint32_t spread_bits(uint32_t x)
+{
+    x &= 0xFFFFu;
+    x = (x | (x << 8)) & 0x00FF00FFu;
+    x = (x | (x << 4)) & 0x0F0F0F0Fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    x = (x | (x << 1)) & 0x55555555u;
+    return x;
+}
+
 struct CompactArgs {
     uint32_t* tword; uint8_t* treq; uint8_t* tvis; uint8_t* ttouch; uint32_t* tlast;
+    uint32_t* tbits;
     uint32_t* tpend; const uint32_t* tpendSlot;
     const ChunkRec* rec;
     uint32_t* reqs; uint64_t reqCap;
@@ -782,9 +677,11 @@ __global__ void __launch_bounds__(256) k_compact(const __grid_constant__ Compact
     for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < a.ntiles; base += stride) {
         const uint64_t t = base + threadIdx.x;
         uint32_t groups = 0;
+        uint32_t finalSt = 0;
         if (t < a.ntiles) {
             const uint32_t w = a.tword[t];
             const uint32_t st = w >> 30;
+            finalSt = st;
             uint32_t slot = w & SLOT_MASK;
             const uint32_t pend = a.tpend[t];
             const bool req = a.treq[t] != 0;
@@ -810,11 +707,22 @@ __global__ void __launch_bounds__(256) k_compact(const __grid_constant__ Compact
                 if (changed) vis = 0;
                 slot = exists ? newSlot : DN_SLOT_NONE;
                 a.treq[t] = (gflag == 3u) ? 1 : 0;
-                a.tword[t] = ((gflag == 3u ? 1u : gflag) << 30) | (slot & SLOT_MASK);
+                finalSt = gflag == 3u ? 1u : gflag;
+                a.tword[t] = (finalSt << 30) | (slot & SLOT_MASK);
             }
             if (pend) a.tpend[t] = 0;
             a.tvis[t] = (uint8_t)vis;
             a.tlast[t] = lu;
+        }
+        // the 2-bit tile map read by the chunk-level DDA step: 32 tiles per warp, two words
+        {
+            const unsigned b0 = __ballot_sync(0xFFFFFFFFu, finalSt == 1u);
+            const unsigned b1 = __ballot_sync(0xFFFFFFFFu, finalSt == 2u);
+            if (lane == 0 && base + threadIdx.x - lane < a.ntiles) {
+                const uint64_t wi = (base + threadIdx.x) >> 4;
+                a.tbits[wi] = spread_bits(b0 & 0xFFFFu) | (spread_bits(b1 & 0xFFFFu) << 1);
+                a.tbits[wi + 1] = spread_bits(b0 >> 16) | (spread_bits(b1 >> 16) << 1);
+            }
         }
         // warp-aggregated append of (tile << 4 | group) request words
         uint32_t incl = groups;
@@ -893,7 +801,7 @@ extern "C" int dn_cuda_sync(DNgpuVolume* g, const dn_sync_params* p, const dn_ti
     }
     CK(cudaMemsetAsync(&g->st->w[ST_REQ], 0, 4, g->stream));
     CompactArgs a;
-    a.tword = g->tword; a.treq = g->treq; a.tvis = g->tvis; a.ttouch = g->ttouch; a.tlast = g->tlast;
+    a.tword = g->tword; a.tbits = g->tbits; a.treq = g->treq; a.tvis = g->tvis; a.ttouch = g->ttouch; a.tlast = g->tlast;
     a.tpend = g->tpend; a.tpendSlot = g->tpendSlot; a.rec = g->rec;
     a.reqs = g->reqs; a.reqCap = g->reqCap; a.st = g->st; a.ntiles = g->ntiles;
     a.op = p->op; a.split = p->split; a.frameNum = p->frameNum;
@@ -912,7 +820,7 @@ static DevMap dev_map(DNgpuVolume* g)
 {
     DevMap m;
     m.sx = g->sx; m.sy = g->sy; m.sz = g->sz;
-    m.tword = g->tword; m.treq = g->treq; m.ttouch = g->ttouch; m.tvis = g->tvis;
+    m.tword = g->tword; m.tbits = g->tbits; m.treq = g->treq; m.ttouch = g->ttouch; m.tvis = g->tvis;
     m.rec = g->rec; m.vox = g->vox; m.diff = g->diff; m.spec = g->spec;
     return m;
 }
@@ -922,21 +830,39 @@ extern "C" int dn_cuda_light(DNgpuVolume* g, const dn_light_params* p, const dn_
     if (!g || !p || !materials) return set_err(DN_CUDA_ERR_ARG, "null argument");
     if (p->K < 1 || p->K > 64) return set_err(DN_CUDA_ERR_ARG, "K = %u", p->K);
     CK(cudaSetDevice(g->device));
-    static thread_local LightArgs* a = nullptr;
-    if (!a) a = new LightArgs();
-    a->m = dev_map(g);
-    a->reqs = g->reqs; a->st = g->st; a->nsamples = g->nsamples; a->out = g->lightOut;
-    a->p = *p;
-    memcpy(a->mats, materials, sizeof(a->mats));
     CK(cudaMemsetAsync(&g->st->w[ST_WORK], 0, 4, g->stream));
-    int perSM = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light, 128, 0));
-    if (perSM < 1) perSM = 1;
+    if (g_lightKernel == 0) {
+        // one voxel per lane in lockstep phases (kept for comparison)
+        static thread_local LightArgs* a = nullptr;
+        if (!a) a = new LightArgs();
+        a->m = dev_map(g);
+        a->reqs = g->reqs; a->st = g->st; a->nsamples = g->nsamples; a->out = g->lightOut;
+        a->p = *p;
+        memcpy(a->mats, materials, sizeof(a->mats));
+        int perSM = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light, 128, 0));
+        if (perSM < 1) perSM = 1;
+        COUNT_LAUNCH();
+        k_light<<<g->numSMs * perSM, 128, 0, g->stream>>>(*a);
+        CK(cudaGetLastError());
+    } else {
+        static thread_local StreamArgs* a = nullptr;
+        if (!a) a = new StreamArgs();
+        a->m = dev_map(g);
+        a->reqs = g->reqs; a->workCounter = &g->st->w[ST_WORK]; a->nreqPtr = &g->st->w[ST_REQ];
+        a->nsamples = g->nsamples; a->out = g->lightOut; a->stats = g->st->lstats;
+        a->batch = g_streamBatch;
+        a->p = *p;
+        memcpy(a->mats, materials, sizeof(a->mats));
+        int perSM = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_stream, 128, 0));
+        if (perSM < 1) perSM = 1;
+        COUNT_LAUNCH();
+        k_light_stream<<<g->numSMs * perSM, 128, 0, g->stream>>>(*a);
+        CK(cudaGetLastError());
+    }
     COUNT_LAUNCH();
-    k_light<<<g->numSMs * perSM, 128, 0, g->stream>>>(*a);
-    CK(cudaGetLastError());
-    COUNT_LAUNCH();
-    k_commit<<<g->numSMs * 4, 256, 0, g->stream>>>(a->m, g->reqs, g->st, g->lightOut, g->diff, g->spec, g->nsamples);
+    k_commit<<<g->numSMs * 4, 256, 0, g->stream>>>(dev_map(g), g->reqs, g->st, g->lightOut, g->diff, g->spec, g->nsamples);
     CK(cudaGetLastError());
     return DN_CUDA_OK;
 }

@@ -150,6 +150,7 @@ struct Counters {             // per-thread traversal counters
 struct DevMap {
     uint32_t sx, sy, sz;
     const uint32_t* __restrict__ tword;  // state << 30 | slot
+    const uint32_t* __restrict__ tbits;  // 2 bits per tile: 0 absent, 1 unloaded, 2 loaded
     uint8_t* treq;
     uint8_t* ttouch;
     uint8_t* tvis;
@@ -364,6 +365,26 @@ __device__ __forceinline__ f3 sky_color(f3 bot, f3 top, f3 dir)
     // voxelShared.comp:289-295 gradient branch; mix(x, y, a) = x*(1-a) + y*a
     float a = dir.y * 0.5f + 1.0f;
     return mk(bot.x * (1.0f - a) + top.x * a, bot.y * (1.0f - a) + top.y * a, bot.z * (1.0f - a) + top.z * a);
+}
+
+// n-th set bit of a chunk mask -> local position; false if n >= popcount
+__device__ __forceinline__ bool select_voxel(const ChunkRec* r, uint32_t n, i3& out, uint32_t& li)
+{
+    uint32_t count = 0;
+    for (uint32_t w = 0; w < 16; w++) {
+        uint32_t bits = __ldg(&r->mask[w]);
+        uint32_t c = __popc(bits);
+        if (count + c > n) {
+            for (uint32_t k = n - count; k > 0; k--) bits &= bits - 1u;   // drop the k lowest set bits
+            uint32_t b = (uint32_t)(__ffs(bits) - 1);
+            uint32_t pos = w * 32u + b;
+            li = pos;
+            out.x = (int32_t)(pos & 7u); out.y = (int32_t)((pos >> 3) & 7u); out.z = (int32_t)(pos >> 6);
+            return true;
+        }
+        count += c;
+    }
+    return false;
 }
 
 } // namespace dn

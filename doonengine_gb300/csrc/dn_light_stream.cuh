@@ -1,0 +1,455 @@
+/*
+ * dn_light_stream.cuh -- the lighting update as persistent per-lane ray streams.
+ *
+ * Every lane of a warp owns one voxel at a time and walks that voxel's ray
+ * jobs in the reference's order (voxelLighting.comp:238-264):
+ *   K specular rays (each up to specBounceLimit segments), then the direct
+ *   light rays (K fixed shadow rays, or one along the sun on the first
+ *   sample), then numDiffuse diffuse paths (each up to diffuseBounceLimit
+ *   segments), then the running average and the write-out.
+ * All lanes share one loop whose body is one traversal step of each lane's
+ * current ray segment (the flattened two-level DDA of dn_light.cuh), so lanes
+ * on different rays, different jobs or different voxels still execute
+ * together.  When a segment ends, the lane waits; the per-segment work
+ * (shading the finished segment, choosing and setting up the next one,
+ * finishing a voxel, fetching the next voxel) runs for all waiting lanes at
+ * once when at least `batch` lanes wait (or no lane is still stepping).
+ * Each lane accumulates its voxel's sums in exactly the order of the
+ * reference loops, so results are bit-identical to the one-voxel-at-a-time
+ * form; only the schedule differs.  Voxels are fetched one per lane from a
+ * warp-local window over the request list, refilled with one atomic per
+ * 32 voxels.
+ */
+#pragma once
+#include "dn_light.cuh"
+
+namespace dn {
+
+enum : uint32_t { PH_FETCH = 0, PH_SPEC = 1, PH_SHADOW = 2, PH_DIFF = 3, PH_FINAL = 4, PH_DONE = 5 };
+
+struct StreamArgs {
+    DevMap m;
+    const uint32_t* reqs;
+    uint32_t* workCounter;
+    const uint32_t* nreqPtr;
+    const uint32_t* nsamples;
+    float4* out;
+    unsigned long long* stats;
+    uint32_t batch;
+    dn_light_params p;
+    Material mats[256];
+};
+
+// traversal state of one ray segment (flattened two-level DDA, refraction off).  Both levels step with
+// the same delta and step signs, so one set of DDA registers (cpos, cside, clast) holds the level being
+// walked; entering a chunk saves the chunk-level registers (opos, oside, olast) and leaving restores them.
+struct Seg {
+    f3 pos, dir, inv;
+    i3 cpos, opos, step;
+    f3 cside, clast, oside, olast, cp;
+    const ChunkRec* rec;
+    uint32_t base;
+    uint32_t flags;      // bit0 inner level, bit1 ignore (current level), bit2 saved outer ignore, bit3 requested
+    f3 cadd;
+    float cmul;
+    TState ts;
+};
+
+__device__ __forceinline__ void seg_begin(Seg& s, f3 pos, f3 dir, f3 inv)
+{
+    // step_map's set-up (voxelShared.comp:421-433) with first voxel ignored
+    s.pos = pos; s.dir = dir; s.inv = inv;
+    s.cadd = mk(0.0f, 0.0f, 0.0f);
+    s.cmul = 1.0f;
+    s.ts.lastVoxID = 255u; s.ts.lastVoxRefract = 1.0f;   // D13: fresh per ray job (spec / diffuse bounces keep it)
+    f3 delta;
+    init_dda(dir, inv, pos, s.cpos, delta, s.step, s.cside);
+    s.clast = mk(0.0f, 0.0f, 0.0f);
+    s.flags = 2u;        // ignore the first voxel
+}
+
+// Advances one traversal step.  Returns 0 while the segment continues, 1 on an opaque hit (s.pos moved to
+// the hit, hitIdx = pool index of the voxel), 2 when it leaves the map.  The common case (a chunk cell that
+// is not loaded, or a voxel cell that is empty) runs one code path for both levels; entering a chunk, leaving
+// it, reaching a voxel and leaving the map are the divergent events.
+__device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Material* mats, f3 sunStrength,
+                                             Counters& c, uint32_t& hitIdx)
+{
+    const f3 delta = vabs(s.inv);
+    const i3 step = s.step;
+    const bool inner = (s.flags & 1u) != 0u;
+    const uint32_t bx = inner ? 8u : m.sx, by = inner ? 8u : m.sy, bz = inner ? 8u : m.sz;
+    const bool inb = (uint32_t)s.cpos.x < bx && (uint32_t)s.cpos.y < by && (uint32_t)s.cpos.z < bz;
+    const uint32_t idx = (uint32_t)s.cpos.x + bx * ((uint32_t)s.cpos.y + by * (uint32_t)s.cpos.z);
+    uint32_t w = 0;
+    if (inb) w = __ldg(inner ? &s.rec->mask[idx >> 5] : &m.tbits[idx >> 4]);
+    // chunk level: 2-bit state (0 absent, 1 unloaded, 2 loaded); voxel level: occupancy bit
+    const uint32_t cst = (w >> ((idx & 15u) * 2u)) & 3u;
+    const bool occ = inb && (inner ? ((((w >> (idx & 31)) & 1u) != 0u) && !(s.flags & 2u)) : (cst == 2u));
+    if (!inb || occ) {
+        if (!inner) {
+            if (!inb) return 2u;
+            // a loaded chunk: enter it (voxelShared.comp:441-449)
+            c.outer++;
+            c.entered++;
+            if (m.ttouch[idx] == 0) m.ttouch[idx] = 1;
+            const float tt = min3(s.clast) - EPS;
+            const f3 up = add(s.pos, muls(s.dir, tt));
+            f3 cp = mk((up.x - (float)s.cpos.x) * 8.0f, (up.y - (float)s.cpos.y) * 8.0f, (up.z - (float)s.cpos.z) * 8.0f);
+            const float lo = EPS, hi_ = 8.0f - EPS;
+            cp.x = gmin(gmax(cp.x, lo), hi_); cp.y = gmin(gmax(cp.y, lo), hi_); cp.z = gmin(gmax(cp.z, lo), hi_);
+            s.cp = cp;
+            s.opos = s.cpos; s.oside = s.cside; s.olast = s.clast;
+            const f3 fl = vfloor(cp);
+            s.cpos.x = f2i(fl.x); s.cpos.y = f2i(fl.y); s.cpos.z = f2i(fl.z);
+            const f3 sg = mk((float)step.x, (float)step.y, (float)step.z);
+            s.cside.x = (sg.x * ((float)s.cpos.x - cp.x) + sg.x * 0.5f + 0.5f) * delta.x;
+            s.cside.y = (sg.y * ((float)s.cpos.y - cp.y) + sg.y * 0.5f + 0.5f) * delta.y;
+            s.cside.z = (sg.z * ((float)s.cpos.z - cp.z) + sg.z * 0.5f + 0.5f) * delta.z;
+            s.clast = mk(0.0f, 0.0f, 0.0f);
+            s.rec = &m.rec[__ldg(&m.tword[idx]) & SLOT_MASK];
+            s.base = __ldg(&s.rec->voxBase);
+            s.flags = (s.flags & ~4u) | 1u | ((s.flags & 2u) << 1);   // inner level; the chunk inherits ignoreFirst
+            return 0u;
+        }
+        if (!inb) {
+            // the chunk was crossed without a hit: back to the chunk level, which then iterates
+            s.cpos = s.opos; s.cside = s.oside; s.clast = s.olast;
+            s.flags = (s.flags & ~3u) | ((s.flags >> 1) & 2u);
+        } else {
+            c.inner++;
+            c.hits++;
+            const uint32_t vi = s.base + vox_rank(s.rec, idx);
+            const uint2 vw = __ldg(&m.vox[vi]);
+            const uint32_t material = vw.x >> 24;
+            const Material& mat = mats[material];
+            if (mat.opacity == 1.0f) {
+                const float t = min3(s.clast) + EPS;
+                const f3 cp = add(s.cp, muls(s.dir, t));
+                s.pos = add(mk((float)s.opos.x, (float)s.opos.y, (float)s.opos.z), muls(cp, INV_CHUNK));
+                hitIdx = vi;
+                return 1u;
+            }
+            const uint32_t thisID = (vw.y & 0xFFFFFF00u) | material;
+            if (s.ts.lastVoxID != thisID) {
+                const f3 alb = mk((float)((vw.y >> 24) & 0xFF) * INV255, (float)((vw.y >> 16) & 0xFF) * INV255,
+                                  (float)((vw.y >> 8) & 0xFF) * INV255);
+                const float k = s.cmul * mat.opacity;
+                s.cadd.x = s.cadd.x + k * alb.x * sunStrength.x;
+                s.cadd.y = s.cadd.y + k * alb.y * sunStrength.y;
+                s.cadd.z = s.cadd.z + k * alb.z * sunStrength.z;
+                s.cmul = s.cmul * (1.0f - mat.opacity);
+                s.ts.lastVoxID = thisID;
+                s.ts.lastVoxRefract = mat.refractIndex;
+            }
+        }
+    } else if (inner) {
+        c.inner++;
+        if (s.ts.lastVoxID != 255u) { s.ts.lastVoxID = 255u; s.ts.lastVoxRefract = 1.0f; }
+    } else {
+        c.outer++;
+        if (!(s.flags & 8u) && cst != 0u) {
+            if (m.treq[idx] == 0) m.treq[idx] = 1;
+            s.flags |= 8u;
+        }
+    }
+    // iterate_DDA on the current level (voxelShared.comp:309-317)
+    s.clast = s.cside;
+    const bool mx = s.cside.x <= gmin(s.cside.y, s.cside.z);
+    const bool my = s.cside.y <= gmin(s.cside.z, s.cside.x);
+    const bool mz = s.cside.z <= gmin(s.cside.x, s.cside.y);
+    s.cside.x = s.cside.x + (mx ? 1.0f : 0.0f) * delta.x;
+    s.cside.y = s.cside.y + (my ? 1.0f : 0.0f) * delta.y;
+    s.cside.z = s.cside.z + (mz ? 1.0f : 0.0f) * delta.z;
+    s.cpos.x += (int32_t)mx * step.x; s.cpos.y += (int32_t)my * step.y; s.cpos.z += (int32_t)mz * step.z;
+    s.flags &= ~2u;
+    return 0u;
+}
+
+__device__ __forceinline__ f3 rcp3(f3 d) { return mk(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z)); }
+
+// per-lane job state of the voxel being lit
+struct Job {
+    uint32_t phase, k, b, i;
+    uint32_t req, vlane, vidx;      // request, lane within it, pool index of the voxel
+    f3 pos0, tnormal, talbedo, refl;
+    uint32_t tmat, key;
+    float indirect;
+    bool firstSample, doSpec, doDiff;
+    f3 spec, direct, acc;           // acc: shadow sum, then diffuse sum
+    f3 jA, jB, jC;                  // spec: mult, lastPos ; diffuse: nc, hitNormal, lastDir
+    uint32_t jU;                    // spec: reflectType ; diffuse: material of the last hit
+};
+
+} // namespace dn
+
+namespace dn {
+
+__device__ __forceinline__ uint32_t lane_id_s()
+{
+    uint32_t l;
+    asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
+    return l;
+}
+
+struct StreamShared {
+    Material mats[256];
+    float sdir[65][3];   // shadow directions k < K, [64]: the first-sample direction sunDir + EPS
+    float sinv[65][3];
+};
+
+// diffuse bounce direction (voxelLighting.comp:160-168)
+__device__ __forceinline__ f3 diffuse_dir(const Job& j, const dn_light_params& p, const Material* mats, bool rngSin)
+{
+    const Material& hm = mats[j.jU];
+    bool lobe = false;
+    const float seed = p.time * (float)(j.i + 1u);
+    if (j.b > 0) {
+        const float r = rngSin ? srand1(seed + (float)p.diffuseBounceLimit + (float)j.b)
+                               : hrand(j.key, 2u, (j.i * 16u + j.b) << 8);
+        lobe = (r + 1.0f) * 0.5f < hm.specular;
+    }
+    if (lobe) {
+        const f3 rs = rngSin ? sphere_sin(p.time + (float)j.b) : sphere_hash(j.key, 3u, j.i * 16u + j.b);
+        return normalize(add(muls(reflect(j.jC, j.jB), (float)hm.shininess), rs));
+    }
+    if (j.firstSample) return adds(normalize(j.jB), EPS);
+    const f3 rs = rngSin ? sphere_sin(seed + (float)j.b) : sphere_hash(j.key, 1u, j.i * 16u + j.b);
+    return adds(normalize(add(j.jB, rs)), EPS);
+}
+
+// Consumes the finished segment (hitState 1 hit / 2 miss) and sets up the next segment of this lane's
+// voxel; returns true when a segment was started.  Leaves the job in PH_FETCH when the voxel is done.
+__device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint32_t hitIdx, const StreamArgs& a,
+                                        const StreamShared& sh, Counters& c, uint32_t& lit)
+{
+    const dn_light_params& p = a.p;
+    const DevMap& m = a.m;
+    const bool rngSin = p.rngMode == 1u;
+    const f3 sun = mk(p.sunStrength[0], p.sunStrength[1], p.sunStrength[2]);
+    const f3 sunDir = mk(p.sunDir[0], p.sunDir[1], p.sunDir[2]);
+    if (hitState) {
+        const bool hit = hitState == 1u;
+        hitState = 0;
+        Voxel hv;
+        if (hit) decompress(m, hitIdx, hv);
+        if (j.phase == PH_SPEC) {
+            // specular_ray body after step_map (voxelLighting.comp:98-144)
+            bool done = true;
+            if (hit) {
+                const i3 hp{f2i(truncf(s.pos.x)), f2i(truncf(s.pos.y)), f2i(truncf(s.pos.z))};
+                if (in_map(m, hp)) {
+                    uint8_t* vp = &m.tvis[map_index(m, hp)];
+                    if (*vp == 0) *vp = 1;
+                }
+                const f3 d = vabs(sub(vfloor(muls(s.pos, 8.0f)), vfloor(muls(j.jB, 8.0f))));
+                if (!(dot(d, d) <= 1.0f)) {
+                    const Material& hm = sh.mats[hv.material];
+                    const f3 hd = muls(hv.diff, 1.0f - hm.specular);
+                    if (hm.emissive) {
+                        j.spec.x = j.spec.x + ((hv.albedo.x * p.emissiveStrength * s.cmul + s.cadd.x) * j.jA.x) * j.talbedo.x;
+                        j.spec.y = j.spec.y + ((hv.albedo.y * p.emissiveStrength * s.cmul + s.cadd.y) * j.jA.y) * j.talbedo.y;
+                        j.spec.z = j.spec.z + ((hv.albedo.z * p.emissiveStrength * s.cmul + s.cadd.z) * j.jA.z) * j.talbedo.z;
+                    } else {
+                        const f3 hc = mul(hd, hv.albedo);
+                        j.spec.x = j.spec.x + (hc.x * s.cmul + s.cadd.x) * j.jA.x;
+                        j.spec.y = j.spec.y + (hc.y * s.cmul + s.cadd.y) * j.jA.y;
+                        j.spec.z = j.spec.z + (hc.z * s.cmul + s.cadd.z) * j.jA.z;
+                        if (hm.specular != 0.0f) {
+                            j.jA.x = j.jA.x * (hv.albedo.x * s.cmul * hm.specular);
+                            j.jA.y = j.jA.y * (hv.albedo.y * s.cmul * hm.specular);
+                            j.jA.z = j.jA.z * (hv.albedo.z * s.cmul * hm.specular);
+                            j.jU = hm.reflectType;
+                            j.jB = s.pos;
+                            const f3 nd = reflect(s.dir, hv.normal);
+                            j.b++;
+                            if (j.b < p.specBounceLimit) {
+                                const TState keep = s.ts;
+                                seg_begin(s, s.pos, nd, rcp3(nd));   // next bounce
+                                s.ts = keep;      // one ray job: bounces keep the transparency state
+                                c.rays++;
+                                return true;
+                            }
+                        }
+                    }
+                }
+            } else if (dot(s.dir, sunDir) > 0.99f) {
+                j.spec.x = j.spec.x + (sun.x * s.cmul + s.cadd.x);
+                j.spec.y = j.spec.y + (sun.y * s.cmul + s.cadd.y);
+                j.spec.z = j.spec.z + (sun.z * s.cmul + s.cadd.z);
+            } else {
+                const f3 sc = (j.jU == 1u) ? sky_color(mk(p.skyBot[0], p.skyBot[1], p.skyBot[2]),
+                                                      mk(p.skyTop[0], p.skyTop[1], p.skyTop[2]), s.dir) : sun;
+                j.spec.x = j.spec.x + (sc.x * s.cmul + s.cadd.x) * j.jA.x;
+                j.spec.y = j.spec.y + (sc.y * s.cmul + s.cadd.y) * j.jA.y;
+                j.spec.z = j.spec.z + (sc.z * s.cmul + s.cadd.z) * j.jA.z;
+            }
+            if (done) { j.k++; j.b = 0; }
+        } else if (j.phase == PH_SHADOW) {
+            if (!hit) {
+                j.acc.x = j.acc.x + (sun.x * s.cmul + s.cadd.x);
+                j.acc.y = j.acc.y + (sun.y * s.cmul + s.cadd.y);
+                j.acc.z = j.acc.z + (sun.z * s.cmul + s.cadd.z);
+            }
+            j.k++;
+        } else if (j.phase == PH_DIFF) {
+            // diffuse_ray body after step_map (voxelLighting.comp:176-201)
+            bool pathDone = true;
+            if (hit) {
+                j.jB = hv.normal;
+                j.jU = hv.material;
+                const f3 d = vabs(sub(vfloor(muls(j.pos0, 8.0f)), vfloor(muls(s.pos, 8.0f))));
+                if (!(dot(d, d) < 1.0f)) {
+                    const Material& hm = sh.mats[hv.material];
+                    if (hm.emissive) {
+                        j.acc.x = j.acc.x + j.jA.x * (hv.albedo.x * p.emissiveStrength * s.cmul + s.cadd.x);
+                        j.acc.y = j.acc.y + j.jA.y * (hv.albedo.y * p.emissiveStrength * s.cmul + s.cadd.y);
+                        j.acc.z = j.acc.z + j.jA.z * (hv.albedo.z * p.emissiveStrength * s.cmul + s.cadd.z);
+                    } else {
+                        j.jA.x = j.jA.x * (hv.albedo.x * s.cmul + s.cadd.x);
+                        j.jA.y = j.jA.y * (hv.albedo.y * s.cmul + s.cadd.y);
+                        j.jA.z = j.jA.z * (hv.albedo.z * s.cmul + s.cadd.z);
+                        j.jC = s.dir;
+                        j.b++;
+                        if (j.b < p.diffuseBounceLimit) {
+                            const f3 nd = diffuse_dir(j, p, sh.mats, rngSin);
+                            const TState keep = s.ts;
+                            seg_begin(s, s.pos, nd, rcp3(nd));
+                            s.ts = keep;
+                            c.rays++;
+                            return true;
+                        }
+                    }
+                }
+            } else {
+                const float k = gmax(dot(s.dir, sunDir), 0.0f);
+                j.acc.x = j.acc.x + (j.jA.x * k * sun.x * s.cmul + s.cadd.x);
+                j.acc.y = j.acc.y + (j.jA.y * k * sun.y * s.cmul + s.cadd.y);
+                j.acc.z = j.acc.z + (j.jA.z * k * sun.z * s.cmul + s.cadd.z);
+            }
+            if (pathDone) { j.acc = add(j.acc, j.direct); j.i++; j.b = 0; }
+        }
+    }
+    // start the next segment of this voxel
+    for (int guard = 0; guard < 8; guard++) {
+        if (j.phase == PH_SPEC) {
+            if (j.k < p.K) {
+                if (p.specBounceLimit == 0u) { j.k++; continue; }
+                const Material& tm = sh.mats[j.tmat];
+                j.b = 0; j.jA = j.talbedo; j.jB = j.pos0; j.jU = tm.reflectType;
+                const f3 P = mk(p.spherePts[j.k][0], p.spherePts[j.k][1], p.spherePts[j.k][2]);
+                const f3 sd = adds(normalize(add(muls(j.refl, (float)tm.shininess), P)), EPS);
+                seg_begin(s, j.pos0, sd, rcp3(sd));
+                c.rays++;
+                return true;
+            }
+            j.spec = divs(j.spec, (float)p.K);
+            j.phase = j.doDiff ? PH_SHADOW : PH_FINAL;
+            j.k = 0;
+            continue;
+        }
+        if (j.phase == PH_SHADOW) {
+            const uint32_t n = j.firstSample ? 1u : p.K;
+            if (j.k < n) {
+                const uint32_t q = j.firstSample ? 64u : j.k;
+                seg_begin(s, j.pos0, mk(sh.sdir[q][0], sh.sdir[q][1], sh.sdir[q][2]),
+                          mk(sh.sinv[q][0], sh.sinv[q][1], sh.sinv[q][2]));
+                c.rays++;
+                return true;
+            }
+            j.direct = divs(j.acc, (float)n);
+            j.acc = mk(0.0f, 0.0f, 0.0f);
+            j.phase = PH_DIFF;
+            j.i = 0; j.b = 0;
+            continue;
+        }
+        if (j.phase == PH_DIFF) {
+            if (j.i < p.numDiffuse) {
+                if (j.b == 0) {
+                    const f3 amb = mk(p.ambient[0], p.ambient[1], p.ambient[2]);
+                    j.acc = add(j.acc, amb);
+                    if (p.diffuseBounceLimit == 0u) { j.acc = add(j.acc, j.direct); j.i++; continue; }
+                    j.jA = mk(1.0f, 1.0f, 1.0f);
+                    j.jB = adds(j.tnormal, EPS);
+                    j.jC = mk(0.0f, 0.0f, 0.0f);
+                    j.jU = j.tmat;
+                }
+                const f3 nd = diffuse_dir(j, p, sh.mats, rngSin);
+                seg_begin(s, j.pos0, nd, rcp3(nd));
+                c.rays++;
+                return true;
+            }
+            const float4 prev = __ldg(&m.diff[j.vidx]);
+            const float den = j.indirect + (float)p.numDiffuse;
+            j.acc.x = (prev.x * j.indirect + j.acc.x) / den;
+            j.acc.y = (prev.y * j.indirect + j.acc.y) / den;
+            j.acc.z = (prev.z * j.indirect + j.acc.z) / den;
+            j.phase = PH_FINAL;
+            continue;
+        }
+        if (j.phase == PH_FINAL) {
+            const float4 outS = make_float4(gmin(gmax(j.spec.x, 0.0f), 1.0f), gmin(gmax(j.spec.y, 0.0f), 1.0f),
+                                            gmin(gmax(j.spec.z, 0.0f), 1.0f), 0.0f);
+            const float4 outD = make_float4(gmin(gmax(j.acc.x, 0.0f), 1.0f), gmin(gmax(j.acc.y, 0.0f), 1.0f),
+                                            gmin(gmax(j.acc.z, 0.0f), 1.0f), 0.0f);
+            const uint64_t o = ((uint64_t)j.req * 32u + j.vlane) * 2u;
+            a.out[o] = outD;
+            a.out[o + 1] = outS;
+            lit++;
+            j.phase = PH_FETCH;
+        }
+        return false;
+    }
+    return false;
+}
+
+// Sets up voxel (req, vlane); returns false (and writes zero outputs) when the slot holds no voxel.
+__device__ __forceinline__ bool voxel_setup(Job& j, uint32_t req, uint32_t vlane, const StreamArgs& a, const StreamShared& sh)
+{
+    const DevMap& m = a.m;
+    const dn_light_params& p = a.p;
+    j.req = req; j.vlane = vlane;
+    const uint32_t word = a.reqs[req];
+    const uint32_t tile = word >> 4, group = word & 15u;
+    const uint32_t tw = __ldg(&m.tword[tile]);
+    const uint32_t vn = group * 32u + vlane;
+    i3 cp; uint32_t li;
+    const ChunkRec* rc = &m.rec[tw & SLOT_MASK];
+    if ((tw >> 30) != 2u || vn >= __ldg(&rc->nvox) || !select_voxel(rc, vn, cp, li)) {
+        const uint64_t o = ((uint64_t)req * 32u + vlane) * 2u;
+        a.out[o] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        a.out[o + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return false;
+    }
+    const i3 mp{__ldg(&rc->pos[0]), __ldg(&rc->pos[1]), __ldg(&rc->pos[2])};
+    j.vidx = __ldg(&rc->voxBase) + vn;
+    const uint2 w = __ldg(&m.vox[j.vidx]);
+    j.tnormal = mk(((float)((w.x >> 16) & 0xFF) * INV255 - 0.5f) * 2.0f, ((float)((w.x >> 8) & 0xFF) * INV255 - 0.5f) * 2.0f,
+                   ((float)(w.x & 0xFF) * INV255 - 0.5f) * 2.0f);
+    j.tmat = w.x >> 24;
+    j.talbedo = mk((float)((w.y >> 24) & 0xFF) * INV255, (float)((w.y >> 16) & 0xFF) * INV255,
+                   (float)((w.y >> 8) & 0xFF) * INV255);
+    const uint32_t samples = __ldg(&a.nsamples[tw & SLOT_MASK]);
+    const uint32_t ns = samples < p.maxDiffuse ? samples : p.maxDiffuse;
+    j.indirect = (float)ns;
+    j.firstSample = (j.indirect == 0.0f);
+    const uint32_t gx = (uint32_t)(mp.x * 8 + cp.x), gy = (uint32_t)(mp.y * 8 + cp.y), gz = (uint32_t)(mp.z * 8 + cp.z);
+    j.key = rng_key(__float_as_uint(p.time), p.mapId, gx + (m.sx * 8u) * (gy + (m.sy * 8u) * gz));
+    f3 rp;
+    rp.x = INV_CHUNK * (float)cp.x + (float)mp.x + HALF_INV_CHUNK;
+    rp.y = INV_CHUNK * (float)cp.y + (float)mp.y + HALF_INV_CHUNK;
+    rp.z = INV_CHUNK * (float)cp.z + (float)mp.z + HALF_INV_CHUNK;
+    const float off = HALF_INV_CHUNK - EPS;
+    j.pos0 = add(rp, muls(j.tnormal, off));
+    const Material& tm = sh.mats[j.tmat];
+    const f3 viewDir = sub(j.pos0, mk(p.camPos[0], p.camPos[1], p.camPos[2]));
+    j.doSpec = tm.specular > 0.0f && dot(viewDir, j.tnormal) < 0.0f && tm.reflectType <= 1u;
+    j.doDiff = tm.specular < 1.0f;
+    if (j.doSpec) j.refl = reflect(normalize(viewDir), j.tnormal);
+    j.spec = mk(0.0f, 0.0f, 0.0f); j.acc = j.spec; j.direct = j.spec;
+    j.k = 0; j.b = 0; j.i = 0;
+    j.phase = j.doSpec ? PH_SPEC : (j.doDiff ? PH_SHADOW : PH_FINAL);
+    return true;
+}
+
+} // namespace dn
