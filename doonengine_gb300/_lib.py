@@ -86,6 +86,15 @@ class DNstats(Structure):
                 ("innerSteps", c_uint64), ("hits", c_uint64), ("litVoxels", c_uint64)]
 
 
+class DnLightParams(Structure):
+    """dn_light_params of include/dn_cuda.h"""
+    _fields_ = [("sunDir", c_float * 3), ("sunStrength", c_float * 3), ("ambient", c_float * 3), ("camPos", c_float * 3),
+                ("skyBot", c_float * 3), ("skyTop", c_float * 3), ("shadowSoftness", c_float), ("time", c_float),
+                ("emissiveStrength", c_float), ("numDiffuse", c_uint32), ("maxDiffuse", c_uint32),
+                ("diffuseBounceLimit", c_uint32), ("specBounceLimit", c_uint32), ("K", c_uint32), ("rngMode", c_uint32),
+                ("mapId", c_uint32), ("spherePts", (c_float * 3) * 64)]
+
+
 MESSAGE_CALLBACK = ctypes.CFUNCTYPE(None, c_int, c_int, c_char_p)
 VOLP = POINTER(DNvolume)
 
@@ -153,6 +162,7 @@ _SIGS = [
     ("dn_cuda_reserve", c_int, [c_void_p, c_uint32, c_uint64, c_uint64]),
     ("dn_cuda_sync", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p, c_uint32, c_void_p, c_uint64]),
     ("dn_cuda_light", c_int, [c_void_p, c_void_p, c_void_p]),
+    ("dn_cuda_light_noalloc", c_int, [c_void_p, c_void_p, c_void_p]),
     ("dn_cuda_draw", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("dn_cuda_draw_host", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("dn_cuda_finish", c_int, [c_void_p, POINTER(c_uint64)]),

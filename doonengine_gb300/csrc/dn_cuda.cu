@@ -20,6 +20,7 @@
 #include <string.h>
 #include <stdlib.h>
 #include <new>
+#include <mutex>
 #include <stdarg.h>
 
 using namespace dn;
@@ -863,6 +864,82 @@ extern "C" int dn_cuda_light(DNgpuVolume* g, const dn_light_params* p, const dn_
     }
     COUNT_LAUNCH();
     k_commit<<<g->numSMs * 4, 256, 0, g->stream>>>(dev_map(g), g->reqs, g->st, g->lightOut, g->diff, g->spec, g->nsamples);
+    CK(cudaGetLastError());
+    return DN_CUDA_OK;
+}
+
+// ------------------------------------------------- lighting without allocation
+//
+// The lighting update keeps the new lighting of every request lane in scratch memory until the commit
+// kernel copies it into the voxel pool.  dn_cuda_light uses the volume's own scratch, which
+// dn_cuda_sync grows with cudaMalloc as the map's lit set grows.  Some callers cannot allow that:
+// a render loop that runs under a fixed device-memory budget, or a host engine that hands out all
+// device memory through its own allocator and forbids ad-hoc cudaMalloc / cudaFree while a frame is
+// in flight.  dn_cuda_light_noalloc serves them: its scratch is the fixed array below, part of this
+// library's device image (every GPU that loads the library holds it until the process exits), so the
+// call itself allocates nothing on the device or the host.
+//
+// Limit: DN_NOALLOC_MAX_REQUESTS request groups (32 voxels each) per call; larger request lists are
+// rejected with DN_CUDA_ERR_CAPACITY and a message naming both numbers.
+// The array's device address is looked up once per device, on that device's first call (with the
+// device current); that first call should come before any stream capture.  Every call shares the
+// array and it keeps the previous call's contents: nothing in it needs to start at zero, because each
+// call writes every slot it later reads.  Calls that overlap on the GPU (two volumes lit concurrently
+// on different streams) race on the array.
+#define DN_NOALLOC_MAX_REQUESTS 8192u   // 8192 groups x 32 lanes x 2 float4 = 8 MiB
+static __device__ __align__(256) float4 g_noallocScratch[DN_NOALLOC_MAX_REQUESTS * 32u * 2u];
+
+static std::mutex g_noallocMutex;
+static float4* g_noallocAddr[64];      // device address of g_noallocScratch, per device ordinal
+
+static int noalloc_scratch(int device, float4** out)
+{
+    if (device < 0 || device >= 64) return set_err(DN_CUDA_ERR_DEVICE, "device ordinal %d out of range", device);
+    std::lock_guard<std::mutex> lock(g_noallocMutex);
+    if (!g_noallocAddr[device]) {
+        float4* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noallocScratch);   // the device is current
+        if (e != cudaSuccess || !ptr)
+            return set_err(DN_CUDA_ERR_LAUNCH, "cudaGetSymbolAddress of the fixed lighting scratch: %s", cudaGetErrorString(e));
+        g_noallocAddr[device] = ptr;
+    }
+    *out = g_noallocAddr[device];
+    return DN_CUDA_OK;
+}
+
+extern "C" int dn_cuda_light_noalloc(DNgpuVolume* g, const dn_light_params* p, const dn_material* materials)
+{
+    if (!g || !p || !materials) return set_err(DN_CUDA_ERR_ARG, "null argument");
+    if (p->K < 1 || p->K > 64) return set_err(DN_CUDA_ERR_ARG, "K = %u", p->K);
+    CK(cudaSetDevice(g->device));
+    float4* scratch = nullptr;
+    int rc = noalloc_scratch(g->device, &scratch);
+    if (rc) return rc;
+    // the request count exists only on the device: read it into the volume's pinned state block
+    CK(cudaMemcpyAsync(&g->hst->w[ST_REQ], &g->st->w[ST_REQ], sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    const uint32_t nreq = g->hst->w[ST_REQ];
+    if (nreq > DN_NOALLOC_MAX_REQUESTS)
+        return set_err(DN_CUDA_ERR_CAPACITY,
+                       "dn_cuda_light_noalloc: %u lighting request groups exceed the fixed scratch of %u groups "
+                       "(%u voxels); use dn_cuda_light for this map", nreq, DN_NOALLOC_MAX_REQUESTS,
+                       DN_NOALLOC_MAX_REQUESTS * 32u);
+    CK(cudaMemsetAsync(&g->st->w[ST_WORK], 0, 4, g->stream));
+    StreamArgs a;                       // launch arguments on the stack: no host allocation either
+    a.m = dev_map(g);
+    a.reqs = g->reqs; a.workCounter = &g->st->w[ST_WORK]; a.nreqPtr = &g->st->w[ST_REQ];
+    a.nsamples = g->nsamples; a.out = scratch; a.stats = g->st->lstats;
+    a.batch = g_streamBatch;
+    a.p = *p;
+    memcpy(a.mats, materials, sizeof(a.mats));
+    int perSM = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_stream, 128, 0));
+    if (perSM < 1) perSM = 1;
+    COUNT_LAUNCH();
+    k_light_stream<<<g->numSMs * perSM, 128, 0, g->stream>>>(a);
+    CK(cudaGetLastError());
+    COUNT_LAUNCH();
+    k_commit<<<g->numSMs * 4, 256, 0, g->stream>>>(dev_map(g), g->reqs, g->st, scratch, g->diff, g->spec, g->nsamples);
     CK(cudaGetLastError());
     return DN_CUDA_OK;
 }

@@ -120,6 +120,17 @@ int dn_cuda_sync(struct DNgpuVolume* g, const dn_sync_params* p,
 /* --- lighting: replaces glDispatchCompute(numLightingRequests) of DN_update_lighting (voxel.c:950) --- */
 int dn_cuda_light(struct DNgpuVolume* g, const dn_light_params* p, const dn_material* materials);
 
+/* Lighting update that allocates nothing (no counterpart in the reference, which has no such
+ * constraint).  For callers that must not allocate device memory while a frame is in flight -- a render
+ * loop under a fixed device-memory budget, or a host engine whose own allocator owns all device memory --
+ * the per-request scratch that dn_cuda_light keeps in the volume (grown with cudaMalloc by dn_cuda_sync)
+ * is replaced by a fixed 8 MiB array in the library's device image, held by every GPU that loads the
+ * library until the process exits.  Same inputs and outputs as dn_cuda_light and the same results.
+ * Limit: 8192 request groups (262144 voxels) per call; more returns DN_CUDA_ERR_CAPACITY with a message.
+ * The first call on a device looks up the array's device address (with that device current); make that
+ * first call before any stream capture.  Calls share the array: calls that overlap on the GPU race. */
+int dn_cuda_light_noalloc(struct DNgpuVolume* g, const dn_light_params* p, const dn_material* materials);
+
 /* --- draw: replaces glDispatchCompute(w/16, h/16) of DN_draw (voxel.c:879); outputs are device pointers --- */
 int dn_cuda_draw(struct DNgpuVolume* g, const dn_draw_params* p, const dn_material* materials,
                  float* colorOut, uint32_t* hitOut, uint8_t* faceOut);
