@@ -147,6 +147,7 @@ _SIGS = [
     ("DN_mat4_inv", DNmat4, [DNmat4]),
     ("DN_mat4_mult", DNmat4, [DNmat4, DNmat4]),
     ("DN_vec3_normalize", DNvec3, [DNvec3]),
+    ("dn_pack_chunk", c_uint32, [VOLP, POINTER(DNchunk), c_void_p, c_void_p, c_void_p]),
     ("dn_scene_palette", None, [VOLP, c_uint32, c_uint32, c_uint32, c_float, c_float, c_float]),
     ("dn_scene_terrain", None, [VOLP, c_uint32, c_float, c_float, c_uint32, c_uint32]),
     ("dn_scene_shapes", None, [VOLP, c_uint32, c_uint32, c_int32, c_int32, c_uint32, c_float, c_float]),

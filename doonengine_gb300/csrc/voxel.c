@@ -1044,3 +1044,16 @@ size_t DN_abi_layout(uint64_t* out, size_t n)
 	for (size_t i = 0; i < n && i < k; i++) out[i] = v[i];
 	return k;
 }
+
+/* addition: the chunk packing DN_sync_gpu applies to every changed chunk (voxel.c:1397-1461), exported
+ * for tests and tools: mask[16], partial[3], 2 words per surface voxel; returns the voxel count */
+uint32_t dn_pack_chunk(const DNvolume* vol, const DNchunk* chunk, uint32_t mask[16], uint32_t partial[3], uint32_t* words)
+{
+	static int tableReady = 0;
+	if (!tableReady) { init_linear_table(); tableReady = 1; }
+	dn_chunk_record r;
+	uint32_t n = pack_chunk(vol, chunk, &r, words);
+	memcpy(mask, r.mask, sizeof(r.mask));
+	memcpy(partial, r.partial, sizeof(r.partial));
+	return n;
+}

@@ -254,6 +254,11 @@ DNvolume* DN_create_volume_cpu(DNuvec3 mapSize, unsigned int minChunks);
 size_t DN_compress_chunk(const DNvolume* vol, const DNchunk* chunk, uint8_t* mem);
 int DN_decompress_chunk(const DNvolume* vol, const uint8_t* mem, size_t size, DNchunk* chunk);
 
+/* The packing DN_sync_gpu applies to a changed chunk (surface cull, 512-bit occupancy mask, partial
+ * counts at 128/256/384, linearised albedo; voxel.c:1397-1461).  words: 2 per surface voxel (normal
+ * word, linear albedo word), room for 512 voxels.  Returns the surface voxel count. */
+uint32_t dn_pack_chunk(const DNvolume* vol, const DNchunk* chunk, uint32_t mask[16], uint32_t partial[3], uint32_t* words);
+
 /* Struct sizes and field offsets for language bindings; returns the number of entries. */
 size_t DN_abi_layout(uint64_t* out, size_t n);
 
