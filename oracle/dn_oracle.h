@@ -8,13 +8,17 @@
  * against and the timed CPU baseline; the product library never links,
  * loads or calls it.
  *
- * Parity status: the reference has no tests and its hot path exists only as
- * GLSL, which cannot run on these machines.  The host-side pieces (voxel
- * codec, chunk packing, camera, CPU picking ray) are pinned against the
- * reference's own C compiled from its sources (oracle/ref/).  The shader
- * transcription is pinned by running the reference shader text itself as
- * C++ through a GLSL shim (oracle/ref/glsl_pin), in the reference-faithful
- * RNG mode.
+ * Parity status: pinned.  The reference has no tests and its hot path exists
+ * only as GLSL, which cannot run on these machines through a graphics API.
+ * The host-side pieces (voxel codec, chunk packing, edit API, camera, CPU
+ * picking ray, .voxvol codec) are pinned against the reference's own C
+ * compiled from its sources (oracle/ref/dnref_shim.c); the shader
+ * transcription is pinned by running the reference's shader source itself
+ * on the CPU, translated to C++ (oracle/ref/glsl_to_cpp.py, glsl_shim.hpp,
+ * pin_harness.cpp), in this oracle's reference-faithful modes
+ * (DNO_RNG_SIN | DNO_PERSIST_TRANSPARENCY | DNO_REFERENCE_SHADOW with the
+ * shader's 15-point table).  Only the sine both sides use is this project's
+ * deterministic sine rather than a GPU's.
  *
  * Deterministic semantics where the reference races or is undefined
  * (numbered D1..D15, each applied identically here and in the kernels):
