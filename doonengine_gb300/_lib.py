@@ -98,6 +98,20 @@ class DnLightParams(Structure):
 MESSAGE_CALLBACK = ctypes.CFUNCTYPE(None, c_int, c_int, c_char_p)
 VOLP = POINTER(DNvolume)
 
+PHASE_DRAW, PHASE_SYNC, PHASE_LIGHT = 1, 2, 4
+
+
+class DNbatchItem(Structure):
+    """DNbatchItem of include/DoonEngine/voxel.h"""
+    _fields_ = [("vol", VOLP), ("phases", c_uint32), ("output", POINTER(DNimage)), ("view", DNmat4),
+                ("projection", DNmat4), ("op", c_int), ("lightingSplit", c_int), ("numDiffuseSamples", c_int),
+                ("maxDiffuseSamples", c_int), ("time", c_float)]
+
+
+class DnBatchTuning(Structure):
+    """dn_batch_tuning of include/dn_cuda.h"""
+    _fields_ = [("streamBatch", c_uint32), ("blocksPerSM", c_uint32), ("useGraph", c_uint32)]
+
 # (name, restype, argtypes)
 _SIGS = [
     ("DN_init", c_bool, []),
@@ -147,6 +161,15 @@ _SIGS = [
     ("DN_mat4_inv", DNmat4, [DNmat4]),
     ("DN_mat4_mult", DNmat4, [DNmat4, DNmat4]),
     ("DN_vec3_normalize", DNvec3, [DNvec3]),
+    ("DN_batch_create", c_void_p, []),
+    ("DN_batch_destroy", None, [c_void_p]),
+    ("DN_batch_add", c_bool, [c_void_p, VOLP]),
+    ("DN_batch_remove", c_bool, [c_void_p, VOLP]),
+    ("DN_batch_run", c_bool, [c_void_p, POINTER(DNbatchItem), c_uint32]),
+    ("DN_batch_finish", c_bool, [c_void_p]),
+    ("DN_batch_get_stats", c_bool, [c_void_p, POINTER(DNstats)]),
+    ("DN_batch_reset_stats", None, [c_void_p]),
+    ("DN_batch_autotune", c_bool, [c_void_p]),
     ("dn_pack_chunk", c_uint32, [VOLP, POINTER(DNchunk), c_void_p, c_void_p, c_void_p]),
     ("dn_scene_palette", None, [VOLP, c_uint32, c_uint32, c_uint32, c_float, c_float, c_float]),
     ("dn_scene_terrain", None, [VOLP, c_uint32, c_float, c_float, c_uint32, c_uint32]),
@@ -187,6 +210,20 @@ _SIGS = [
     ("dn_cuda_stream_sync", c_int, [c_void_p]),
     ("dn_cuda_device_sync", c_int, []),
     ("dn_cuda_flush_l2", c_int, [c_void_p, c_size_t]),
+    ("dn_cuda_sync_stage", c_int, [c_void_p, c_void_p, c_uint32, c_void_p, c_uint32, c_void_p, c_uint64]),
+    ("dn_cuda_batch_create", c_int, [POINTER(c_void_p)]),
+    ("dn_cuda_batch_destroy", None, [c_void_p]),
+    ("dn_cuda_batch_add", c_int, [c_void_p, c_void_p]),
+    ("dn_cuda_batch_remove", c_int, [c_void_p, c_void_p]),
+    ("dn_cuda_batch_frame", c_int, [c_void_p, c_void_p, c_uint32]),
+    ("dn_cuda_batch_finish", c_int, [c_void_p]),
+    ("dn_cuda_batch_stats", c_int, [c_void_p, c_int, c_void_p]),
+    ("dn_cuda_batch_reset_stats", c_int, [c_void_p]),
+    ("dn_cuda_batch_stream", c_void_p, [c_void_p]),
+    ("dn_cuda_batch_get_tuning", c_int, [c_void_p, POINTER(DnBatchTuning)]),
+    ("dn_cuda_batch_set_tuning", c_int, [c_void_p, POINTER(DnBatchTuning)]),
+    ("dn_cuda_batch_autotune", c_int, [c_void_p, POINTER(DnBatchTuning)]),
+    ("dn_cuda_requests_of", c_uint64, [c_void_p]),
     ("dn_cuda_kernel_names", c_char_p, []),
     ("dn_cuda_launch_count", c_uint64, []),
 ]
@@ -224,11 +261,12 @@ def exported_names():
 def check_layout(lib=None):
     """Compare the ctypes struct layouts with the library's own sizes / offsets; returns a list of mismatches."""
     lib = lib or load()
-    buf = (c_uint64 * 32)()
-    n = lib.DN_abi_layout(buf, 32)
+    buf = (c_uint64 * 64)()
+    n = lib.DN_abi_layout(buf, 64)
     want = [ctypes.sizeof(DNvolume), DNvolume.mapSize.offset, DNvolume.map.offset, DNvolume.chunks.offset,
             DNvolume.materials.offset, DNvolume.camPos.offset, DNvolume.sunDir.offset, DNvolume.useCubemap.offset,
             DNvolume.frameNum.offset, DNvolume.emissiveStrength.offset, DNvolume.deviceBudgetBytes.offset,
             ctypes.sizeof(DNchunk), ctypes.sizeof(DNmaterial), ctypes.sizeof(DNimage), ctypes.sizeof(DNchunkHandle),
-            ctypes.sizeof(DNstats), DNchunk.voxels.offset, ctypes.sizeof(DNvoxel)]
+            ctypes.sizeof(DNstats), DNchunk.voxels.offset, ctypes.sizeof(DNvoxel),
+            ctypes.sizeof(DNbatchItem), DNbatchItem.view.offset, DNbatchItem.op.offset, DNbatchItem.time.offset]
     return [(i, int(buf[i]), w) for i, w in enumerate(want[:n]) if int(buf[i]) != w]

@@ -40,3 +40,24 @@ def build_volume(name, cpu_only=False, **over):
     vol.s.emissiveStrength = 5.0
     vol.s.sunDir.x, vol.s.sunDir.y, vol.s.sunDir.z = 0.4, 1.0, 0.25
     return vol, cfg
+
+
+RESOLUTIONS = ((320, 180), (640, 360), (1280, 720), (1920, 1080))
+
+
+def batched_specs(n=64, seed=7, dim_lo=8, dim_hi=64, res=RESOLUTIONS):
+    """The batched workload: n independent maps with chunk dimensions uniform in [dim_lo, dim_hi] per axis,
+    non-empty chunk fraction uniform in [0.05, 0.5], each with its own seeded camera and a resolution drawn
+    from ``res``; K=16 direct / specular rays.  Returns a list of per-map overrides for ``build_volume``."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        dims = tuple(int(x) for x in rng.integers(dim_lo, dim_hi + 1, size=3))
+        frac = float(rng.uniform(0.05, 0.5))
+        r = res[int(rng.integers(len(res)))]
+        cam = (float(rng.uniform(0.05, 0.3)), float(rng.uniform(0.6, 0.9)), float(rng.uniform(0.05, 0.3)),
+               float(rng.uniform(20.0, 40.0)), float(rng.uniform(30.0, 60.0)))
+        out.append(dict(map=dims, seed=int(seed * 1000 + i), mean=frac, amp=frac * 0.5, shapes=0,
+                        res=tuple(r), K=16, cam=cam))
+    return out

@@ -1,0 +1,669 @@
+/*
+ * dn_batch.cu -- batched frames over many maps (the dn_cuda_batch_* entries of include/dn_cuda.h).
+ *
+ * A frame of a batch is a fixed handful of device operations whatever the number of maps:
+ *   1. one host-to-device copy of the frame's table (per-map parameters, image pointers, materials);
+ *   2. k_batch_reset: zero the request counters of the maps whose per-tile pass runs;
+ *   3. k_draw_batch: every pixel of every image (blocks of 8x32 pixels; a block belongs to one map);
+ *   4. k_compact_batch: the per-tile sync pass over every tile of every map (blocks of 256 tiles);
+ *   5. k_batch_prep: clamp the request counts, lay the maps' request lists end to end as one queue (an
+ *      exclusive prefix over the counts) and compute each map's shadow directions;
+ *   6. k_light_stream_batch: the persistent lighting loop (dn_light_stream.cuh) over the whole queue;
+ *   7. k_commit_batch: commit every map's new lighting.
+ * Host-memory images are copied back on a second stream that overlaps steps 4-7.  A frame whose
+ * composition repeats is captured once and replayed as a CUDA graph.
+ *
+ * Each map's results equal those of its single-map calls: the kernels run the same per-pixel, per-tile
+ * and per-voxel code as dn_cuda.cu, every map's work reads and writes only that map's arrays, and the
+ * lighting of a voxel does not depend on which lane, warp or launch computes it.
+ */
+#include "dn_internal.cuh"
+#include "dn_light.cuh"
+#include "dn_light_stream.cuh"
+#include <string.h>
+#include <stddef.h>
+#include <new>
+#include <vector>
+#include <algorithm>
+
+using namespace dn;
+
+struct BatchDrawEntry {
+    DrawMap d;
+    const Material* mats;
+    uint32_t gridX;             // blocks of 8 pixels across
+};
+
+struct DNgpuBatch {
+    int device;
+    cudaStream_t stream, side;
+    cudaEvent_t drawDone, copiesDone, tableFree;
+    std::vector<DNgpuVolume*> members;
+    unsigned char* htab; unsigned char* dtab; size_t tabCap;
+    uint64_t tabGen;
+    uint32_t* workCounter;
+    DevState* bst;              // counters of batched launches (device)
+    DevState* hbst;             // pinned copy
+    unsigned long long* lsave;  // lighting counters saved around autotuning (device)
+    DevState** dsts; uint32_t dstsCap; bool stsDirty;
+    uint32_t* dgather; uint32_t* hgather;
+    dn_batch_tuning tuning;
+    int maxBlocksPerSM;
+    std::vector<uint64_t> lastKey;
+    std::vector<uint64_t> graphKey;
+    cudaGraphExec_t graph;
+    // the lighting launch of the last frame (autotuning re-runs it)
+    BatchLightArgs lastLight;
+    bool lastLightValid;
+};
+
+// ------------------------------------------------------------------ kernels
+
+// largest i < n with start[i] <= v (start[0] = 0, non-decreasing): the entry whose range holds v
+__device__ __forceinline__ uint32_t find_range(const uint32_t* start, uint32_t n, uint32_t v)
+{
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&start[mid]) <= v) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_batch_reset(const CompactArgs* s, uint32_t ns)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ns) s[i].st->w[ST_REQ] = 0;
+}
+
+__global__ void __launch_bounds__(256) k_draw_batch(const BatchDrawEntry* d, const uint32_t* start, uint32_t nd,
+                                                    unsigned long long* stats)
+{
+    __shared__ Material smat[256];
+    const uint32_t mi = find_range(start, nd, blockIdx.x);
+    const BatchDrawEntry& e = d[mi];
+    for (int i = threadIdx.x + threadIdx.y * blockDim.x; i < 256; i += blockDim.x * blockDim.y) smat[i] = e.mats[i];
+    __syncthreads();
+    const uint32_t local = blockIdx.x - start[mi];
+    const uint32_t bx = local % e.gridX, by = local / e.gridX;
+    Counters c;
+    const uint32_t primary = draw_pixel(e.d, smat, bx * blockDim.x + threadIdx.x, by * blockDim.y + threadIdx.y, c);
+    flush_counters(stats, c, primary, 0);
+}
+
+__global__ void __launch_bounds__(256) k_compact_batch(const CompactArgs* s, const uint32_t* start, uint32_t ns)
+{
+    const uint32_t mi = find_range(start, ns, blockIdx.x);
+    compact_tiles(s[mi], (uint64_t)(blockIdx.x - start[mi]) * blockDim.x);
+}
+
+// blocks [0, nl): shadow directions of light map blockIdx.x.  Block nl: clamp the request count of every
+// synced map to its capacity (dn_cuda_sync's k_clamp_requests), then the exclusive prefix of the light
+// maps' counts into reqStart[0..nl] and a zero work counter.
+__global__ void k_batch_prep(BatchLightMap* l, uint32_t nl, const CompactArgs* s, uint32_t ns, uint32_t* reqStart,
+                             uint32_t* workCounter)
+{
+    if (blockIdx.x < nl) {
+        BatchLightMap& e = l[blockIdx.x];
+        for (int k = threadIdx.x; k < 65; k += blockDim.x) shadow_dir(e.p, k, e.sdir[k], e.sinv[k]);
+        return;
+    }
+    for (uint32_t i = threadIdx.x; i < ns; i += blockDim.x) {
+        uint32_t* c = &s[i].st->w[ST_REQ];
+        if (*c > s[i].reqCap) *c = (uint32_t)s[i].reqCap;
+    }
+    __shared__ uint32_t warpSum[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) { carry = 0; *workCounter = 0; }
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for (uint32_t base = 0; base < nl; base += blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        uint32_t v = 0;
+        if (i < nl) {
+            v = *l[i].nreqPtr;
+            if (v > l[i].reqCap) v = (uint32_t)l[i].reqCap;
+        }
+        uint32_t incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if ((int)lane >= o) incl += t;
+        }
+        if (lane == 31u) warpSum[warp] = incl;
+        __syncthreads();
+        uint32_t before = carry;
+        for (uint32_t w = 0; w < warp; w++) before += warpSum[w];
+        if (i < nl) reqStart[i] = before + incl - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = before + incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) reqStart[nl] = carry;
+}
+
+__global__ void __launch_bounds__(128, DN_STREAM_MIN_BLOCKS) k_light_stream_batch(const __grid_constant__ BatchLightArgs a)
+{
+    __shared__ Job jobs[128];
+    stream_loop<true>(nullptr, &a, nullptr, jobs[threadIdx.x]);
+}
+
+__global__ void k_commit_batch(const BatchLightMap* l, const uint32_t* reqStart, uint32_t nl)
+{
+    const uint64_t total = (uint64_t)reqStart[nl] * 32u;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t r = (uint32_t)(i >> 5), lane = (uint32_t)(i & 31u);
+        const uint32_t mi = find_range(reqStart, nl, r);
+        const BatchLightMap& e = l[mi];
+        const uint32_t lr = r - __ldg(&reqStart[mi]);
+        commit_lane(e.m, e.reqs, e.out, (uint64_t)lr * 32u + lane, lr, lane, e.diffOut, e.specOut, e.samplesOut);
+    }
+}
+
+// the status words of every member into one array (error flags are cleared once read)
+__global__ void k_batch_gather(DevState* const* sts, uint32_t n, uint32_t* out)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        DevState* s = sts[i];
+        out[4 * i] = s->w[0]; out[4 * i + 1] = s->w[1]; out[4 * i + 2] = s->w[2]; out[4 * i + 3] = s->w[3];
+        s->w[ST_ERR] = 0;
+    }
+}
+
+// ------------------------------------------------------------------ host
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+extern "C" int dn_cuda_batch_create(DNgpuBatch** out)
+{
+    if (!out) return dn_set_err(DN_CUDA_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (g_device < 0) return dn_set_err(DN_CUDA_ERR_DEVICE, "dn_cuda_init was not called");
+    CK(cudaSetDevice(g_device));
+    DNgpuBatch* b = new (std::nothrow) DNgpuBatch();
+    if (!b) return dn_set_err(DN_CUDA_ERR_NOMEM, "host allocation");
+    b->device = g_device;
+    b->stream = b->side = nullptr;
+    b->drawDone = b->copiesDone = b->tableFree = nullptr;
+    b->htab = b->dtab = nullptr; b->tabCap = 0; b->tabGen = 0;
+    b->workCounter = nullptr; b->bst = nullptr; b->hbst = nullptr; b->lsave = nullptr;
+    b->dsts = nullptr; b->dstsCap = 0; b->stsDirty = true; b->dgather = nullptr; b->hgather = nullptr;
+    b->tuning.streamBatch = g_streamBatch; b->tuning.blocksPerSM = DN_STREAM_MIN_BLOCKS; b->tuning.useGraph = 1;
+    b->graph = nullptr;
+    b->lastLightValid = false;
+    int rc = DN_CUDA_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->drawDone, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->copiesDone, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->tableFree, cudaEventDisableTiming);
+    if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "stream / event: %s", cudaGetErrorString(e));
+    if (!rc) rc = dalloc(&b->workCounter, 1);
+    if (!rc) rc = dalloc(&b->bst, 1);
+    if (!rc) rc = dalloc(&b->lsave, 8);
+    if (!rc) {
+        e = cudaMallocHost((void**)&b->hbst, sizeof(DevState));
+        if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_NOMEM, "pinned: %s", cudaGetErrorString(e));
+    }
+    if (!rc) {
+        e = cudaMemsetAsync(b->bst, 0, sizeof(DevState), b->stream);
+        if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "memset: %s", cudaGetErrorString(e));
+    }
+    if (!rc) {
+        int perSM = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_stream_batch, 128, 0);
+        if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "occupancy: %s", cudaGetErrorString(e));
+        b->maxBlocksPerSM = perSM < 1 ? 1 : perSM;
+        if ((int)b->tuning.blocksPerSM > b->maxBlocksPerSM) b->tuning.blocksPerSM = (uint32_t)b->maxBlocksPerSM;
+    }
+    if (rc) { dn_cuda_batch_destroy(b); return rc; }
+    *out = b;
+    return DN_CUDA_OK;
+}
+
+extern "C" int dn_cuda_batch_add(DNgpuBatch* b, DNgpuVolume* g)
+{
+    if (!b || !g) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
+    if (g->batch) return dn_set_err(DN_CUDA_ERR_ARG, "the volume already belongs to a batch");
+    if (g->device != b->device) return dn_set_err(DN_CUDA_ERR_ARG, "the volume lives on another device");
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamSynchronize(g->ownStream));
+    g->stream = b->stream;
+    g->batch = b;
+    b->members.push_back(g);
+    b->stsDirty = true;
+    return DN_CUDA_OK;
+}
+
+extern "C" int dn_cuda_batch_remove(DNgpuBatch* b, DNgpuVolume* g)
+{
+    if (!b || !g) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
+    auto it = std::find(b->members.begin(), b->members.end(), g);
+    if (it == b->members.end() || g->batch != b) return dn_set_err(DN_CUDA_ERR_ARG, "the volume is not a member");
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamSynchronize(b->stream));
+    CK(cudaStreamSynchronize(b->side));
+    g->stream = g->ownStream;
+    g->batch = nullptr;
+    b->members.erase(it);
+    b->stsDirty = true;
+    b->lastKey.clear();
+    b->lastLightValid = false;
+    return DN_CUDA_OK;
+}
+
+extern "C" void dn_cuda_batch_destroy(DNgpuBatch* b)
+{
+    if (!b) return;
+    cudaSetDevice(b->device);
+    while (!b->members.empty()) {
+        DNgpuVolume* g = b->members.back();
+        if (b->stream) cudaStreamSynchronize(b->stream);
+        g->stream = g->ownStream;
+        g->batch = nullptr;
+        b->members.pop_back();
+    }
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->side) cudaStreamSynchronize(b->side);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    dfree(b->dtab); dfree(b->workCounter); dfree(b->bst); dfree(b->lsave); dfree(b->dsts); dfree(b->dgather);
+    if (b->htab) cudaFreeHost(b->htab);
+    if (b->hbst) cudaFreeHost(b->hbst);
+    if (b->hgather) cudaFreeHost(b->hgather);
+    if (b->drawDone) cudaEventDestroy(b->drawDone);
+    if (b->copiesDone) cudaEventDestroy(b->copiesDone);
+    if (b->tableFree) cudaEventDestroy(b->tableFree);
+    if (b->side) cudaStreamDestroy(b->side);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+// byte offsets of the sections of a frame's table
+struct TableLayout {
+    uint32_t nm, nd, ns, nl;
+    size_t oMats, oDraw, oSync, oLight, oReqStart, oDrawStart, oSyncStart, size;
+};
+
+static TableLayout layout(uint32_t nm, uint32_t nd, uint32_t ns, uint32_t nl)
+{
+    TableLayout t;
+    t.nm = nm; t.nd = nd; t.ns = ns; t.nl = nl;
+    size_t o = 0;
+    t.oMats = o; o = align256(o + (size_t)nm * 256 * sizeof(Material));
+    t.oDraw = o; o = align256(o + (size_t)nd * sizeof(BatchDrawEntry));
+    t.oSync = o; o = align256(o + (size_t)ns * sizeof(CompactArgs));
+    t.oLight = o; o = align256(o + (size_t)nl * sizeof(BatchLightMap));
+    t.oReqStart = o; o = align256(o + (size_t)(nl + 1) * 4);
+    t.oDrawStart = o; o = align256(o + (size_t)(nd + 1) * 4);
+    t.oSyncStart = o; o = align256(o + (size_t)(ns + 1) * 4);
+    t.size = o;
+    return t;
+}
+
+struct FramePlan {
+    TableLayout t;
+    uint32_t drawBlocks, syncBlocks;
+    bool hostImages;
+};
+
+static int issue_light(DNgpuBatch* b, const BatchLightArgs& la, cudaStream_t s)
+{
+    COUNT_LAUNCH();
+    k_light_stream_batch<<<(unsigned)(g_numSMs * (int)b->tuning.blocksPerSM), 128, 0, s>>>(la);
+    CK(cudaGetLastError());
+    return DN_CUDA_OK;
+}
+
+// the device work of one frame on b->stream; capturing: issued under stream capture
+static int issue_frame(DNgpuBatch* b, const dn_batch_item* items, uint32_t n, const FramePlan& f, bool capturing)
+{
+    const TableLayout& t = f.t;
+    cudaStream_t s = b->stream;
+    unsigned char* d = b->dtab;
+    const CompactArgs* syncs = (const CompactArgs*)(d + t.oSync);
+    CK(cudaMemcpyAsync(d, b->htab, t.size, cudaMemcpyHostToDevice, s));
+    // the host may rewrite its copy of the table once this fires (in a graph: an event record node)
+    if (capturing) CK(cudaEventRecordWithFlags(b->tableFree, s, cudaEventRecordExternal));
+    else CK(cudaEventRecord(b->tableFree, s));
+    if (t.ns) {
+        COUNT_LAUNCH();
+        k_batch_reset<<<(t.ns + 255) / 256, 256, 0, s>>>(syncs, t.ns);
+        CK(cudaGetLastError());
+    }
+    if (t.nd) {
+        COUNT_LAUNCH();
+        k_draw_batch<<<f.drawBlocks, dim3(8, 32), 0, s>>>((const BatchDrawEntry*)(d + t.oDraw),
+                                                         (const uint32_t*)(d + t.oDrawStart), t.nd, b->bst->stats);
+        CK(cudaGetLastError());
+    }
+    if (f.hostImages) {
+        // host images: copies on the side stream overlap the rest of the frame
+        CK(cudaEventRecord(b->drawDone, s));
+        CK(cudaStreamWaitEvent(b->side, b->drawDone, 0));
+        for (uint32_t i = 0; i < n; i++) {
+            const dn_batch_item& it = items[i];
+            if (!(it.phases & DN_BATCH_DRAW) || !it.hostImage) continue;
+            const size_t px = (size_t)it.draw.width * it.draw.height;
+            DNgpuVolume* g = it.map;
+            CK(cudaMemcpyAsync(it.colorOut, g->dimg, px * 16, cudaMemcpyDeviceToHost, b->side));
+            if (it.hitOut) CK(cudaMemcpyAsync(it.hitOut, g->dhit, px * 4, cudaMemcpyDeviceToHost, b->side));
+            if (it.faceOut) CK(cudaMemcpyAsync(it.faceOut, g->dface, px, cudaMemcpyDeviceToHost, b->side));
+        }
+        CK(cudaEventRecord(b->copiesDone, b->side));
+    }
+    if (t.ns) {
+        COUNT_LAUNCH();
+        k_compact_batch<<<f.syncBlocks, 256, 0, s>>>(syncs, (const uint32_t*)(d + t.oSyncStart), t.ns);
+        CK(cudaGetLastError());
+    }
+    if (t.nl || t.ns) {
+        COUNT_LAUNCH();
+        k_batch_prep<<<t.nl + 1, 128, 0, s>>>((BatchLightMap*)(d + t.oLight), t.nl, syncs, t.ns,
+                                              (uint32_t*)(d + t.oReqStart), b->workCounter);
+        CK(cudaGetLastError());
+    }
+    if (t.nl) {
+        BatchLightArgs la;
+        la.maps = (BatchLightMap*)(d + t.oLight);
+        la.reqStart = (const uint32_t*)(d + t.oReqStart);
+        la.nmaps = t.nl;
+        la.workCounter = b->workCounter;
+        la.stats = b->bst->lstats;
+        la.batch = b->tuning.streamBatch;
+        int rc = issue_light(b, la, s);
+        if (rc) return rc;
+        COUNT_LAUNCH();
+        k_commit_batch<<<(unsigned)(g_numSMs * 4), 256, 0, s>>>(la.maps, la.reqStart, t.nl);
+        CK(cudaGetLastError());
+        b->lastLight = la;
+        b->lastLightValid = true;
+    }
+    if (f.hostImages) CK(cudaStreamWaitEvent(s, b->copiesDone, 0));
+    return DN_CUDA_OK;
+}
+
+extern "C" int dn_cuda_batch_frame(DNgpuBatch* b, const dn_batch_item* items, uint32_t n)
+{
+    if (!b || (!items && n)) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
+    if (n == 0) return DN_CUDA_OK;
+    CK(cudaSetDevice(b->device));
+    // validate, count sections, reserve image staging
+    uint32_t nm = 0, nd = 0, ns = 0, nl = 0;
+    bool hostImages = false;
+    std::vector<const DNgpuVolume*> seen;
+    seen.reserve(n);
+    for (uint32_t i = 0; i < n; i++) {
+        const dn_batch_item& it = items[i];
+        DNgpuVolume* g = it.map;
+        if (!g || g->batch != b) return dn_set_err(DN_CUDA_ERR_ARG, "item %u: the map is not a member of the batch", i);
+        if (!it.phases || (it.phases & ~(DN_BATCH_DRAW | DN_BATCH_SYNC | DN_BATCH_LIGHT)))
+            return dn_set_err(DN_CUDA_ERR_ARG, "item %u: phases 0x%x", i, it.phases);
+        seen.push_back(g);
+        if (it.phases & (DN_BATCH_DRAW | DN_BATCH_LIGHT)) {
+            if (!it.materials) return dn_set_err(DN_CUDA_ERR_ARG, "item %u: no materials", i);
+            nm++;
+        }
+        if (it.phases & DN_BATCH_DRAW) {
+            if (!it.colorOut || it.draw.width == 0 || it.draw.height == 0)
+                return dn_set_err(DN_CUDA_ERR_ARG, "item %u: bad image", i);
+            if (it.hostImage) {
+                hostImages = true;
+                int rc = dn_reserve_image_staging(g, (size_t)it.draw.width * it.draw.height);
+                if (rc) return rc;
+            }
+            nd++;
+        }
+        if (it.phases & DN_BATCH_SYNC) {
+            if (it.sync.split == 0 || it.sync.op > 2) return dn_set_err(DN_CUDA_ERR_ARG, "item %u: bad sync parameters", i);
+            ns++;
+        }
+        if (it.phases & DN_BATCH_LIGHT) {
+            if (it.light.K < 1 || it.light.K > 64) return dn_set_err(DN_CUDA_ERR_ARG, "item %u: K = %u", i, it.light.K);
+            nl++;
+        }
+    }
+    std::sort(seen.begin(), seen.end());
+    if (std::adjacent_find(seen.begin(), seen.end()) != seen.end())
+        return dn_set_err(DN_CUDA_ERR_ARG, "a map appears twice in one batched frame");
+
+    FramePlan f;
+    f.t = layout(nm, nd, ns, nl);
+    f.hostImages = hostImages;
+    if (f.t.size > b->tabCap) {
+        CK(cudaStreamSynchronize(b->stream));
+        if (b->htab) cudaFreeHost(b->htab);
+        b->htab = nullptr;
+        dfree(b->dtab);
+        const size_t nc = f.t.size + f.t.size / 2;
+        CK(cudaMallocHost((void**)&b->htab, nc));
+        int rc = dalloc(&b->dtab, nc);
+        if (rc) { b->tabCap = 0; return rc; }
+        b->tabCap = nc;
+        b->tabGen++;
+    }
+    // the previous frame's copy of the table has been consumed once tableFree fired
+    CK(cudaEventSynchronize(b->tableFree));
+    unsigned char* h = b->htab;
+    Material* hm = (Material*)(h + f.t.oMats);
+    BatchDrawEntry* hd = (BatchDrawEntry*)(h + f.t.oDraw);
+    CompactArgs* hs = (CompactArgs*)(h + f.t.oSync);
+    BatchLightMap* hl = (BatchLightMap*)(h + f.t.oLight);
+    uint32_t* drawStart = (uint32_t*)(h + f.t.oDrawStart);
+    uint32_t* syncStart = (uint32_t*)(h + f.t.oSyncStart);
+    const Material* dm = (const Material*)(b->dtab + f.t.oMats);
+    uint32_t im = 0, id = 0, is = 0, il = 0, blocksD = 0, blocksS = 0;
+    std::vector<uint64_t> key;
+    key.reserve(4 + (size_t)n * 10);
+    key.push_back(n); key.push_back(b->tabGen); key.push_back(b->tuning.streamBatch); key.push_back(b->tuning.blocksPerSM);
+    for (uint32_t i = 0; i < n; i++) {
+        const dn_batch_item& it = items[i];
+        DNgpuVolume* g = it.map;
+        key.push_back((uint64_t)(uintptr_t)g); key.push_back(g->gen); key.push_back(it.phases | (it.hostImage << 8));
+        const Material* mats = nullptr;
+        if (it.phases & (DN_BATCH_DRAW | DN_BATCH_LIGHT)) {
+            memcpy(hm + (size_t)im * 256, it.materials, 256 * sizeof(Material));
+            mats = dm + (size_t)im * 256;
+            im++;
+        }
+        if (it.phases & DN_BATCH_DRAW) {
+            BatchDrawEntry& e = hd[id];
+            memset(&e, 0, sizeof(e));
+            e.d.m = dev_map(g);
+            e.d.p = it.draw;
+            e.d.color = it.hostImage ? g->dimg : (float4*)it.colorOut;
+            e.d.hit = it.hitOut ? (it.hostImage ? g->dhit : it.hitOut) : nullptr;
+            e.d.face = it.faceOut ? (it.hostImage ? g->dface : it.faceOut) : nullptr;
+            e.d.stats = b->bst->stats;
+            e.mats = mats;
+            e.gridX = (it.draw.width + 7) / 8;
+            drawStart[id] = blocksD;
+            blocksD += e.gridX * ((it.draw.height + 31) / 32);
+            key.push_back((uint64_t)(uintptr_t)it.colorOut); key.push_back((uint64_t)(uintptr_t)it.hitOut);
+            key.push_back((uint64_t)(uintptr_t)it.faceOut); key.push_back(((uint64_t)it.draw.width << 32) | it.draw.height);
+            id++;
+        }
+        if (it.phases & DN_BATCH_SYNC) {
+            CompactArgs& a = hs[is];
+            memset(&a, 0, sizeof(a));
+            a.tword = g->tword; a.tbits = g->tbits; a.treq = g->treq; a.tvis = g->tvis; a.ttouch = g->ttouch; a.tlast = g->tlast;
+            a.tpend = g->tpend; a.tpendSlot = g->tpendSlot; a.rec = g->rec;
+            a.reqs = g->reqs; a.reqCap = g->reqCap; a.st = g->st; a.ntiles = g->ntiles;
+            a.op = it.sync.op; a.split = it.sync.split; a.frameNum = it.sync.frameNum;
+            syncStart[is] = blocksS;
+            blocksS += (uint32_t)((g->ntiles + 255) / 256);
+            is++;
+        }
+        if (it.phases & DN_BATCH_LIGHT) {
+            BatchLightMap& e = hl[il];
+            memset(&e, 0, offsetof(BatchLightMap, sdir));
+            e.m = dev_map(g);
+            e.reqs = g->reqs; e.nsamples = g->nsamples; e.out = g->lightOut;
+            e.nreqPtr = &g->st->w[ST_REQ]; e.reqCap = g->reqCap;
+            e.p = it.light;
+            e.mats = mats;
+            e.diffOut = g->diff; e.specOut = g->spec; e.samplesOut = g->nsamples;
+            il++;
+        }
+    }
+    drawStart[nd] = blocksD;
+    syncStart[ns] = blocksS;
+    f.drawBlocks = blocksD;
+    f.syncBlocks = blocksS;
+
+    const bool repeat = b->tuning.useGraph && key == b->lastKey;
+    b->lastKey = key;
+    if (!repeat) return issue_frame(b, items, n, f, false);
+    if (!b->graph || b->graphKey != key) {
+        if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+        b->graphKey.clear();
+        CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const unsigned long long before = g_launches;
+        int rc = issue_frame(b, items, n, f, true);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+        __atomic_store_n(&g_launches, before, __ATOMIC_RELAXED);   // captured launches run when the graph does
+        if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+        if (e != cudaSuccess) return dn_set_err(DN_CUDA_ERR_LAUNCH, "stream capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&b->graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) { b->graph = nullptr; return dn_set_err(DN_CUDA_ERR_LAUNCH, "graph instantiate: %s", cudaGetErrorString(e)); }
+        b->graphKey = key;
+    }
+    // the graph's kernels: reset and compact (sync), draw, prep, light and commit
+    const unsigned long long k = (f.t.ns ? 2u : 0u) + (f.t.nd ? 1u : 0u) + ((f.t.nl || f.t.ns) ? 1u : 0u) + (f.t.nl ? 2u : 0u);
+    __atomic_fetch_add(&g_launches, k, __ATOMIC_RELAXED);
+    CK(cudaGraphLaunch(b->graph, b->stream));
+    return DN_CUDA_OK;
+}
+
+extern "C" int dn_cuda_batch_finish(DNgpuBatch* b)
+{
+    if (!b) return dn_set_err(DN_CUDA_ERR_ARG, "null batch");
+    CK(cudaSetDevice(b->device));
+    const uint32_t n = (uint32_t)b->members.size();
+    if (n && (b->stsDirty || n > b->dstsCap)) {
+        CK(cudaStreamSynchronize(b->stream));
+        if (n > b->dstsCap) {
+            dfree(b->dsts); dfree(b->dgather);
+            if (b->hgather) cudaFreeHost(b->hgather);
+            b->hgather = nullptr;
+            b->dstsCap = 0;
+            int rc;
+            if ((rc = dalloc(&b->dsts, n)) || (rc = dalloc(&b->dgather, (size_t)n * 4))) return rc;
+            CK(cudaMallocHost((void**)&b->hgather, (size_t)n * 16));
+            b->dstsCap = n;
+        }
+        std::vector<DevState*> sts(n);
+        for (uint32_t i = 0; i < n; i++) sts[i] = b->members[i]->st;
+        CK(cudaMemcpy(b->dsts, sts.data(), (size_t)n * sizeof(DevState*), cudaMemcpyHostToDevice));
+        b->stsDirty = false;
+    }
+    if (n) {
+        COUNT_LAUNCH();
+        k_batch_gather<<<(n + 255) / 256, 256, 0, b->stream>>>(b->dsts, n, b->dgather);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(b->hgather, b->dgather, (size_t)n * 16, cudaMemcpyDeviceToHost, b->stream));
+    }
+    CK(cudaMemcpyAsync(b->hbst, b->bst, sizeof(DevState), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    CK(cudaStreamSynchronize(b->side));
+    uint32_t bad = 0, first = 0, flags = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        DNgpuVolume* g = b->members[i];
+        memcpy(g->hst->w, &b->hgather[4 * i], sizeof(g->hst->w));
+        if (g->hst->w[ST_ERR]) { if (!bad) { first = i; flags = g->hst->w[ST_ERR]; } bad++; }
+    }
+    if (bad) return dn_set_err(DN_CUDA_ERR_KERNEL, "kernel error flags 0x%x on member %u (%u members flagged)", flags, first, bad);
+    return DN_CUDA_OK;
+}
+
+extern "C" int dn_cuda_batch_stats(DNgpuBatch* b, int kind, dn_stats* out)
+{
+    if (!b || !out || kind < 0 || kind > 2) return dn_set_err(DN_CUDA_ERR_ARG, "bad argument");
+    int rc = dn_cuda_batch_finish(b);
+    if (rc && rc != DN_CUDA_ERR_KERNEL) return rc;
+    unsigned long long s[8];
+    for (int k = 0; k < 8; k++) s[k] = (kind != 2 ? b->hbst->stats[k] : 0ull) + (kind != 1 ? b->hbst->lstats[k] : 0ull);
+    out->rays = s[S_RAYS]; out->primary = s[S_PRIMARY]; out->outerSteps = s[S_OUTER];
+    out->chunksEntered = s[S_ENTERED]; out->innerSteps = s[S_INNER]; out->hits = s[S_HITS]; out->litVoxels = s[S_LIT];
+    return rc;
+}
+
+extern "C" int dn_cuda_batch_reset_stats(DNgpuBatch* b)
+{
+    if (!b) return dn_set_err(DN_CUDA_ERR_ARG, "null batch");
+    CK(cudaSetDevice(b->device));
+    CK(cudaMemsetAsync(b->bst->stats, 0, sizeof(b->bst->stats) + sizeof(b->bst->lstats), b->stream));
+    return DN_CUDA_OK;
+}
+
+extern "C" void* dn_cuda_batch_stream(DNgpuBatch* b) { return b ? (void*)b->stream : nullptr; }
+
+extern "C" int dn_cuda_batch_get_tuning(DNgpuBatch* b, dn_batch_tuning* out)
+{
+    if (!b || !out) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
+    *out = b->tuning;
+    return DN_CUDA_OK;
+}
+
+extern "C" int dn_cuda_batch_set_tuning(DNgpuBatch* b, const dn_batch_tuning* t)
+{
+    if (!b || !t) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
+    if (t->streamBatch < 1 || t->streamBatch > 32) return dn_set_err(DN_CUDA_ERR_ARG, "streamBatch %u", t->streamBatch);
+    if (t->blocksPerSM < 1 || (int)t->blocksPerSM > b->maxBlocksPerSM)
+        return dn_set_err(DN_CUDA_ERR_ARG, "blocksPerSM %u (1..%d)", t->blocksPerSM, b->maxBlocksPerSM);
+    b->tuning = *t;
+    b->tuning.useGraph = t->useGraph ? 1u : 0u;
+    return DN_CUDA_OK;
+}
+
+extern "C" int dn_cuda_batch_autotune(DNgpuBatch* b, dn_batch_tuning* chosen)
+{
+    if (!b) return dn_set_err(DN_CUDA_ERR_ARG, "null batch");
+    if (!b->lastLightValid) return dn_set_err(DN_CUDA_ERR_ARG, "no batched lighting launch to tune on");
+    CK(cudaSetDevice(b->device));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    // the reruns write only the lighting scratch and idempotent flags; keep the launch counters out of them
+    CK(cudaMemcpyAsync(b->lsave, b->bst->lstats, sizeof(b->bst->lstats), cudaMemcpyDeviceToDevice, b->stream));
+    const dn_batch_tuning keep = b->tuning;
+    dn_batch_tuning best = keep;
+    float bestMs = 3.4e38f;
+    const uint32_t batches[] = {16u, 20u, 24u, 28u, 32u};
+    int rc = DN_CUDA_OK;
+    for (uint32_t bps = 2; bps <= (uint32_t)b->maxBlocksPerSM && bps <= 6 && !rc; bps++) {
+        for (uint32_t sb : batches) {
+            b->tuning.streamBatch = sb;
+            b->tuning.blocksPerSM = bps;
+            BatchLightArgs la = b->lastLight;
+            la.batch = sb;
+            float ms = 3.4e38f;
+            for (int rep = 0; rep < 2 && !rc; rep++) {
+                cudaError_t e = cudaMemsetAsync(b->workCounter, 0, 4, b->stream);
+                if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+                if (e != cudaSuccess) { rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "autotune: %s", cudaGetErrorString(e)); break; }
+                rc = issue_light(b, la, b->stream);
+                if (rc) break;
+                e = cudaEventRecord(e1, b->stream);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                float t = 0.0f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+                if (e != cudaSuccess) { rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "autotune: %s", cudaGetErrorString(e)); break; }
+                if (t < ms) ms = t;
+            }
+            if (!rc && ms < bestMs) { bestMs = ms; best = b->tuning; }
+        }
+    }
+    b->tuning = rc ? keep : best;
+    b->tuning.useGraph = keep.useGraph;
+    cudaMemcpyAsync(b->bst->lstats, b->lsave, sizeof(b->bst->lstats), cudaMemcpyDeviceToDevice, b->stream);
+    cudaStreamSynchronize(b->stream);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    b->lastKey.clear();
+    if (chosen) *chosen = b->tuning;
+    return DN_CUDA_OK;
+}
+
+extern "C" uint64_t dn_cuda_requests_of(DNgpuVolume* g) { return g && g->hst ? g->hst->w[ST_REQ] : 0u; }

@@ -102,7 +102,7 @@ __device__ __forceinline__ float det_sin(float x)
     return q == 0 ? s : (q == 1 ? c : (q == 2 ? -s : -c));
 }
 __device__ __forceinline__ float srand1(float s) { float v = det_sin(s) * 43758.5453f; return (v - floorf(v)) * 2.0f - 1.0f; }
-__device__ __noinline__ f3 sphere_sin(float seed)
+static __device__ __noinline__ f3 sphere_sin(float seed)
 {
     for (int t = 0; t < 64; t++) {
         float s = seed;
@@ -239,7 +239,7 @@ struct RayCtx {
 };
 
 // step_chunk, voxelShared.comp:328-418
-__device__ __noinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapPos, uint32_t slot, uint32_t tile,
+static __device__ __noinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapPos, uint32_t slot, uint32_t tile,
                                         f3& rayDir, f3& inv, f3& rayPos, bool ignoreFirst, float maxDepth,
                                         f3& hitNormal, Voxel& vox, f3& colorAdd, float& colorMult,
                                         bool& refracted, HitInfo& hi)
@@ -314,7 +314,7 @@ __device__ __noinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapPos, uint32
 }
 
 // step_map, voxelShared.comp:421-475
-__device__ __noinline__ bool step_map(RayCtx& c, TState& ts, f3& rayDir, f3 inv, f3& rayPos, bool ignoreFirst,
+static __device__ __noinline__ bool step_map(RayCtx& c, TState& ts, f3& rayDir, f3 inv, f3& rayPos, bool ignoreFirst,
                                       float maxDepth, f3& hitNormal, Voxel& vox, f3& colorAdd, float& colorMult,
                                       HitInfo& hi)
 {

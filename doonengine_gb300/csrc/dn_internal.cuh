@@ -1,0 +1,366 @@
+/*
+ * dn_internal.cuh -- what the single-map entry points (dn_cuda.cu) and the
+ * batched ones (dn_batch.cu) share: the per-map device state, error and
+ * launch bookkeeping, and the per-pixel / per-tile / per-lane kernel bodies
+ * that both the one-map kernels and the many-map kernels run.
+ */
+#pragma once
+#include "dn_cuda.h"
+#include "dn_device.cuh"
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+// ------------------------------------------------------------------ errors
+
+int dn_set_err(int code, const char* fmt, ...);
+
+#define CK(call)                                                                           \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return dn_set_err(e_ == cudaErrorMemoryAllocation ? DN_CUDA_ERR_NOMEM : DN_CUDA_ERR_LAUNCH, \
+                              "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+// ------------------------------------------------------------------ state
+
+enum { ST_REQ = 0, ST_WORK = 1, ST_ERR = 2 };
+enum { S_RAYS = 0, S_PRIMARY, S_OUTER, S_ENTERED, S_INNER, S_HITS, S_LIT, S_COUNT };
+
+struct DevState {
+    uint32_t w[4];                      // nreq, work counter, error flags, pad
+    unsigned long long stats[8];        // draw kernels
+    unsigned long long lstats[8];       // lighting kernels
+};
+
+struct DNgpuBatch;
+
+struct DNgpuVolume {
+    int device;
+    cudaStream_t stream;                // the batch's stream while the volume belongs to a batch
+    cudaStream_t ownStream;
+    DNgpuBatch* batch;
+    uint64_t gen;                       // unique per allocation state (dn_new_generation)
+    uint32_t sx, sy, sz;
+    uint64_t ntiles;
+    uint32_t* tword; uint8_t* treq; uint8_t* tvis; uint8_t* ttouch;
+    uint32_t* tbits;                    // 2 bits per tile: 0 absent, 1 unloaded, 2 loaded (16 tiles per word)
+    uint32_t* tlast; uint32_t* tpend; uint32_t* tpendSlot;
+    dn::ChunkRec* rec; uint32_t* nsamples; uint32_t slotCap;
+    uint2* vox; float4* diff; float4* spec; uint64_t voxCap;
+    uint32_t* reqs; float4* lightOut; uint64_t reqCap;
+    DevState* st;
+    // pinned staging for sync uploads and small readbacks
+    unsigned char* hstage; size_t hstageCap;
+    unsigned char* dstage; size_t dstageCap;
+    cudaEvent_t stageFree;
+    DevState* hst;                      // pinned copy of DevState
+    // device staging for host-memory draws
+    float4* dimg; uint32_t* dhit; uint8_t* dface; size_t dimgCap;
+    int numSMs;
+};
+
+extern int g_device;
+extern int g_numSMs;
+extern unsigned long long g_launches;   // kernels launched by this library (all threads)
+extern int g_lightKernel;               // 0 lockstep, 1 per-lane ray streams
+extern uint32_t g_streamBatch;          // lanes that wait before per-segment work runs (1..32)
+#define COUNT_LAUNCH() __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED)
+
+template <class T> static int dalloc(T** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    CK(cudaMalloc((void**)p, count * sizeof(T)));
+    return DN_CUDA_OK;
+}
+template <class T> static void dfree(T*& p) { if (p) cudaFree(p); p = nullptr; }
+
+static inline dn::DevMap dev_map(const DNgpuVolume* g)
+{
+    dn::DevMap m;
+    m.sx = g->sx; m.sy = g->sy; m.sz = g->sz;
+    m.tword = g->tword; m.tbits = g->tbits; m.treq = g->treq; m.ttouch = g->ttouch; m.tvis = g->tvis;
+    m.rec = g->rec; m.vox = g->vox; m.diff = g->diff; m.spec = g->spec;
+    return m;
+}
+
+// the staging half of a sync (host ops -> records and voxels); compaction follows separately
+int dn_stage_ops(DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops, const dn_chunk_record* records,
+                 uint32_t nrecords, const uint32_t* voxelWords, uint64_t nvoxels);
+// grows the device staging of host-memory draws to n pixels
+int dn_reserve_image_staging(DNgpuVolume* g, size_t n);
+// gives g a new process-wide unique generation (after any device array of g is reallocated)
+void dn_new_generation(DNgpuVolume* g);
+
+// ------------------------------------------------------------ counters
+
+__device__ __forceinline__ uint32_t lane_id()
+{
+    uint32_t l;
+    asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
+    return l;
+}
+
+__device__ __forceinline__ void flush_counters(unsigned long long* stats, const dn::Counters& c, uint32_t primary, uint32_t lit)
+{
+    // warp-reduce then one atomic per counter per warp
+    uint32_t v[7] = {c.rays, primary, c.outer, c.entered, c.inner, c.hits, lit};
+    const unsigned full = __activemask();
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+        uint32_t x = v[k];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(full, x, o);
+        v[k] = x;
+    }
+    int leader = __ffs(full) - 1;
+    if ((int)lane_id() == leader) {
+#pragma unroll
+        for (int k = 0; k < 7; k++) if (v[k]) atomicAdd(&stats[k], (unsigned long long)v[k]);
+    }
+}
+
+// ------------------------------------------------------------------ draw
+
+// one image of one map
+struct DrawMap {
+    dn::DevMap m;
+    dn_draw_params p;
+    float4* color;
+    uint32_t* hit;
+    uint8_t* face;
+    unsigned long long* stats;
+};
+
+struct DrawArgs {
+    DrawMap d;
+    dn::Material mats[256];
+};
+
+// One primary ray (voxelDraw.comp:24-147): pixel (x, y) of the image described by a; smat holds the map's
+// materials.  Returns 1 when a primary ray was traced.
+__device__ __forceinline__ uint32_t draw_pixel(const DrawMap& a, const dn::Material* smat, uint32_t x, uint32_t y,
+                                               dn::Counters& cnt)
+{
+    using namespace dn;
+    const dn_draw_params& p = a.p;
+    RayCtx c;
+    c.m = &a.m; c.mats = smat;
+    c.sunStrength = mk(p.sunStrength[0], p.sunStrength[1], p.sunStrength[2]);
+    c.emissive = p.emissiveStrength;
+    c.refraction = true;   // voxelDraw.comp:65
+    c.c = Counters{0, 0, 0, 0, 0};
+    uint32_t primary = 0;
+    if (x < p.width && y < p.height) {
+        const uint64_t pix = (uint64_t)y * p.width + x;
+        uint32_t hitIdx = 0xFFFFFFFFu;
+        uint8_t face = 6;
+        float4 out;
+        const uint32_t limW = p.truncate16 ? (p.width / 16u) * 16u : p.width;
+        const uint32_t limH = p.truncate16 ? (p.height / 16u) * 16u : p.height;
+        if (x >= limW || y >= limH) {
+            out = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+        } else {
+            const float sx = (float)x / (float)p.width * 2.0f - 1.0f;
+            const float sy = (float)y / (float)p.height * 2.0f - 1.0f;
+            f3 rayPos = mk(p.origin[0], p.origin[1], p.origin[2]);
+            c.orgRayPos = rayPos;
+            const float (*M)[4] = p.dirMat;
+            f3 rd = mk(M[0][0] * sx + M[1][0] * sy + M[2][0] * 0.0f + M[3][0] * 1.0f,
+                       M[0][1] * sx + M[1][1] * sy + M[2][1] * 0.0f + M[3][1] * 1.0f,
+                       M[0][2] * sx + M[1][2] * sy + M[2][2] * 0.0f + M[3][2] * 1.0f);
+            f3 rayDir = adds(normalize(rd), EPS);
+            f3 inv = mk(1.0f / rayDir.x, 1.0f / rayDir.y, 1.0f / rayDir.z);
+            const float maxDepth = -1.0f;
+            const f3 mapMax = mk((float)a.m.sx, (float)a.m.sy, (float)a.m.sz);
+            const f3 skyBot = mk(p.skyBot[0], p.skyBot[1], p.skyBot[2]), skyTop = mk(p.skyTop[0], p.skyTop[1], p.skyTop[2]);
+            // intersect_AABB, voxelShared.comp:261-273
+            f3 tMin = mul(sub(mk(0.0f, 0.0f, 0.0f), rayPos), inv);
+            f3 tMax = mul(sub(mapMax, rayPos), inv);
+            f3 t1 = mk(gmin(tMin.x, tMax.x), gmin(tMin.y, tMax.y), gmin(tMin.z, tMax.z));
+            f3 t2 = mk(gmax(tMin.x, tMax.x), gmax(tMin.y, tMax.y), gmax(tMin.z, tMax.z));
+            float tNear = gmax(gmax(t1.x, t1.y), t1.z);
+            float tFar = gmin(gmin(t2.x, t2.y), t2.z);
+            f3 fc;
+            float depth = -1.0f;
+            if (tNear > tFar || tFar < 0.0f) {
+                f3 s = sky_color(skyBot, skyTop, rayDir);
+                fc = mk(powf(s.x, 2.2f), powf(s.y, 2.2f), powf(s.z, 2.2f));
+            } else {
+                if (tNear > 0.0f) rayPos = add(rayPos, muls(rayDir, tNear + EPS));
+                // normal_AABB, voxelShared.comp:276-284
+                f3 cc = muls(add(mk(0.0f, 0.0f, 0.0f), mapMax), 0.5f);
+                f3 pp = sub(rayPos, cc);
+                f3 dd = muls(sub(mapMax, mk(0.0f, 0.0f, 0.0f)), 0.5f);
+                const float bias = 1.0f + EPS;
+                f3 q = mk(pp.x / dd.x * bias, pp.y / dd.y * bias, pp.z / dd.z * bias);
+                f3 hitNormal = normalize(mk(truncf(q.x), truncf(q.y), truncf(q.z)));
+                TState ts{255u, 1.0f};
+                Voxel fv;
+                fv.normal = mk(0.0f, 0.0f, 0.0f); fv.material = 0; fv.albedo = fv.normal; fv.spec = fv.normal; fv.diff = fv.normal;
+                f3 cadd; float cmul; HitInfo hi;
+                primary = 1;
+                if (step_map(c, ts, rayDir, inv, rayPos, false, maxDepth, hitNormal, fv, cadd, cmul, hi)) {
+                    i3 mp{f2i(floorf(rayPos.x)), f2i(floorf(rayPos.y)), f2i(floorf(rayPos.z))};
+                    if (in_map(a.m, mp)) {
+                        uint8_t* vp = &a.m.tvis[map_index(a.m, mp)];
+                        if (*vp == 0) *vp = 1;
+                    }
+                    f3 dv = sub(rayPos, c.orgRayPos);
+                    depth = sqrtf(dot(dv, dv));
+                    // voxel_color, voxelDraw.comp:32-61
+                    const Material& mt = smat[fv.material];
+                    f3 sp = muls(fv.spec, mt.specular);
+                    f3 df = muls(fv.diff, 1.0f - mt.specular);
+                    switch (p.viewMode) {
+                    case 0: {
+                        f3 solid = mt.emissive ? muls(fv.albedo, c.emissive) : add(mul(df, fv.albedo), sp);
+                        fc = add(muls(solid, cmul), cadd);
+                        break;
+                    }
+                    case 1: fc = fv.albedo; break;
+                    case 2: fc = mt.emissive ? fv.albedo : df; break;
+                    case 3: fc = mt.emissive ? fv.albedo : sp; break;
+                    case 4: fc = vabs(fv.normal); break;
+                    case 5: fc = vabs(hitNormal); break;
+                    default: fc = mk(0.0f, 0.0f, 0.0f); break;
+                    }
+                    const uint32_t tx = hi.tile % a.m.sx, ty = (hi.tile / a.m.sx) % a.m.sy, tz = hi.tile / (a.m.sx * a.m.sy);
+                    const uint32_t gx = tx * 8u + (uint32_t)hi.local.x, gy = ty * 8u + (uint32_t)hi.local.y,
+                                   gz = tz * 8u + (uint32_t)hi.local.z;
+                    hitIdx = gx + (a.m.sx * 8u) * (gy + (a.m.sy * 8u) * gz);
+                    if (hitNormal.x > 0.0f) face = 0; else if (hitNormal.x < 0.0f) face = 1;
+                    else if (hitNormal.y > 0.0f) face = 2; else if (hitNormal.y < 0.0f) face = 3;
+                    else if (hitNormal.z > 0.0f) face = 4; else if (hitNormal.z < 0.0f) face = 5;
+                } else {
+                    f3 s = sky_color(skyBot, skyTop, rayDir);
+                    f3 bg = mk(powf(s.x, 2.2f), powf(s.y, 2.2f), powf(s.z, 2.2f));
+                    fc = add(muls(bg, cmul), cadd);
+                    depth = maxDepth;
+                }
+            }
+            out = make_float4(powf(fc.x, 0.4545f), powf(fc.y, 0.4545f), powf(fc.z, 0.4545f), depth);
+        }
+        a.color[pix] = out;
+        if (a.hit) a.hit[pix] = hitIdx;
+        if (a.face) a.face[pix] = face;
+    }
+    cnt = c.c;
+    return primary;
+}
+
+// -------------------------------------------------------------- sync
+
+// spreads the 16 low bits of x to the even bit positions of a word
+__device__ __forceinline__ uint32_t spread_bits(uint32_t x)
+{
+    x &= 0xFFFFu;
+    x = (x | (x << 8)) & 0x00FF00FFu;
+    x = (x | (x << 4)) & 0x0F0F0F0Fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    x = (x | (x << 1)) & 0x55555555u;
+    return x;
+}
+
+struct CompactArgs {
+    uint32_t* tword; uint8_t* treq; uint8_t* tvis; uint8_t* ttouch; uint32_t* tlast;
+    uint32_t* tbits;
+    uint32_t* tpend; const uint32_t* tpendSlot;
+    const dn::ChunkRec* rec;
+    uint32_t* reqs; uint64_t reqCap;
+    DevState* st;
+    uint64_t ntiles;
+    uint32_t op, split, frameNum;
+};
+
+// Tiles [base, base + blockDim.x) of one map: the per-tile loop of DN_sync_gpu (voxel.c:738-762) with the
+// request rule of _DN_request_chunk_lighting (1463-1489) and the state machine of _DN_stream_to_gpu
+// (1491-1536).  blockDim.x is a multiple of 32 and base a multiple of 32.
+__device__ __forceinline__ void compact_tiles(const CompactArgs& a, uint64_t base)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t t = base + threadIdx.x;
+    uint32_t groups = 0;
+    uint32_t finalSt = 0;
+    if (t < a.ntiles) {
+        const uint32_t w = a.tword[t];
+        const uint32_t st = w >> 30;
+        finalSt = st;
+        uint32_t slot = w & dn::SLOT_MASK;
+        const uint32_t pend = a.tpend[t];
+        const bool req = a.treq[t] != 0;
+        uint32_t vis = a.tvis[t];
+        uint32_t gflag = (st == 1u && req) ? 3u : st;
+        const bool updated = (pend & DN_PEND_UPDATED) != 0;
+        uint32_t lu = a.tlast[t];
+        if (a.ttouch[t]) { lu = 0; a.ttouch[t] = 0; }
+        if (lu != 0xFFFFFFFFu) lu++;
+        if (a.op != 1u && gflag == 2u && vis && (((uint32_t)t % a.split) == a.frameNum || updated)) {
+            groups = (a.rec[slot].nvox + 31u) / 32u;
+            vis = 0;
+        }
+        if (a.op != 0u) {
+            const bool valid = (pend & DN_PEND_VALID) != 0;
+            const bool exists = valid ? (pend & DN_PEND_EXISTS) != 0 : (st != 0u);
+            const uint32_t newSlot = (pend & DN_PEND_STAGED) ? a.tpendSlot[t] : (valid ? DN_SLOT_NONE : slot);
+            bool changed = false;
+            if (exists && gflag == 0u) { gflag = 1u; changed = true; }
+            else if (!exists && gflag != 0u) { gflag = 0u; changed = true; }
+            if (gflag == 2u && updated) { gflag = 3u; changed = true; }
+            if (gflag == 3u && exists && newSlot != DN_SLOT_NONE) { gflag = 2u; lu = 0; changed = true; }
+            if (changed) vis = 0;
+            slot = exists ? newSlot : DN_SLOT_NONE;
+            a.treq[t] = (gflag == 3u) ? 1 : 0;
+            finalSt = gflag == 3u ? 1u : gflag;
+            a.tword[t] = (finalSt << 30) | (slot & dn::SLOT_MASK);
+        }
+        if (pend) a.tpend[t] = 0;
+        a.tvis[t] = (uint8_t)vis;
+        a.tlast[t] = lu;
+    }
+    // the 2-bit tile map read by the chunk-level DDA step: 32 tiles per warp, two words
+    {
+        const unsigned b0 = __ballot_sync(0xFFFFFFFFu, finalSt == 1u);
+        const unsigned b1 = __ballot_sync(0xFFFFFFFFu, finalSt == 2u);
+        if (lane == 0 && base + threadIdx.x - lane < a.ntiles) {
+            const uint64_t wi = (base + threadIdx.x) >> 4;
+            a.tbits[wi] = spread_bits(b0 & 0xFFFFu) | (spread_bits(b1 & 0xFFFFu) << 1);
+            a.tbits[wi + 1] = spread_bits(b0 >> 16) | (spread_bits(b1 >> 16) << 1);
+        }
+    }
+    // warp-aggregated append of (tile << 4 | group) request words
+    uint32_t incl = groups;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if ((int)lane >= o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    uint32_t wbase = 0;
+    if (lane == 31 && total) wbase = atomicAdd(&a.st->w[ST_REQ], total);
+    wbase = __shfl_sync(0xFFFFFFFFu, wbase, 31);
+    if (groups) {
+        const uint32_t first = wbase + incl - groups;
+        for (uint32_t gi = 0; gi < groups; gi++) {
+            if ((uint64_t)first + gi < a.reqCap) a.reqs[first + gi] = ((uint32_t)t << 4) | gi;
+            else atomicOr(&a.st->w[ST_ERR], 4u);
+        }
+    }
+}
+
+// D1/D2: lane `lane` of request r of one map: copy its new lighting into the pool and count the sample
+__device__ __forceinline__ void commit_lane(const dn::DevMap& m, const uint32_t* reqs, const float4* out, uint64_t i,
+                                            uint32_t r, uint32_t lane, float4* diff, float4* spec, uint32_t* nsamples)
+{
+    const uint32_t word = reqs[r];
+    const uint32_t tile = word >> 4, group = word & 15u;
+    const uint32_t tw = m.tword[tile];
+    if ((tw >> 30) != 2u) return;
+    const uint32_t slot = tw & dn::SLOT_MASK;
+    const dn::ChunkRec* rc = &m.rec[slot];
+    const uint32_t vn = group * 32u + lane;
+    if (vn >= rc->nvox) return;
+    const uint32_t idx = rc->voxBase + vn;
+    diff[idx] = out[i * 2u];
+    spec[idx] = out[i * 2u + 1u];
+    if (vn == 0) nsamples[slot] += 1u;
+}

@@ -25,6 +25,10 @@
 
 namespace dn {
 
+#ifndef DN_STREAM_MIN_BLOCKS
+#define DN_STREAM_MIN_BLOCKS 4   // 4 blocks of 4 warps per SM (measured best: leaves L1 room for the tile map)
+#endif
+
 enum : uint32_t { PH_FETCH = 0, PH_SPEC = 1, PH_SHADOW = 2, PH_DIFF = 3, PH_FINAL = 4, PH_DONE = 5 };
 
 struct StreamArgs {
@@ -72,7 +76,7 @@ __device__ __forceinline__ void seg_begin(Seg& s, f3 pos, f3 dir, f3 inv)
 // the hit, hitIdx = pool index of the voxel), 2 when it leaves the map.  The common case (a chunk cell that
 // is not loaded, or a voxel cell that is empty) runs one code path for both levels; entering a chunk, leaving
 // it, reaching a voxel and leaving the map are the divergent events.
-__device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Material* mats, f3 sunStrength,
+__device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Material* mats, const float* sunStrength,
                                              Counters& c, uint32_t& hitIdx)
 {
     const f3 delta = vabs(s.inv);
@@ -135,9 +139,9 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
                 const f3 alb = mk((float)((vw.y >> 24) & 0xFF) * INV255, (float)((vw.y >> 16) & 0xFF) * INV255,
                                   (float)((vw.y >> 8) & 0xFF) * INV255);
                 const float k = s.cmul * mat.opacity;
-                s.cadd.x = s.cadd.x + k * alb.x * sunStrength.x;
-                s.cadd.y = s.cadd.y + k * alb.y * sunStrength.y;
-                s.cadd.z = s.cadd.z + k * alb.z * sunStrength.z;
+                s.cadd.x = s.cadd.x + k * alb.x * sunStrength[0];
+                s.cadd.y = s.cadd.y + k * alb.y * sunStrength[1];
+                s.cadd.z = s.cadd.z + k * alb.z * sunStrength[2];
                 s.cmul = s.cmul * (1.0f - mat.opacity);
                 s.ts.lastVoxID = thisID;
                 s.ts.lastVoxRefract = mat.refractIndex;
@@ -179,6 +183,7 @@ struct Job {
     f3 spec, direct, acc;           // acc: shadow sum, then diffuse sum
     f3 jA, jB, jC;                  // spec: mult, lastPos ; diffuse: nc, hitNormal, lastDir
     uint32_t jU;                    // spec: reflectType ; diffuse: material of the last hit
+    uint32_t map;                   // many-map launches: the voxel's map
 };
 
 } // namespace dn
@@ -220,11 +225,10 @@ __device__ __forceinline__ f3 diffuse_dir(const Job& j, const dn_light_params& p
 
 // Consumes the finished segment (hitState 1 hit / 2 miss) and sets up the next segment of this lane's
 // voxel; returns true when a segment was started.  Leaves the job in PH_FETCH when the voxel is done.
-__device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint32_t hitIdx, const StreamArgs& a,
-                                        const StreamShared& sh, Counters& c, uint32_t& lit)
+__device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint32_t hitIdx, const DevMap& m,
+                                        const dn_light_params& p, const Material* mats, const float (*sdir)[3],
+                                        const float (*sinv)[3], float4* out, Counters& c, uint32_t& lit)
 {
-    const dn_light_params& p = a.p;
-    const DevMap& m = a.m;
     const bool rngSin = p.rngMode == 1u;
     const f3 sun = mk(p.sunStrength[0], p.sunStrength[1], p.sunStrength[2]);
     const f3 sunDir = mk(p.sunDir[0], p.sunDir[1], p.sunDir[2]);
@@ -244,7 +248,7 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
                 }
                 const f3 d = vabs(sub(vfloor(muls(s.pos, 8.0f)), vfloor(muls(j.jB, 8.0f))));
                 if (!(dot(d, d) <= 1.0f)) {
-                    const Material& hm = sh.mats[hv.material];
+                    const Material& hm = mats[hv.material];
                     const f3 hd = muls(hv.diff, 1.0f - hm.specular);
                     if (hm.emissive) {
                         j.spec.x = j.spec.x + ((hv.albedo.x * p.emissiveStrength * s.cmul + s.cadd.x) * j.jA.x) * j.talbedo.x;
@@ -300,7 +304,7 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
                 j.jU = hv.material;
                 const f3 d = vabs(sub(vfloor(muls(j.pos0, 8.0f)), vfloor(muls(s.pos, 8.0f))));
                 if (!(dot(d, d) < 1.0f)) {
-                    const Material& hm = sh.mats[hv.material];
+                    const Material& hm = mats[hv.material];
                     if (hm.emissive) {
                         j.acc.x = j.acc.x + j.jA.x * (hv.albedo.x * p.emissiveStrength * s.cmul + s.cadd.x);
                         j.acc.y = j.acc.y + j.jA.y * (hv.albedo.y * p.emissiveStrength * s.cmul + s.cadd.y);
@@ -312,7 +316,7 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
                         j.jC = s.dir;
                         j.b++;
                         if (j.b < p.diffuseBounceLimit) {
-                            const f3 nd = diffuse_dir(j, p, sh.mats, rngSin);
+                            const f3 nd = diffuse_dir(j, p, mats, rngSin);
                             const TState keep = s.ts;
                             seg_begin(s, s.pos, nd, rcp3(nd));
                             s.ts = keep;
@@ -335,7 +339,7 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
         if (j.phase == PH_SPEC) {
             if (j.k < p.K) {
                 if (p.specBounceLimit == 0u) { j.k++; continue; }
-                const Material& tm = sh.mats[j.tmat];
+                const Material& tm = mats[j.tmat];
                 j.b = 0; j.jA = j.talbedo; j.jB = j.pos0; j.jU = tm.reflectType;
                 const f3 P = mk(p.spherePts[j.k][0], p.spherePts[j.k][1], p.spherePts[j.k][2]);
                 const f3 sd = adds(normalize(add(muls(j.refl, (float)tm.shininess), P)), EPS);
@@ -352,8 +356,7 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
             const uint32_t n = j.firstSample ? 1u : p.K;
             if (j.k < n) {
                 const uint32_t q = j.firstSample ? 64u : j.k;
-                seg_begin(s, j.pos0, mk(sh.sdir[q][0], sh.sdir[q][1], sh.sdir[q][2]),
-                          mk(sh.sinv[q][0], sh.sinv[q][1], sh.sinv[q][2]));
+                seg_begin(s, j.pos0, mk(sdir[q][0], sdir[q][1], sdir[q][2]), mk(sinv[q][0], sinv[q][1], sinv[q][2]));
                 c.rays++;
                 return true;
             }
@@ -374,7 +377,7 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
                     j.jC = mk(0.0f, 0.0f, 0.0f);
                     j.jU = j.tmat;
                 }
-                const f3 nd = diffuse_dir(j, p, sh.mats, rngSin);
+                const f3 nd = diffuse_dir(j, p, mats, rngSin);
                 seg_begin(s, j.pos0, nd, rcp3(nd));
                 c.rays++;
                 return true;
@@ -393,8 +396,8 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
             const float4 outD = make_float4(gmin(gmax(j.acc.x, 0.0f), 1.0f), gmin(gmax(j.acc.y, 0.0f), 1.0f),
                                             gmin(gmax(j.acc.z, 0.0f), 1.0f), 0.0f);
             const uint64_t o = ((uint64_t)j.req * 32u + j.vlane) * 2u;
-            a.out[o] = outD;
-            a.out[o + 1] = outS;
+            out[o] = outD;
+            out[o + 1] = outS;
             lit++;
             j.phase = PH_FETCH;
         }
@@ -404,12 +407,11 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
 }
 
 // Sets up voxel (req, vlane); returns false (and writes zero outputs) when the slot holds no voxel.
-__device__ __forceinline__ bool voxel_setup(Job& j, uint32_t req, uint32_t vlane, const StreamArgs& a, const StreamShared& sh)
+__device__ __forceinline__ bool voxel_setup(Job& j, uint32_t req, uint32_t vlane, const DevMap& m, const dn_light_params& p,
+                                            const Material* mats, const uint32_t* reqs, const uint32_t* nsamples, float4* out)
 {
-    const DevMap& m = a.m;
-    const dn_light_params& p = a.p;
     j.req = req; j.vlane = vlane;
-    const uint32_t word = a.reqs[req];
+    const uint32_t word = reqs[req];
     const uint32_t tile = word >> 4, group = word & 15u;
     const uint32_t tw = __ldg(&m.tword[tile]);
     const uint32_t vn = group * 32u + vlane;
@@ -417,8 +419,8 @@ __device__ __forceinline__ bool voxel_setup(Job& j, uint32_t req, uint32_t vlane
     const ChunkRec* rc = &m.rec[tw & SLOT_MASK];
     if ((tw >> 30) != 2u || vn >= __ldg(&rc->nvox) || !select_voxel(rc, vn, cp, li)) {
         const uint64_t o = ((uint64_t)req * 32u + vlane) * 2u;
-        a.out[o] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        a.out[o + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        out[o] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        out[o + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         return false;
     }
     const i3 mp{__ldg(&rc->pos[0]), __ldg(&rc->pos[1]), __ldg(&rc->pos[2])};
@@ -429,7 +431,7 @@ __device__ __forceinline__ bool voxel_setup(Job& j, uint32_t req, uint32_t vlane
     j.tmat = w.x >> 24;
     j.talbedo = mk((float)((w.y >> 24) & 0xFF) * INV255, (float)((w.y >> 16) & 0xFF) * INV255,
                    (float)((w.y >> 8) & 0xFF) * INV255);
-    const uint32_t samples = __ldg(&a.nsamples[tw & SLOT_MASK]);
+    const uint32_t samples = __ldg(&nsamples[tw & SLOT_MASK]);
     const uint32_t ns = samples < p.maxDiffuse ? samples : p.maxDiffuse;
     j.indirect = (float)ns;
     j.firstSample = (j.indirect == 0.0f);
@@ -441,7 +443,7 @@ __device__ __forceinline__ bool voxel_setup(Job& j, uint32_t req, uint32_t vlane
     rp.z = INV_CHUNK * (float)cp.z + (float)mp.z + HALF_INV_CHUNK;
     const float off = HALF_INV_CHUNK - EPS;
     j.pos0 = add(rp, muls(j.tnormal, off));
-    const Material& tm = sh.mats[j.tmat];
+    const Material& tm = mats[j.tmat];
     const f3 viewDir = sub(j.pos0, mk(p.camPos[0], p.camPos[1], p.camPos[2]));
     j.doSpec = tm.specular > 0.0f && dot(viewDir, j.tnormal) < 0.0f && tm.reflectType <= 1u;
     j.doDiff = tm.specular < 1.0f;
@@ -450,6 +452,146 @@ __device__ __forceinline__ bool voxel_setup(Job& j, uint32_t req, uint32_t vlane
     j.k = 0; j.b = 0; j.i = 0;
     j.phase = j.doSpec ? PH_SPEC : (j.doDiff ? PH_SHADOW : PH_FINAL);
     return true;
+}
+
+// ------------------------------------------------------------ launches
+
+// one map of a many-map lighting launch (device memory, written by the host and by k_batch_prep)
+struct BatchLightMap {
+    DevMap m;
+    const uint32_t* reqs;
+    const uint32_t* nsamples;
+    float4* out;
+    uint32_t* nreqPtr;          // the map's request count (clamped by k_batch_prep)
+    uint64_t reqCap;
+    dn_light_params p;
+    const Material* mats;       // the map's 256 materials
+    float4* diffOut;            // committed lighting and sample counts (k_commit_batch)
+    float4* specOut;
+    uint32_t* samplesOut;
+    float sdir[65][3];          // shadow directions of this map (k_batch_prep)
+    float sinv[65][3];
+};
+
+struct BatchLightArgs {
+    BatchLightMap* maps;
+    const uint32_t* reqStart;   // [nmaps + 1]: first request of each map in the launch's queue
+    uint32_t nmaps;
+    uint32_t* workCounter;
+    unsigned long long* stats;
+    uint32_t batch;
+};
+
+// shadow directions normalize(sunDir * softness + P_k) + EPS (k < K) and sunDir + EPS ([64]) with reciprocals
+__device__ __forceinline__ void shadow_dir(const dn_light_params& p, int k, float* d3, float* i3)
+{
+    const f3 sd = mk(p.sunDir[0], p.sunDir[1], p.sunDir[2]);
+    f3 d;
+    if (k == 64) d = adds(sd, EPS);
+    else if ((uint32_t)k < p.K) {
+        const f3 P = mk(p.spherePts[k][0], p.spherePts[k][1], p.spherePts[k][2]);
+        d = adds(normalize(add(muls(sd, p.shadowSoftness), P)), EPS);
+    } else d = mk(1.0f, 1.0f, 1.0f);
+    d3[0] = d.x; d3[1] = d.y; d3[2] = d.z;
+    i3[0] = __frcp_rn(d.x); i3[1] = __frcp_rn(d.y); i3[2] = __frcp_rn(d.z);
+}
+
+// The persistent loop of a lighting launch.  MANY = false: one map whose arguments live in the launch's
+// parameter space (one) and whose materials and shadow directions were staged into sh.  MANY = true: a
+// queue over the requests of many maps (many); each lane keeps a register copy of its current voxel's map
+// and reads that map's parameters, materials and shadow directions from device memory.
+template <bool MANY>
+__device__ __forceinline__ void stream_loop(const StreamArgs* one, const BatchLightArgs* many, const StreamShared* sh,
+                                            Job& j)
+{
+    const uint32_t lane = lane_id_s();
+    const uint32_t batch = MANY ? many->batch : one->batch;
+    uint32_t nreq = 0;
+    if constexpr (MANY) nreq = *(volatile const uint32_t*)&many->reqStart[many->nmaps];
+    else nreq = *(volatile const uint32_t*)one->nreqPtr;
+    uint32_t* const counter = MANY ? many->workCounter : one->workCounter;
+    uint32_t winMap = 0, winReq = 0, winNext = 32;     // warp-uniform voxel window: map, request, next lane in it
+    bool exhausted = false;
+    j.phase = PH_FETCH;
+    j.map = 0;
+    // the lane's current map (MANY only)
+    DevMap lm;
+    const BatchLightMap* le = nullptr;
+    uint32_t lmi = 0xFFFFFFFFu;
+    if constexpr (MANY) { lm = many->maps[0].m; le = &many->maps[0]; lmi = 0; }
+    auto M = [&]() -> const DevMap& { if constexpr (MANY) return lm; else return one->m; };
+    auto P = [&]() -> const dn_light_params& { if constexpr (MANY) return le->p; else return one->p; };
+    auto MATS = [&]() -> const Material* { if constexpr (MANY) return le->mats; else return sh->mats; };
+    Seg s;
+    bool rayActive = false;
+    uint32_t hitState = 0, hitIdx = 0;
+    Counters c{0, 0, 0, 0, 0};
+    uint32_t lit = 0;
+    while (true) {
+        const unsigned waiting = __ballot_sync(0xFFFFFFFFu, !rayActive && j.phase != PH_DONE);
+        const unsigned stepping = __ballot_sync(0xFFFFFFFFu, rayActive);
+        if (waiting == 0u && stepping == 0u) break;
+        if (stepping == 0u || (uint32_t)__popc(waiting) >= batch) {
+            for (int round = 0; round < 4; round++) {
+                // warp-cooperative voxel fetch for lanes whose voxel is done
+                for (int guard = 0; guard < 64; guard++) {
+                    const unsigned need = __ballot_sync(0xFFFFFFFFu, j.phase == PH_FETCH);
+                    if (need == 0u) break;
+                    if (winNext >= 32u) {
+                        uint32_t r = 0;
+                        if (!exhausted && lane == 0) r = atomicAdd(counter, 1u);
+                        r = __shfl_sync(0xFFFFFFFFu, r, 0);
+                        if (exhausted || r >= nreq) {
+                            exhausted = true;
+                            if (j.phase == PH_FETCH) j.phase = PH_DONE;
+                            break;
+                        }
+                        if constexpr (MANY) {
+                            // the map whose request range holds r: reqStart[map] <= r < reqStart[map + 1]
+                            uint32_t lo = 0, hi = many->nmaps;
+                            while (hi - lo > 1u) {
+                                const uint32_t mid = (lo + hi) >> 1;
+                                if (__ldg(&many->reqStart[mid]) <= r) lo = mid; else hi = mid;
+                            }
+                            winMap = lo;
+                            winReq = r - __ldg(&many->reqStart[lo]);
+                        } else {
+                            winReq = r;
+                        }
+                        winNext = 0;
+                    }
+                    const uint32_t rank = __popc(need & ((1u << lane) - 1u));
+                    if (j.phase == PH_FETCH && winNext + rank < 32u) {
+                        if constexpr (MANY) {
+                            const BatchLightMap& e = many->maps[winMap];
+                            if (winMap != lmi) { lm = e.m; le = &e; lmi = winMap; }
+                            j.map = winMap;
+                            voxel_setup(j, winReq, winNext + rank, lm, e.p, e.mats, e.reqs, e.nsamples, e.out);
+                        } else {
+                            voxel_setup(j, winReq, winNext + rank, one->m, one->p, sh->mats, one->reqs, one->nsamples, one->out);
+                        }
+                    }
+                    const uint32_t took = (uint32_t)__popc(need) < 32u - winNext ? (uint32_t)__popc(need) : 32u - winNext;
+                    winNext += took;
+                }
+                // shade the finished segment and set up the next one (or finish the voxel)
+                if (!rayActive && j.phase != PH_DONE && j.phase != PH_FETCH) {
+                    if constexpr (MANY) {
+                        if (j.map != lmi) { le = &many->maps[j.map]; lm = le->m; lmi = j.map; }
+                        rayActive = advance(j, s, hitState, hitIdx, lm, le->p, le->mats, le->sdir, le->sinv, le->out, c, lit);
+                    } else {
+                        rayActive = advance(j, s, hitState, hitIdx, one->m, one->p, sh->mats, sh->sdir, sh->sinv, one->out, c, lit);
+                    }
+                }
+                if (__ballot_sync(0xFFFFFFFFu, j.phase == PH_FETCH) == 0u) break;
+            }
+        }
+        if (rayActive) {
+            const uint32_t r = seg_step(s, M(), MATS(), P().sunStrength, c, hitIdx);
+            if (r) { rayActive = false; hitState = r; }
+        }
+    }
+    flush_counters(MANY ? many->stats : one->stats, c, 0, lit);
 }
 
 } // namespace dn

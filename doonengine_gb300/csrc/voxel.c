@@ -104,6 +104,8 @@ typedef struct DNvolumePriv
 	u32vec deferredSlots;
 	/* the last view/projection passed to DN_draw */
 	float sphereK; float spherePts[64][3]; uint32_t sphereValid;
+	struct DNbatch* batch;     /* the batch this volume belongs to, if any */
+	uint64_t batchStamp;       /* the batch run that last listed this volume */
 } DNvolumePriv;
 
 static inline DNvolumePriv* priv(DNvolume* v) { return (DNvolumePriv*)v; }
@@ -281,6 +283,7 @@ void DN_delete_volume(DNvolume* vol)
 {
 	if (!vol) return;
 	DNvolumePriv* p = priv(vol);
+	if (p->batch) DN_batch_remove(p->batch, vol);
 	if (vol->gpu) dn_cuda_map_destroy(vol->gpu);
 	DN_FREE(vol->map); DN_FREE(vol->chunks); DN_FREE(vol->materials);
 	free_priv_arrays(p);
@@ -752,11 +755,12 @@ static bool grow_scratch(void** buf, size_t* cap, size_t need, size_t elem)
 
 /* ---------------------------------------------------------------- sync */
 
-void DN_sync_gpu(DNvolume* vol, DNmemOp op, int lightingSplit)
+/* Host half of DN_sync_gpu (voxel.c:719-786): advances frameNum, packs every dirty chunk into the
+ * volume's op / record / voxel-word scratch and fills sp.  Returns false when the scratch cannot grow. */
+static bool sync_prepare(DNvolume* vol, DNmemOp op, int lightingSplit, dn_sync_params* spOut, uint32_t* nopsOut,
+                         uint32_t* nrecsOut, uint64_t* nvwOut)
 {
-	/* DN_sync_gpu, voxel.c:719-786 */
 	DNvolumePriv* p = priv(vol);
-	if (!need_device(vol, "DN_sync_gpu")) return;
 	if (lightingSplit < 1) lightingSplit = 1;
 	vol->frameNum++;
 	if (vol->frameNum >= (uint32_t)lightingSplit) vol->frameNum = 0;
@@ -766,7 +770,7 @@ void DN_sync_gpu(DNvolume* vol, DNmemOp op, int lightingSplit)
 	    !grow_scratch((void**)&p->recs, &p->recsCap, nd ? nd : 1, sizeof(dn_chunk_record)) ||
 	    !grow_scratch((void**)&p->vwords, &p->vwordsCap, (nd ? nd : 1) * 1024, sizeof(uint32_t))) {
 		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to allocate sync scratch");
-		return;
+		return false;
 	}
 	uint32_t nops = 0, nrecs = 0;
 	uint64_t nvw = 0;
@@ -817,17 +821,38 @@ void DN_sync_gpu(DNvolume* vol, DNmemOp op, int lightingSplit)
 	}
 	if (p->groupsStaged > vol->lightingRequestCap) DN_set_max_lighting_requests(vol, (size_t)p->groupsStaged * 2);
 
-	dn_sync_params sp;
-	sp.op = (uint32_t)op;
-	sp.split = (uint32_t)lightingSplit;
-	sp.frameNum = vol->frameNum;
-	int rc = dn_cuda_sync(vol->gpu, &sp, p->ops, nops, p->recs, nrecs, p->vwords, nvw / 2);
-	if (rc != DN_CUDA_OK)
-		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "device sync failed: %s", dn_cuda_last_error());
-	/* slots replaced or removed by this sync are reusable by later uploads (stream order) */
+	spOut->op = (uint32_t)op;
+	spOut->split = (uint32_t)lightingSplit;
+	spOut->frameNum = vol->frameNum;
+	*nopsOut = nops;
+	*nrecsOut = nrecs;
+	*nvwOut = nvw;
+	return true;
+}
+
+/* after the device work of a sync was issued: slots replaced or removed by it are reusable by later
+ * uploads (stream order) */
+static void sync_done(DNvolume* vol)
+{
+	DNvolumePriv* p = priv(vol);
 	for (size_t k = 0; k < p->deferredSlots.n; k++) free_slot(p, p->deferredSlots.v[k]);
 	p->deferredSlots.n = 0;
 	vol->numVoxelNodes = (size_t)p->stagedChunks;
+}
+
+void DN_sync_gpu(DNvolume* vol, DNmemOp op, int lightingSplit)
+{
+	/* DN_sync_gpu, voxel.c:719-786 */
+	DNvolumePriv* p = priv(vol);
+	if (!need_device(vol, "DN_sync_gpu")) return;
+	dn_sync_params sp;
+	uint32_t nops = 0, nrecs = 0;
+	uint64_t nvw = 0;
+	if (!sync_prepare(vol, op, lightingSplit, &sp, &nops, &nrecs, &nvw)) return;
+	int rc = dn_cuda_sync(vol->gpu, &sp, p->ops, nops, p->recs, nrecs, p->vwords, nvw / 2);
+	if (rc != DN_CUDA_OK)
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "device sync failed: %s", dn_cuda_last_error());
+	sync_done(vol);
 }
 
 /* ------------------------------------------------------------- drawing */
@@ -856,6 +881,26 @@ void DN_draw_matrices(DNmat4 view, DNmat4 projection, DNmat4* invView, DNmat4* i
 	*invProjection = DN_mat4_inv(projection);
 }
 
+/* the draw parameters DN_draw passes to the device (voxel.c:812-881) */
+static void draw_prepare(DNvolume* vol, const DNimage* output, DNmat4 view, DNmat4 projection, dn_draw_params* dp)
+{
+	DNmat4 iv, icv, ip;
+	DN_draw_matrices(view, projection, &iv, &icv, &ip);
+	DNmat4 M = DN_mat4_mult(icv, ip);
+	memset(dp, 0, sizeof(*dp));
+	for (int r = 0; r < 3; r++)
+		dp->origin[r] = iv.m[0][r] * 0.0f + iv.m[1][r] * 0.0f + iv.m[2][r] * 0.0f + iv.m[3][r] * 1.0f;
+	memcpy(dp->dirMat, M.m, sizeof(dp->dirMat));
+	dp->width = output->width;
+	dp->height = output->height;
+	dp->viewMode = vol->camViewMode;
+	dp->truncate16 = vol->truncateDispatch;
+	memcpy(dp->sunStrength, vol->sunStrength.v, 12);
+	memcpy(dp->skyBot, vol->skyGradientBot.v, 12);
+	memcpy(dp->skyTop, vol->skyGradientTop.v, 12);
+	dp->emissiveStrength = vol->emissiveStrength;
+}
+
 void DN_draw(DNvolume* vol, DNimage* output, DNmat4 view, DNmat4 projection, int rasterColorTexture, int rasterDepthTexture)
 {
 	/* DN_draw, voxel.c:812-881 */
@@ -868,22 +913,8 @@ void DN_draw(DNvolume* vol, DNimage* output, DNmat4 view, DNmat4 projection, int
 		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_NOTE, "raster composition is not available; drawing without it");
 	if (vol->useCubemap)
 		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_NOTE, "cube-map sky is not available; using the sky gradient");
-	DNmat4 iv, icv, ip;
-	DN_draw_matrices(view, projection, &iv, &icv, &ip);
-	DNmat4 M = DN_mat4_mult(icv, ip);
 	dn_draw_params dp;
-	memset(&dp, 0, sizeof(dp));
-	for (int r = 0; r < 3; r++)
-		dp.origin[r] = iv.m[0][r] * 0.0f + iv.m[1][r] * 0.0f + iv.m[2][r] * 0.0f + iv.m[3][r] * 1.0f;
-	memcpy(dp.dirMat, M.m, sizeof(dp.dirMat));
-	dp.width = output->width;
-	dp.height = output->height;
-	dp.viewMode = vol->camViewMode;
-	dp.truncate16 = vol->truncateDispatch;
-	memcpy(dp.sunStrength, vol->sunStrength.v, 12);
-	memcpy(dp.skyBot, vol->skyGradientBot.v, 12);
-	memcpy(dp.skyTop, vol->skyGradientTop.v, 12);
-	dp.emissiveStrength = vol->emissiveStrength;
+	draw_prepare(vol, output, view, projection, &dp);
 	int rc = output->onDevice
 		? dn_cuda_draw(vol->gpu, &dp, (const dn_material*)vol->materials, output->color, output->hitIndex, output->hitFace)
 		: dn_cuda_draw_host(vol->gpu, &dp, (const dn_material*)vol->materials, output->color, output->hitIndex, output->hitFace);
@@ -905,11 +936,11 @@ static void sphere_points(uint32_t K, float out[64][3])
 	}
 }
 
-void DN_update_lighting(DNvolume* vol, int numDiffuseSamples, int maxDiffuseSamples, float time)
+/* the lighting parameters DN_update_lighting passes to the device (voxel.c:883-952); latches the time on
+ * the first frame of a lighting split */
+static void light_prepare(DNvolume* vol, int numDiffuseSamples, int maxDiffuseSamples, float time, dn_light_params* lpOut)
 {
-	/* DN_update_lighting, voxel.c:883-952 */
 	DNvolumePriv* p = priv(vol);
-	if (!need_device(vol, "DN_update_lighting")) return;
 	if (vol->frameNum == 0) vol->lastTime = time;
 	dn_light_params lp;
 	memset(&lp, 0, sizeof(lp));
@@ -939,6 +970,15 @@ void DN_update_lighting(DNvolume* vol, int numDiffuseSamples, int maxDiffuseSamp
 		p->sphereValid = 1;
 	}
 	memcpy(lp.spherePts, p->spherePts, sizeof(lp.spherePts));
+	*lpOut = lp;
+}
+
+void DN_update_lighting(DNvolume* vol, int numDiffuseSamples, int maxDiffuseSamples, float time)
+{
+	/* DN_update_lighting, voxel.c:883-952 */
+	if (!need_device(vol, "DN_update_lighting")) return;
+	dn_light_params lp;
+	light_prepare(vol, numDiffuseSamples, maxDiffuseSamples, time, &lp);
 	int rc = dn_cuda_light(vol->gpu, &lp, (const dn_material*)vol->materials);
 	if (rc != DN_CUDA_OK)
 		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_ERROR, "lighting update failed: %s", dn_cuda_last_error());
@@ -1038,7 +1078,8 @@ size_t DN_abi_layout(uint64_t* out, size_t n)
 		offsetof(DNvolume, materials), offsetof(DNvolume, camPos), offsetof(DNvolume, sunDir),
 		offsetof(DNvolume, useCubemap), offsetof(DNvolume, frameNum), offsetof(DNvolume, emissiveStrength),
 		offsetof(DNvolume, deviceBudgetBytes), sizeof(DNchunk), sizeof(DNmaterial), sizeof(DNimage),
-		sizeof(DNchunkHandle), sizeof(DNstats), offsetof(DNchunk, voxels), sizeof(DNvoxel)
+		sizeof(DNchunkHandle), sizeof(DNstats), offsetof(DNchunk, voxels), sizeof(DNvoxel),
+		sizeof(DNbatchItem), offsetof(DNbatchItem, view), offsetof(DNbatchItem, op), offsetof(DNbatchItem, time)
 	};
 	size_t k = sizeof(v) / sizeof(v[0]);
 	for (size_t i = 0; i < n && i < k; i++) out[i] = v[i];
@@ -1056,4 +1097,169 @@ uint32_t dn_pack_chunk(const DNvolume* vol, const DNchunk* chunk, uint32_t mask[
 	memcpy(mask, r.mask, sizeof(r.mask));
 	memcpy(partial, r.partial, sizeof(r.partial));
 	return n;
+}
+
+/* ---------------------------------------------------------------- batches */
+
+struct DNbatch
+{
+	struct DNgpuBatch* gpu;
+	DNvolume** members; size_t nmembers, membersCap;
+	dn_batch_item* items; size_t itemsCap;
+	uint64_t runs;
+};
+
+DNbatch* DN_batch_create(void)
+{
+	DNbatch* b = (DNbatch*)DN_MALLOC(sizeof(DNbatch));
+	if (!b) { dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to allocate a batch"); return NULL; }
+	memset(b, 0, sizeof(*b));
+	if (dn_cuda_batch_create(&b->gpu) != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "failed to create a batch: %s", dn_cuda_last_error());
+		DN_FREE(b);
+		return NULL;
+	}
+	return b;
+}
+
+void DN_batch_destroy(DNbatch* b)
+{
+	if (!b) return;
+	for (size_t i = 0; i < b->nmembers; i++) priv(b->members[i])->batch = NULL;
+	dn_cuda_batch_destroy(b->gpu);
+	DN_FREE(b->members);
+	DN_FREE(b->items);
+	DN_FREE(b);
+}
+
+bool DN_batch_add(DNbatch* b, DNvolume* vol)
+{
+	if (!b || !vol || !need_device(vol, "DN_batch_add")) return false;
+	if (priv(vol)->batch) { dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "DN_batch_add: the volume already belongs to a batch"); return false; }
+	if (!grow_scratch((void**)&b->members, &b->membersCap, b->nmembers + 1, sizeof(DNvolume*))) {
+		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to grow a batch");
+		return false;
+	}
+	if (dn_cuda_batch_add(b->gpu, vol->gpu) != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "DN_batch_add: %s", dn_cuda_last_error());
+		return false;
+	}
+	b->members[b->nmembers++] = vol;
+	priv(vol)->batch = b;
+	return true;
+}
+
+bool DN_batch_remove(DNbatch* b, DNvolume* vol)
+{
+	if (!b || !vol || priv(vol)->batch != b) return false;
+	for (size_t i = 0; i < b->nmembers; i++) {
+		if (b->members[i] != vol) continue;
+		b->members[i] = b->members[--b->nmembers];
+		priv(vol)->batch = NULL;
+		if (dn_cuda_batch_remove(b->gpu, vol->gpu) != DN_CUDA_OK) {
+			dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "DN_batch_remove: %s", dn_cuda_last_error());
+			return false;
+		}
+		return true;
+	}
+	return false;
+}
+
+bool DN_batch_run(DNbatch* b, const DNbatchItem* items, unsigned int count)
+{
+	if (!b || (!items && count)) return false;
+	if (!grow_scratch((void**)&b->items, &b->itemsCap, count ? count : 1, sizeof(dn_batch_item))) {
+		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to allocate batch items");
+		return false;
+	}
+	/* every item is checked before any volume's state moves */
+	const uint64_t run = ++b->runs;
+	for (unsigned int i = 0; i < count; i++) {
+		const DNbatchItem* it = &items[i];
+		DNvolume* vol = it->vol;
+		if (!vol || priv(vol)->batch != b) {
+			dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "DN_batch_run: item %u is not a member of the batch", i);
+			return false;
+		}
+		if (priv(vol)->batchStamp == run) {
+			dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "DN_batch_run: item %u repeats a volume of this run", i);
+			return false;
+		}
+		priv(vol)->batchStamp = run;
+		const DNimage* out = it->output;
+		if ((it->phases & DN_PHASE_DRAW) && (!out || !out->color || out->width == 0 || out->height == 0)) {
+			dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_ERROR, "DN_batch_run: item %u has an invalid output image", i);
+			return false;
+		}
+	}
+	/* host halves in item order: draw parameters, chunk staging (issued now on the batch's stream; the
+	 * staged records are published by the sync pass, after the draw), lighting parameters */
+	for (unsigned int i = 0; i < count; i++) {
+		const DNbatchItem* it = &items[i];
+		DNvolume* vol = it->vol;
+		dn_batch_item* d = &b->items[i];
+		memset(d, 0, sizeof(*d));
+		d->map = vol->gpu;
+		d->phases = it->phases & (DN_PHASE_DRAW | DN_PHASE_SYNC | DN_PHASE_LIGHT);
+		d->materials = (const dn_material*)vol->materials;
+		if (it->phases & DN_PHASE_DRAW) {
+			const DNimage* out = it->output;
+			draw_prepare(vol, out, it->view, it->projection, &d->draw);
+			d->hostImage = out->onDevice ? 0u : 1u;
+			d->colorOut = out->color; d->hitOut = out->hitIndex; d->faceOut = out->hitFace;
+		}
+		if (it->phases & DN_PHASE_SYNC) {
+			DNvolumePriv* p = priv(vol);
+			uint32_t nops = 0, nrecs = 0;
+			uint64_t nvw = 0;
+			if (!sync_prepare(vol, it->op, it->lightingSplit, &d->sync, &nops, &nrecs, &nvw)) return false;
+			int rc = dn_cuda_sync_stage(vol->gpu, p->ops, nops, p->recs, nrecs, p->vwords, nvw / 2);
+			sync_done(vol);
+			if (rc != DN_CUDA_OK) {
+				dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "device sync failed: %s", dn_cuda_last_error());
+				return false;
+			}
+		}
+		if (it->phases & DN_PHASE_LIGHT) light_prepare(vol, it->numDiffuseSamples, it->maxDiffuseSamples, it->time, &d->light);
+	}
+	if (dn_cuda_batch_frame(b->gpu, b->items, count) != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_ERROR, "batched frame failed: %s", dn_cuda_last_error());
+		return false;
+	}
+	return true;
+}
+
+bool DN_batch_finish(DNbatch* b)
+{
+	if (!b) return false;
+	int rc = dn_cuda_batch_finish(b->gpu);
+	for (size_t i = 0; i < b->nmembers; i++)
+		b->members[i]->numLightingRequests = (size_t)dn_cuda_requests_of(b->members[i]->gpu);
+	if (rc != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_ERROR, "batched device work failed: %s", dn_cuda_last_error());
+		return false;
+	}
+	return true;
+}
+
+bool DN_batch_get_stats(DNbatch* b, DNstats* out)
+{
+	dn_stats s;
+	if (!b || !out || dn_cuda_batch_stats(b->gpu, 0, &s) != DN_CUDA_OK) return false;
+	out->rays = s.rays; out->primaryRays = s.primary; out->outerSteps = s.outerSteps;
+	out->chunksEntered = s.chunksEntered; out->innerSteps = s.innerSteps; out->hits = s.hits;
+	out->litVoxels = s.litVoxels;
+	return true;
+}
+
+void DN_batch_reset_stats(DNbatch* b) { if (b) dn_cuda_batch_reset_stats(b->gpu); }
+
+bool DN_batch_autotune(DNbatch* b)
+{
+	if (!b) return false;
+	if (dn_cuda_batch_autotune(b->gpu, NULL) != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_ERROR, "batch autotuning failed: %s", dn_cuda_last_error());
+		return false;
+	}
+	return true;
 }

@@ -243,3 +243,100 @@ class Volume:
 
     def camera(self, fx, fy, fz, pitch, yaw, fov=90.0):
         self.lib.dn_scene_camera(self.ptr, fx, fy, fz, pitch, yaw, fov)
+
+
+class Batch:
+    """A DNbatch: frames of many volumes as batched kernels (DN_batch_*)."""
+
+    def __init__(self, volumes=()):
+        self.lib = L.load()
+        self.ptr = self.lib.DN_batch_create()
+        if not self.ptr:
+            raise RuntimeError("DN_batch_create failed: %s" % self.lib.dn_cuda_last_error().decode())
+        self.members = []
+        for v in volumes:
+            self.add(v)
+
+    def add(self, vol):
+        if not self.lib.DN_batch_add(self.ptr, vol.ptr):
+            raise RuntimeError("DN_batch_add failed: %s" % self.lib.dn_cuda_last_error().decode())
+        self.members.append(vol)
+
+    def remove(self, vol):
+        if not self.lib.DN_batch_remove(self.ptr, vol.ptr):
+            raise RuntimeError("DN_batch_remove failed")
+        self.members.remove(vol)
+
+    def close(self):
+        if self.ptr:
+            self.lib.DN_batch_destroy(self.ptr)
+            self.ptr = None
+            self.members = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def item(vol, image=None, view=None, proj=None, sync=None, light=None):
+        """One DNbatchItem: draw into image with (view, proj); sync=(op, split); light=(numDiffuse, maxDiffuse, time)."""
+        it = L.DNbatchItem()
+        it.vol = vol.ptr
+        ph = 0
+        if image is not None:
+            ph |= L.PHASE_DRAW
+            it.output = image.ptr
+            it.view, it.projection = view, proj
+        if sync is not None:
+            ph |= L.PHASE_SYNC
+            it.op, it.lightingSplit = sync
+        if light is not None:
+            ph |= L.PHASE_LIGHT
+            it.numDiffuseSamples, it.maxDiffuseSamples, it.time = light
+        it.phases = ph
+        return it
+
+    def run(self, items):
+        arr = (L.DNbatchItem * len(items))(*items)
+        if not self.lib.DN_batch_run(self.ptr, arr, len(items)):
+            raise RuntimeError("DN_batch_run failed: %s" % self.lib.dn_cuda_last_error().decode())
+
+    def finish(self):
+        return bool(self.lib.DN_batch_finish(self.ptr))
+
+    def stats(self):
+        s = L.DNstats()
+        if not self.lib.DN_batch_get_stats(self.ptr, byref(s)):
+            raise RuntimeError("DN_batch_get_stats failed: %s" % self.lib.dn_cuda_last_error().decode())
+        return {k: int(getattr(s, k)) for k, _ in L.DNstats._fields_}
+
+    def reset_stats(self):
+        self.lib.DN_batch_reset_stats(self.ptr)
+
+    def autotune(self):
+        if not self.lib.DN_batch_autotune(self.ptr):
+            raise RuntimeError("DN_batch_autotune failed: %s" % self.lib.dn_cuda_last_error().decode())
+        return self.tuning()
+
+    def _gpu(self):
+        # struct DNbatch starts with its struct DNgpuBatch pointer
+        return ctypes.cast(self.ptr, POINTER(c_void_p))[0]
+
+    def tuning(self):
+        t = L.DnBatchTuning()
+        if self.lib.dn_cuda_batch_get_tuning(self._gpu(), byref(t)) != 0:
+            raise RuntimeError("dn_cuda_batch_get_tuning failed")
+        return {"streamBatch": t.streamBatch, "blocksPerSM": t.blocksPerSM, "useGraph": t.useGraph}
+
+    def set_tuning(self, streamBatch=None, blocksPerSM=None, useGraph=None):
+        cur = self.tuning()
+        t = L.DnBatchTuning(streamBatch if streamBatch is not None else cur["streamBatch"],
+                            blocksPerSM if blocksPerSM is not None else cur["blocksPerSM"],
+                            useGraph if useGraph is not None else cur["useGraph"])
+        if self.lib.dn_cuda_batch_set_tuning(self._gpu(), byref(t)) != 0:
+            raise RuntimeError("dn_cuda_batch_set_tuning failed: %s" % self.lib.dn_cuda_last_error().decode())
+
+    def stream(self):
+        return self.lib.dn_cuda_batch_stream(self._gpu())

@@ -262,6 +262,44 @@ uint32_t dn_pack_chunk(const DNvolume* vol, const DNchunk* chunk, uint32_t mask[
 /* Struct sizes and field offsets for language bindings; returns the number of entries. */
 size_t DN_abi_layout(uint64_t* out, size_t n);
 
+/* Batches: the frame work of many volumes run as kernels that each cover every volume (one draw launch
+ * over all images, one sync launch over all maps, one persistent lighting launch over every map's
+ * lighting requests), replayed as a CUDA graph while the frame's composition repeats.  Each volume's
+ * results are exactly those of calling DN_draw, DN_sync_gpu and DN_update_lighting on it in that order
+ * with the same arguments.  A volume added to a batch runs all its device work on the batch's stream. */
+typedef struct DNbatch DNbatch;
+
+#define DN_PHASE_DRAW  0x1u
+#define DN_PHASE_SYNC  0x2u
+#define DN_PHASE_LIGHT 0x4u
+
+typedef struct DNbatchItem
+{
+	DNvolume* vol;
+	unsigned int phases;                 /* DN_PHASE_*: run in the order draw, sync, lighting */
+	DNimage* output;                     /* draw: as DN_draw */
+	DNmat4 view, projection;
+	DNmemOp op;                          /* sync: as DN_sync_gpu */
+	int lightingSplit;
+	int numDiffuseSamples, maxDiffuseSamples;   /* lighting: as DN_update_lighting */
+	float time;
+} DNbatchItem;
+
+DNbatch* DN_batch_create(void);
+void DN_batch_destroy(DNbatch* batch);
+bool DN_batch_add(DNbatch* batch, DNvolume* vol);
+bool DN_batch_remove(DNbatch* batch, DNvolume* vol);
+/* one frame over the items (each volume at most once, every volume a member) */
+bool DN_batch_run(DNbatch* batch, const DNbatchItem* items, unsigned int count);
+/* waits for the batch's work; refreshes every member's numLightingRequests */
+bool DN_batch_finish(DNbatch* batch);
+/* counters of the batch's launches since the last reset */
+bool DN_batch_get_stats(DNbatch* batch, DNstats* out);
+void DN_batch_reset_stats(DNbatch* batch);
+/* picks the batched lighting launch's stream batch and blocks per SM by timing the last frame's
+ * lighting under each candidate; results are unaffected */
+bool DN_batch_autotune(DNbatch* batch);
+
 #ifdef __cplusplus
 }
 #endif

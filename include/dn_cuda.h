@@ -138,6 +138,67 @@ int dn_cuda_draw(struct DNgpuVolume* g, const dn_draw_params* p, const dn_materi
 int dn_cuda_draw_host(struct DNgpuVolume* g, const dn_draw_params* p, const dn_material* materials,
                       float* colorOut, uint32_t* hitOut, uint8_t* faceOut);
 
+/* The staging half of dn_cuda_sync: uploads and publishes the ops, records and voxels without the
+ * per-tile pass (for maps whose per-tile pass runs in a batched frame, DN_BATCH_SYNC). */
+int dn_cuda_sync_stage(struct DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops,
+                       const dn_chunk_record* records, uint32_t nrecords,
+                       const uint32_t* voxelWords, uint64_t nvoxels);
+
+/* --- batches (no counterpart in the reference, which issues one GL dispatch sequence per volume) ---
+ * A batch runs the frame work of many maps as kernels that each cover every map of the frame: one draw
+ * launch over all maps' pixels, one launch of the per-tile sync pass over all maps' tiles, one persistent
+ * lighting launch over a device-side queue of every map's lighting requests, one commit launch.  Each map's
+ * results are exactly those of the single-map calls (dn_cuda_draw, dn_cuda_sync, dn_cuda_light) with the
+ * same arguments.  Member volumes run all their work on the batch's stream.  A frame whose composition
+ * repeats (same maps, phases, images and device arrays) is replayed as one CUDA graph. */
+struct DNgpuBatch;
+
+#define DN_BATCH_DRAW  0x1u   /* dn_cuda_draw / dn_cuda_draw_host with 'draw' */
+#define DN_BATCH_SYNC  0x2u   /* the per-tile pass of dn_cuda_sync with 'sync' (ops staged before) */
+#define DN_BATCH_LIGHT 0x4u   /* dn_cuda_light with 'light' */
+
+typedef struct dn_batch_item {
+    struct DNgpuVolume* map;
+    uint32_t phases;            /* DN_BATCH_*; phases run in the order draw, sync, light */
+    uint32_t hostImage;         /* 1: colorOut / hitOut / faceOut are host memory (valid after finish) */
+    const dn_material* materials;   /* 256 entries */
+    dn_draw_params draw;
+    float* colorOut;            /* width * height * 4 floats */
+    uint32_t* hitOut;           /* optional */
+    uint8_t* faceOut;           /* optional */
+    dn_sync_params sync;
+    dn_light_params light;
+} dn_batch_item;
+
+/* knobs of the batched lighting launch, chosen by dn_cuda_batch_autotune */
+typedef struct dn_batch_tuning {
+    uint32_t streamBatch;       /* lanes of a warp that wait before per-segment work runs, 1..32 */
+    uint32_t blocksPerSM;       /* resident lighting blocks per SM, 1..4 */
+    uint32_t useGraph;          /* replay repeated frames as a CUDA graph */
+} dn_batch_tuning;
+
+int dn_cuda_batch_create(struct DNgpuBatch** out);
+/* removes every member (their work returns to their own streams) and frees the batch */
+void dn_cuda_batch_destroy(struct DNgpuBatch* b);
+int dn_cuda_batch_add(struct DNgpuBatch* b, struct DNgpuVolume* g);
+int dn_cuda_batch_remove(struct DNgpuBatch* b, struct DNgpuVolume* g);
+/* one frame: every item's phases; each map at most once; every map a member of b */
+int dn_cuda_batch_frame(struct DNgpuBatch* b, const dn_batch_item* items, uint32_t n);
+/* waits for the batch's work; reports kernel error flags of every member */
+int dn_cuda_batch_finish(struct DNgpuBatch* b);
+/* counters of batched launches (kind 0 all, 1 draw, 2 lighting); single-map calls count on their map */
+int dn_cuda_batch_stats(struct DNgpuBatch* b, int kind, dn_stats* out);
+int dn_cuda_batch_reset_stats(struct DNgpuBatch* b);
+void* dn_cuda_batch_stream(struct DNgpuBatch* b);
+int dn_cuda_batch_get_tuning(struct DNgpuBatch* b, dn_batch_tuning* out);
+int dn_cuda_batch_set_tuning(struct DNgpuBatch* b, const dn_batch_tuning* t);
+/* Times the lighting launch of the last batched frame under each candidate tuning (re-running it leaves
+ * every map's state as it was: it writes only scratch and idempotent flags), keeps the fastest and
+ * returns it in chosen (may be NULL).  Call after a frame with DN_BATCH_LIGHT items. */
+int dn_cuda_batch_autotune(struct DNgpuBatch* b, dn_batch_tuning* chosen);
+/* request groups of the map's last sync, as read by its last dn_cuda_finish or dn_cuda_batch_finish */
+uint64_t dn_cuda_requests_of(struct DNgpuVolume* g);
+
 /* --- synchronisation, counters, introspection (additions) --- */
 int dn_cuda_finish(struct DNgpuVolume* g, uint64_t* numRequests);
 int dn_cuda_stats(struct DNgpuVolume* g, dn_stats* out);
