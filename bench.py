@@ -483,6 +483,277 @@ def run_batched(args):
         print(json.dumps(result), flush=True)
 
 
+# ------------------------------------------------------------ streaming-edits workload
+
+def catmull_rom(p, t):
+    """Point at t in [0, 1] on the uniform Catmull-Rom spline through the rows of p (end points repeated)."""
+    n = len(p) - 1
+    x = min(max(t, 0.0), 1.0) * n
+    i = min(int(x), n - 1)
+    u = x - i
+    p0, p1, p2, p3 = p[max(i - 1, 0)], p[i], p[i + 1], p[min(i + 2, n)]
+    return 0.5 * ((2.0 * p1) + (-p0 + p2) * u + (2.0 * p0 - 5.0 * p1 + 4.0 * p2 - p3) * u * u
+                  + (-p0 + 3.0 * p1 - 3.0 * p2 + p3) * u * u * u)
+
+
+def run_streaming(args):
+    """One large map edited every frame: 1-512 chunks re-rolled, the camera on a seeded Catmull-Rom spline,
+    and only edited, visible chunks relit (lighting split larger than any frame count, so the split
+    filter never selects an unedited chunk)."""
+    import ctypes
+    rank, world, local, pg = dist_setup()
+    import doonengine_gb300 as dn
+    from doonengine_gb300 import configs
+    lib = dn.load()
+    if lib.dn_cuda_init(local) != 0:
+        raise RuntimeError("dn_cuda_init(%d): %s" % (local, lib.dn_cuda_last_error().decode()))
+    dn.init()
+    t0 = time.perf_counter()
+    seed = 31 + 1000 * rank
+    vol, cfg = configs.build_volume("small", map=(128, 32, 128), seed=seed, mean=0.1, amp=0.05, shapes=0,
+                                    res=(1280, 720), K=16, cam=(0.1, 0.8, 0.1, 25.0, 45.0))
+    vol.s.mapId = rank
+    build_s = time.perf_counter() - t0
+    W, H = cfg["res"]
+    sx, sy, sz = cfg["map"]
+    flags = np.array([vol.s.map[t].flag for t in range(vol.num_tiles)], np.uint8)
+    occ = np.nonzero(flags)[0]
+    chunk_pos = np.stack([occ % sx, (occ // sx) % sy, occ // (sx * sy)], 1).astype(np.int32)
+    nonempty = len(occ) / vol.num_tiles
+    rng = np.random.default_rng(seed)
+    ctrl = np.stack([rng.uniform(0.05, 0.95, 8) * sx, rng.uniform(0.6, 0.9, 8) * sy, rng.uniform(0.05, 0.95, 8) * sz], 1)
+    total = args.warmup + args.steps
+    split = 1 << 30
+    img = dn.Image(W, H, on_device=True)
+    stream = vol.stream()
+    edits_per_frame = rng.integers(1, 513, size=total)
+    frame = [0]
+
+    def edit_and_camera(f):
+        t = f / max(1, total - 1)
+        p = catmull_rom(ctrl, t)
+        q = catmull_rom(ctrl, min(1.0, t + 1e-3))
+        d = q - p
+        vol.s.camPos.x, vol.s.camPos.y, vol.s.camPos.z = float(p[0]), float(p[1]), float(p[2])
+        vol.s.camOrient.x = 25.0
+        vol.s.camOrient.y = float(np.degrees(np.arctan2(d[0], d[2])))
+        n = int(edits_per_frame[f])
+        sel = np.ascontiguousarray(chunk_pos[rng.integers(len(chunk_pos), size=n)])
+        h0 = time.perf_counter()
+        lib.dn_scene_reroll(vol.ptr, sel.ctypes.data, n, seed * 7919 + f, 14)
+        return n, time.perf_counter() - h0
+
+    def gpu_frame(f):
+        v, p = vol.view_proj(H / W)
+        vol.draw(img, v, p)
+        vol.sync(dn.DN_READ_WRITE, split)
+        vol.update_lighting(1, 1000, 1.0 + 0.25 * f)
+
+    for f in range(args.warmup):
+        edit_and_camera(f)
+        gpu_frame(f)
+    assert vol.finish(), lib.dn_cuda_last_error().decode()
+    K = args.steps
+    evs = []
+    for _ in range(2 * K):
+        e = ctypes.c_void_p()
+        lib.dn_cuda_event_create(e)
+        evs.append(e)
+    vol.reset_stats()
+    launches0 = lib.dn_cuda_launch_count()
+    clocks = ClockSampler(local)
+    barrier(pg)
+    lib.dn_cuda_device_sync()
+    clocks.start()
+    t0 = time.perf_counter()
+    host_edit_s, edited = 0.0, 0
+    for k in range(K):
+        f = args.warmup + k
+        n, hs = edit_and_camera(f)
+        host_edit_s += hs
+        edited += n
+        lib.dn_cuda_flush_l2(stream, L2_FLUSH_BYTES)
+        lib.dn_cuda_event_record(evs[2 * k], stream)
+        gpu_frame(f)
+        lib.dn_cuda_event_record(evs[2 * k + 1], stream)
+    assert vol.finish(), lib.dn_cuda_last_error().decode()
+    lib.dn_cuda_device_sync()
+    barrier(pg)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches = lib.dn_cuda_launch_count() - launches0 - K
+    ms = ctypes.c_float()
+    dev_ms = 0.0
+    for k in range(K):
+        lib.dn_cuda_event_elapsed_ms(evs[2 * k], evs[2 * k + 1], ms)
+        dev_ms += ms.value
+    st = vol.stats()
+    dev_ms_max = allreduce_max(pg, dev_ms)
+    rays = allreduce_sum(pg, st["rays"])
+    result = {
+        "metric": METRIC + " (streaming edits)", "value": rays / (dev_ms_max / 1e3), "unit": "rays/s",
+        "n_gpus": world, "steps": K, "warmup": args.warmup, "ms_per_step": dev_ms_max / K,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded heightfield; seeded chunk re-rolls)",
+        "config": {"workload": "streaming edits: %dx%dx%d chunks (~%.0f%% non-empty), %dx%d draw, camera on a "
+                               "seeded Catmull-Rom spline, 1-512 chunks re-rolled per frame, only edited and "
+                               "visible chunks relit, K=16" % (sx, sy, sz, 100 * nonempty, W, H),
+                   "map_chunks": [sx, sy, sz], "nonempty_chunk_frac": round(nonempty, 4), "frames": total,
+                   "l2": "flushed between timed steps (256 MiB write, outside the timed events)",
+                   "parallelism": "replicas: one map per GPU, no collective"},
+        "lit_voxels_per_s": allreduce_sum(pg, st["litVoxels"]) / (dev_ms_max / 1e3),
+        "primary_rays_per_s": allreduce_sum(pg, st["primaryRays"]) / (dev_ms_max / 1e3),
+        "chunks_edited_per_step": edited / K, "host_edit_ms_per_step": host_edit_s * 1e3 / K,
+        "wall_ms_per_step": wall * 1e3 / K, "build_s": build_s,
+        "gpu_launches": int(allreduce_sum(pg, launches)), "clocks": clk,
+    }
+    img.close()
+    vol.close()
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+
+
+# ------------------------------------------------------------ serving workload
+
+def run_serving(args):
+    """Poisson request streams over many resident maps through the serving loop (serve.h), swept over
+    arrival rates: 70% draws, 25% relights of the visible chunks, 5% edit batches of 1-256 chunks."""
+    import ctypes
+    rank, world, local, pg = dist_setup()
+    import doonengine_gb300 as dn
+    from doonengine_gb300 import configs, _lib as L
+    lib = dn.load()
+    if lib.dn_cuda_init(local) != 0:
+        raise RuntimeError("dn_cuda_init(%d): %s" % (local, lib.dn_cuda_last_error().decode()))
+    dn.init()
+    specs = configs.serving_specs(args.maps, seed=11 + 1000 * rank)
+    vols, views = [], []
+    t0 = time.perf_counter()
+    tiles = 0
+    for i, sp in enumerate(specs):
+        vol, cfg = configs.build_volume("small", **sp)
+        vol.s.mapId = i
+        vols.append(vol)
+        tiles += vol.num_tiles
+    build_s = time.perf_counter() - t0
+    log("built %d maps in %.1f s (%d tiles)" % (len(vols), build_s, tiles))
+    budget = int(args.budget_gb * (1 << 30))
+    server = dn.Server(vols, budget_bytes=budget)
+    # draw targets: a ring of device images per resolution (the bench does not read them back)
+    ring = {r: [dn.Image(r[0], r[1], on_device=True, hit_info=True) for _ in range(args.image_ring)]
+            for r in configs.RESOLUTIONS}
+    ring_pos = {r: 0 for r in ring}
+    vp = {}
+    for i, vol in enumerate(vols):
+        for r in ring:
+            vp[(i, r)] = vol.view_proj(r[1] / r[0])
+    rng = np.random.default_rng(1234 + rank)
+
+    def make_requests(rate, seconds):
+        n = int(rng.poisson(rate * seconds))
+        offs = np.sort(rng.uniform(0.0, seconds, size=n))
+        kinds = rng.choice(3, size=n, p=[0.70, 0.25, 0.05])
+        which = rng.integers(len(vols), size=n)
+        reqs = []
+        for k, vi in zip(kinds, which):
+            vi = int(vi)
+            if k == 0:
+                r = configs.RESOLUTIONS[int(rng.integers(len(configs.RESOLUTIONS)))]
+                img = ring[r][ring_pos[r]]
+                ring_pos[r] = (ring_pos[r] + 1) % len(ring[r])
+                v, p = vp[(vi, r)]
+                reqs.append(server.draw_request(vi, img, v, p, user=1))
+            elif k == 1:
+                reqs.append(server.relight_request(vi, 1, 1000, float(rng.uniform(0.0, 100.0)), user=2))
+            else:
+                sx, sy, sz = specs[vi]["map"]
+                nch = int(rng.integers(1, 257))
+                edits = []
+                for _ in range(nch):
+                    mp = (int(rng.integers(sx)), int(rng.integers(sy)), int(rng.integers(sz)))
+                    for _ in range(4):
+                        cp = tuple(int(c) for c in rng.integers(8, size=3))
+                        edits.append((mp, cp, int(rng.integers(16)), (0.0, 1.0, 0.0),
+                                      tuple(int(c) for c in rng.integers(40, 240, size=3)), False))
+                reqs.append(server.edit_request(vi, edits, user=3))
+        return reqs, offs
+
+    server.start()
+    # warm-up: every map drawn once and relit once
+    warm = []
+    for vi in range(len(vols)):
+        r = specs[vi]["res"]
+        v, p = vp[(vi, r)]
+        warm.append(server.draw_request(vi, ring[r][0], v, p))
+        warm.append(server.relight_request(vi, 1, 1000, 0.5))
+    for q in warm:
+        server.submit(q)
+    assert server.drain(1800.0), "warm-up did not drain"
+    server.poll()
+    sweep = []
+    rates = [float(x) for x in args.rates.split(",")]
+    lib.DN_batch_reset_stats(lib.DN_server_batch(server.ptr))
+    tot_rays, tot_s = 0, 0.0
+    for rate in rates:
+        reqs, offs = make_requests(rate, args.seconds)
+        st0 = server.stats()
+        b0 = server.batch_stats()
+        t0 = time.perf_counter()
+        server.replay(reqs, offs)
+        ok = server.drain(args.drain_timeout)
+        el = time.perf_counter() - t0
+        comps = server.poll()
+        b1 = server.batch_stats()
+        st1 = server.stats()
+        lat = np.array([c["finished"] - c["arrival"] for c in comps]) * 1e3
+        by_kind = {}
+        for name, kind in (("draw", 0), ("relight", 1), ("edit", 2)):
+            lk = np.array([c["finished"] - c["arrival"] for c in comps if c["kind"] == kind]) * 1e3
+            if len(lk):
+                by_kind[name] = {"n": int(len(lk)), "p50_ms": float(np.percentile(lk, 50)),
+                                 "p99_ms": float(np.percentile(lk, 99))}
+        rays = b1["rays"] - b0["rays"]
+        tot_rays += rays
+        tot_s += el
+        row = {"offered_rps": rate, "requests": len(reqs), "completed": len(comps), "drained": bool(ok),
+               "achieved_rps": len(comps) / el if el else None, "wall_s": el,
+               "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+               "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+               "rays_per_s": rays / el if el else None, "by_kind": by_kind,
+               "ticks": st1["ticks"] - st0["ticks"], "items": st1["items"] - st0["items"],
+               "evictions": st1["evictions"] - st0["evictions"], "restores": st1["restores"] - st0["restores"]}
+        log("rate %g: %s" % (rate, {k: row[k] for k in ("completed", "achieved_rps", "p50_ms", "p99_ms", "rays_per_s")}))
+        sweep.append(row)
+        if not ok:
+            break
+    st = server.stats()
+    good = [r for r in sweep if r["p99_ms"] is not None and r["p99_ms"] <= 33.0 and r["drained"]]
+    best = max(good, key=lambda r: r["achieved_rps"]) if good else None
+    result = {
+        "metric": METRIC + " (served)", "value": tot_rays / tot_s if tot_s else 0.0, "unit": "rays/s",
+        "n_gpus": world, "steps": len(sweep), "warmup": 1, "ms_per_step": tot_s * 1e3 / max(1, len(sweep)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded heightfields; Poisson arrivals)",
+        "config": {"workload": "serving: %d resident maps, chunk dims log-uniform 8^3..96x32x96, requests 70%% draw "
+                               "(320x180..1920x1080) / 25%% relight / 5%% edit batches of 1-256 chunks, Poisson "
+                               "arrivals swept over %s req/s, %.0f s each" % (len(vols), args.rates, args.seconds),
+                   "maps": len(vols), "tiles": tiles, "device_budget_gb": args.budget_gb,
+                   "parallelism": "replicas: own maps per GPU, no collective"},
+        "sweep": sweep,
+        "max_rps_with_p99_le_33ms": best["achieved_rps"] if best else None,
+        "resident_bytes": st["residentBytes"], "resident_maps": st["residentVolumes"],
+        "evictions": st["evictions"], "restores": st["restores"], "build_s": build_s,
+    }
+    server.close()
+    for imgs in ring.values():
+        for im in imgs:
+            im.close()
+    for v in vols:
+        v.close()
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+
+
 # ------------------------------------------------------------ reference arm
 
 def run_reference(args):
@@ -562,10 +833,15 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-pixels", type=int, default=0, help="pixels per reference step (0 = the full image)")
     ap.add_argument("--ref-requests", type=int, default=2048, help="lighting request groups per reference step")
-    ap.add_argument("--workload", default="plain", choices=["plain", "batched"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "serving", "streaming"],
                     help="plain: one map per step (the headline); batched: many maps per step")
     ap.add_argument("--maps", type=int, default=64, help="maps of the batched workload")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--rates", default="500,1000,2000,5000,10000,20000", help="serving: offered req/s")
+    ap.add_argument("--seconds", type=float, default=4.0, help="serving: seconds of arrivals per rate")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device budget")
+    ap.add_argument("--image-ring", type=int, default=16, help="serving: draw targets per resolution")
+    ap.add_argument("--drain-timeout", type=float, default=120.0)
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3 (at least three untimed steps)")
@@ -574,6 +850,12 @@ def main():
         run_reference(args)
     elif args.workload == "batched":
         run_batched(args)
+    elif args.workload == "streaming":
+        run_streaming(args)
+    elif args.workload == "serving":
+        if args.maps == 64:
+            args.maps = 256
+        run_serving(args)
     else:
         run_ours(args)
 

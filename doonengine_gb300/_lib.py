@@ -3,7 +3,7 @@
 library's own ``DN_abi_layout``."""
 import ctypes
 import os
-from ctypes import (POINTER, Structure, c_bool, c_char_p, c_float, c_int, c_size_t, c_uint8, c_uint32,
+from ctypes import (POINTER, Structure, c_bool, c_char_p, c_double, c_float, c_int, c_size_t, c_uint8, c_uint32,
                     c_uint64, c_void_p, c_int32)
 
 from . import build as _build
@@ -108,9 +108,40 @@ class DNbatchItem(Structure):
                 ("maxDiffuseSamples", c_int), ("time", c_float)]
 
 
+REQUEST_DRAW, REQUEST_RELIGHT, REQUEST_EDIT = 0, 1, 2
+
+
+class DNvoxelEdit(Structure):
+    """DNvoxelEdit of include/DoonEngine/serve.h"""
+    _fields_ = [("mapPos", DNivec3), ("chunkPos", DNivec3), ("voxel", DNvoxel), ("remove", c_int)]
+
+
+class DNrequest(Structure):
+    """DNrequest of include/DoonEngine/serve.h"""
+    _fields_ = [("kind", c_int), ("volume", c_uint32), ("output", POINTER(DNimage)), ("view", DNmat4),
+                ("projection", DNmat4), ("numDiffuseSamples", c_int), ("maxDiffuseSamples", c_int), ("time", c_float),
+                ("edits", POINTER(DNvoxelEdit)), ("numEdits", c_uint32), ("user", c_void_p)]
+
+
+class DNcompletion(Structure):
+    """DNcompletion of include/DoonEngine/serve.h"""
+    _fields_ = [("id", c_uint64), ("user", c_void_p), ("kind", c_int), ("volume", c_uint32), ("arrival", c_double),
+                ("admitted", c_double), ("finished", c_double), ("ok", c_int)]
+
+
+class DNserveConfig(Structure):
+    _fields_ = [("deviceBudgetBytes", c_uint64), ("maxVolumesPerTick", c_uint32), ("maxTicksInFlight", c_uint32)]
+
+
+class DNserveStats(Structure):
+    _fields_ = [("submitted", c_uint64), ("completed", c_uint64), ("failed", c_uint64), ("ticks", c_uint64),
+                ("items", c_uint64), ("evictions", c_uint64), ("restores", c_uint64), ("residentBytes", c_uint64),
+                ("residentVolumes", c_uint32)]
+
+
 class DnBatchTuning(Structure):
     """dn_batch_tuning of include/dn_cuda.h"""
-    _fields_ = [("streamBatch", c_uint32), ("blocksPerSM", c_uint32), ("useGraph", c_uint32)]
+    _fields_ = [("streamBatch", c_uint32), ("blocksPerSM", c_uint32), ("useGraph", c_uint32), ("kernel", c_uint32)]
 
 # (name, restype, argtypes)
 _SIGS = [
@@ -170,11 +201,24 @@ _SIGS = [
     ("DN_batch_get_stats", c_bool, [c_void_p, POINTER(DNstats)]),
     ("DN_batch_reset_stats", None, [c_void_p]),
     ("DN_batch_autotune", c_bool, [c_void_p]),
+    ("DN_batch_stream", c_void_p, [c_void_p]),
+    ("DN_server_create", c_void_p, [POINTER(DNserveConfig)]),
+    ("DN_server_destroy", None, [c_void_p]),
+    ("DN_server_add_volume", c_int, [c_void_p, VOLP]),
+    ("DN_server_start", c_bool, [c_void_p]),
+    ("DN_server_submit", c_uint64, [c_void_p, POINTER(DNrequest)]),
+    ("DN_server_replay", c_size_t, [c_void_p, POINTER(DNrequest), POINTER(c_double), c_size_t]),
+    ("DN_server_drain", c_bool, [c_void_p, c_double]),
+    ("DN_server_poll", c_size_t, [c_void_p, POINTER(DNcompletion), c_size_t]),
+    ("DN_server_get_stats", None, [c_void_p, POINTER(DNserveStats)]),
+    ("DN_server_batch", c_void_p, [c_void_p]),
+    ("DN_server_clock", c_double, []),
     ("dn_pack_chunk", c_uint32, [VOLP, POINTER(DNchunk), c_void_p, c_void_p, c_void_p]),
     ("dn_scene_palette", None, [VOLP, c_uint32, c_uint32, c_uint32, c_float, c_float, c_float]),
     ("dn_scene_terrain", None, [VOLP, c_uint32, c_float, c_float, c_uint32, c_uint32]),
     ("dn_scene_shapes", None, [VOLP, c_uint32, c_uint32, c_int32, c_int32, c_uint32, c_float, c_float]),
     ("dn_scene_camera", None, [VOLP, c_float, c_float, c_float, c_float, c_float, c_float]),
+    ("dn_scene_reroll", None, [VOLP, c_void_p, c_uint32, c_uint32, c_uint32]),
     # C ABI
     ("dn_cuda_init", c_int, [c_int]),
     ("dn_cuda_shutdown", None, []),
@@ -224,6 +268,11 @@ _SIGS = [
     ("dn_cuda_batch_set_tuning", c_int, [c_void_p, POINTER(DnBatchTuning)]),
     ("dn_cuda_batch_autotune", c_int, [c_void_p, POINTER(DnBatchTuning)]),
     ("dn_cuda_requests_of", c_uint64, [c_void_p]),
+    ("dn_cuda_map_footprint", c_uint64, [c_void_p]),
+    ("dn_cuda_map_is_resident", c_int, [c_void_p]),
+    ("dn_cuda_map_evict", c_int, [c_void_p]),
+    ("dn_cuda_map_restore", c_int, [c_void_p]),
+    ("dn_cuda_event_query", c_int, [c_void_p]),
     ("dn_cuda_kernel_names", c_char_p, []),
     ("dn_cuda_launch_count", c_uint64, []),
 ]
@@ -268,5 +317,7 @@ def check_layout(lib=None):
             DNvolume.frameNum.offset, DNvolume.emissiveStrength.offset, DNvolume.deviceBudgetBytes.offset,
             ctypes.sizeof(DNchunk), ctypes.sizeof(DNmaterial), ctypes.sizeof(DNimage), ctypes.sizeof(DNchunkHandle),
             ctypes.sizeof(DNstats), DNchunk.voxels.offset, ctypes.sizeof(DNvoxel),
-            ctypes.sizeof(DNbatchItem), DNbatchItem.view.offset, DNbatchItem.op.offset, DNbatchItem.time.offset]
+            ctypes.sizeof(DNbatchItem), DNbatchItem.view.offset, DNbatchItem.op.offset, DNbatchItem.time.offset,
+            ctypes.sizeof(DNrequest), DNrequest.edits.offset, DNrequest.user.offset, ctypes.sizeof(DNcompletion),
+            ctypes.sizeof(DNvoxelEdit), ctypes.sizeof(DNserveStats)]
     return [(i, int(buf[i]), w) for i, w in enumerate(want[:n]) if int(buf[i]) != w]

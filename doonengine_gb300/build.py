@@ -27,10 +27,11 @@ C_FLAGS = ["-O2", "-fPIC", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", 
            "-Wno-unused-function", "-I" + INCLUDE]
 
 CU_SOURCES = ["dn_cuda.cu", "dn_batch.cu"]
-C_SOURCES = ["voxel.c", "dn_math.c", "dn_scenes.c", "voxvol.c"]
+C_SOURCES = ["voxel.c", "dn_math.c", "dn_scenes.c", "voxvol.c", "dn_serve.c"]
 HEADERS = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))) + [
     os.path.join(INCLUDE, "dn_cuda.h"), os.path.join(INCLUDE, "DoonEngine", "voxel.h"),
-    os.path.join(INCLUDE, "DoonEngine", "globals.h"), os.path.join(INCLUDE, "DoonEngine", "dn_math.h")]
+    os.path.join(INCLUDE, "DoonEngine", "globals.h"), os.path.join(INCLUDE, "DoonEngine", "dn_math.h"),
+    os.path.join(INCLUDE, "DoonEngine", "serve.h")]
 
 
 def _stale(target, deps):
@@ -69,7 +70,7 @@ def build(force=False, verbose=False):
             if verbose and out:
                 sys.stdout.write(out)
     if force or jobs or _stale(LIB, objs):
-        _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lm"])
+        _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lm", "-lpthread"])
     return LIB
 
 

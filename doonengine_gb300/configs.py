@@ -61,3 +61,19 @@ def batched_specs(n=64, seed=7, dim_lo=8, dim_hi=64, res=RESOLUTIONS):
         out.append(dict(map=dims, seed=int(seed * 1000 + i), mean=frac, amp=frac * 0.5, shapes=0,
                         res=tuple(r), K=16, cam=cam))
     return out
+
+
+def serving_specs(n=256, seed=11, lo=(8, 8, 8), hi=(96, 32, 96), res=RESOLUTIONS):
+    """The serving workload's maps: chunk dimensions log-uniform per axis between lo and hi (8^3 to
+    96x32x96 chunks), non-empty chunk fraction uniform in [0.05, 0.5], own seeded camera, K=16."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        dims = tuple(int(round(float(np.exp(rng.uniform(np.log(a), np.log(b)))))) for a, b in zip(lo, hi))
+        frac = float(rng.uniform(0.05, 0.5))
+        cam = (float(rng.uniform(0.05, 0.3)), float(rng.uniform(0.6, 0.9)), float(rng.uniform(0.05, 0.3)),
+               float(rng.uniform(20.0, 40.0)), float(rng.uniform(30.0, 60.0)))
+        out.append(dict(map=dims, seed=int(seed * 1000 + i), mean=frac, amp=frac * 0.5, shapes=0,
+                        res=tuple(res[int(rng.integers(len(res)))]), K=16, cam=cam))
+    return out

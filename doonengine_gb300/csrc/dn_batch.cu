@@ -20,6 +20,7 @@
 #include "dn_internal.cuh"
 #include "dn_light.cuh"
 #include "dn_light_stream.cuh"
+#include "dn_light_packet.cuh"
 #include <string.h>
 #include <stddef.h>
 #include <new>
@@ -47,14 +48,18 @@ struct DNgpuBatch {
     unsigned long long* lsave;  // lighting counters saved around autotuning (device)
     DevState** dsts; uint32_t dstsCap; bool stsDirty;
     uint32_t* dgather; uint32_t* hgather;
+    std::vector<DevState*> gatherHost;  // the pointer list last copied to dsts
+    uint32_t gatherCount;
     dn_batch_tuning tuning;
     int maxBlocksPerSM;
     std::vector<uint64_t> lastKey;
     std::vector<uint64_t> graphKey;
     cudaGraphExec_t graph;
-    // the lighting launch of the last frame (autotuning re-runs it)
+    // the lighting launch of the last frame (autotuning re-runs it) and the generations of its maps
     BatchLightArgs lastLight;
     bool lastLightValid;
+    bool lastPackets;
+    std::vector<std::pair<DNgpuVolume*, uint64_t>> lastLightGens;
 };
 
 // ------------------------------------------------------------------ kernels
@@ -147,6 +152,12 @@ __global__ void __launch_bounds__(128, DN_STREAM_MIN_BLOCKS) k_light_stream_batc
     stream_loop<true>(nullptr, &a, nullptr, jobs[threadIdx.x]);
 }
 
+__global__ void __launch_bounds__(128, DN_PACKET_MIN_BLOCKS) k_light_packet_batch(const __grid_constant__ BatchLightArgs a)
+{
+    __shared__ PacketWarp warps[4];
+    packet_loop<true>(nullptr, &a, nullptr, warps[threadIdx.x >> 5]);
+}
+
 __global__ void k_commit_batch(const BatchLightMap* l, const uint32_t* reqStart, uint32_t nl)
 {
     const uint64_t total = (uint64_t)reqStart[nl] * 32u;
@@ -187,7 +198,10 @@ extern "C" int dn_cuda_batch_create(DNgpuBatch** out)
     b->htab = b->dtab = nullptr; b->tabCap = 0; b->tabGen = 0;
     b->workCounter = nullptr; b->bst = nullptr; b->hbst = nullptr; b->lsave = nullptr;
     b->dsts = nullptr; b->dstsCap = 0; b->stsDirty = true; b->dgather = nullptr; b->hgather = nullptr;
+    b->gatherCount = 0;
     b->tuning.streamBatch = g_streamBatch; b->tuning.blocksPerSM = DN_STREAM_MIN_BLOCKS; b->tuning.useGraph = 1;
+    b->tuning.kernel = g_lightKernel == 2 ? 2u : 1u;
+    b->lastPackets = false;
     b->graph = nullptr;
     b->lastLightValid = false;
     int rc = DN_CUDA_OK;
@@ -209,9 +223,11 @@ extern "C" int dn_cuda_batch_create(DNgpuBatch** out)
         if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "memset: %s", cudaGetErrorString(e));
     }
     if (!rc) {
-        int perSM = 0;
+        int perSM = 0, perSM2 = 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_stream_batch, 128, 0);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM2, k_light_packet_batch, 128, 0);
         if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "occupancy: %s", cudaGetErrorString(e));
+        if (perSM2 < perSM) perSM = perSM2;
         b->maxBlocksPerSM = perSM < 1 ? 1 : perSM;
         if ((int)b->tuning.blocksPerSM > b->maxBlocksPerSM) b->tuning.blocksPerSM = (uint32_t)b->maxBlocksPerSM;
     }
@@ -303,12 +319,15 @@ struct FramePlan {
     TableLayout t;
     uint32_t drawBlocks, syncBlocks;
     bool hostImages;
+    bool packets;               // lighting as warp packets (dn_light_packet.cuh)
 };
 
-static int issue_light(DNgpuBatch* b, const BatchLightArgs& la, cudaStream_t s)
+// packets: the lighting kernel of dn_light_packet.cuh (every map's specBounceLimit within its limit)
+static int issue_light(DNgpuBatch* b, const BatchLightArgs& la, cudaStream_t s, bool packets)
 {
     COUNT_LAUNCH();
-    k_light_stream_batch<<<(unsigned)(g_numSMs * (int)b->tuning.blocksPerSM), 128, 0, s>>>(la);
+    if (packets) k_light_packet_batch<<<(unsigned)(g_numSMs * (int)b->tuning.blocksPerSM), 128, 0, s>>>(la);
+    else k_light_stream_batch<<<(unsigned)(g_numSMs * (int)b->tuning.blocksPerSM), 128, 0, s>>>(la);
     CK(cudaGetLastError());
     return DN_CUDA_OK;
 }
@@ -369,13 +388,16 @@ static int issue_frame(DNgpuBatch* b, const dn_batch_item* items, uint32_t n, co
         la.workCounter = b->workCounter;
         la.stats = b->bst->lstats;
         la.batch = b->tuning.streamBatch;
-        int rc = issue_light(b, la, s);
+        int rc = issue_light(b, la, s, f.packets);
         if (rc) return rc;
         COUNT_LAUNCH();
         k_commit_batch<<<(unsigned)(g_numSMs * 4), 256, 0, s>>>(la.maps, la.reqStart, t.nl);
         CK(cudaGetLastError());
         b->lastLight = la;
         b->lastLightValid = true;
+        b->lastLightGens.clear();
+        for (uint32_t i = 0; i < n; i++)
+            if (items[i].phases & DN_BATCH_LIGHT) b->lastLightGens.emplace_back(items[i].map, items[i].map->gen);
     }
     if (f.hostImages) CK(cudaStreamWaitEvent(s, b->copiesDone, 0));
     return DN_CUDA_OK;
@@ -395,6 +417,7 @@ extern "C" int dn_cuda_batch_frame(DNgpuBatch* b, const dn_batch_item* items, ui
         const dn_batch_item& it = items[i];
         DNgpuVolume* g = it.map;
         if (!g || g->batch != b) return dn_set_err(DN_CUDA_ERR_ARG, "item %u: the map is not a member of the batch", i);
+        if (g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "item %u: the map is evicted", i);
         if (!it.phases || (it.phases & ~(DN_BATCH_DRAW | DN_BATCH_SYNC | DN_BATCH_LIGHT)))
             return dn_set_err(DN_CUDA_ERR_ARG, "item %u: phases 0x%x", i, it.phases);
         seen.push_back(g);
@@ -428,6 +451,11 @@ extern "C" int dn_cuda_batch_frame(DNgpuBatch* b, const dn_batch_item* items, ui
     FramePlan f;
     f.t = layout(nm, nd, ns, nl);
     f.hostImages = hostImages;
+    uint32_t maxSpec = 0;
+    for (uint32_t i = 0; i < n; i++)
+        if ((items[i].phases & DN_BATCH_LIGHT) && items[i].light.specBounceLimit > maxSpec) maxSpec = items[i].light.specBounceLimit;
+    f.packets = b->tuning.kernel == 2u && maxSpec <= PK_MAX_SPEC_SEGMENTS;
+    b->lastPackets = f.packets;
     if (f.t.size > b->tabCap) {
         CK(cudaStreamSynchronize(b->stream));
         if (b->htab) cudaFreeHost(b->htab);
@@ -454,6 +482,7 @@ extern "C" int dn_cuda_batch_frame(DNgpuBatch* b, const dn_batch_item* items, ui
     std::vector<uint64_t> key;
     key.reserve(4 + (size_t)n * 10);
     key.push_back(n); key.push_back(b->tabGen); key.push_back(b->tuning.streamBatch); key.push_back(b->tuning.blocksPerSM);
+    key.push_back(b->tuning.kernel);
     for (uint32_t i = 0; i < n; i++) {
         const dn_batch_item& it = items[i];
         DNgpuVolume* g = it.map;
@@ -539,25 +568,33 @@ extern "C" int dn_cuda_batch_finish(DNgpuBatch* b)
 {
     if (!b) return dn_set_err(DN_CUDA_ERR_ARG, "null batch");
     CK(cudaSetDevice(b->device));
-    const uint32_t n = (uint32_t)b->members.size();
-    if (n && (b->stsDirty || n > b->dstsCap)) {
-        CK(cudaStreamSynchronize(b->stream));
-        if (n > b->dstsCap) {
-            dfree(b->dsts); dfree(b->dgather);
-            if (b->hgather) cudaFreeHost(b->hgather);
-            b->hgather = nullptr;
-            b->dstsCap = 0;
-            int rc;
-            if ((rc = dalloc(&b->dsts, n)) || (rc = dalloc(&b->dgather, (size_t)n * 4))) return rc;
-            CK(cudaMallocHost((void**)&b->hgather, (size_t)n * 16));
-            b->dstsCap = n;
-        }
-        std::vector<DevState*> sts(n);
-        for (uint32_t i = 0; i < n; i++) sts[i] = b->members[i]->st;
-        CK(cudaMemcpy(b->dsts, sts.data(), (size_t)n * sizeof(DevState*), cudaMemcpyHostToDevice));
-        b->stsDirty = false;
-    }
+    // the status blocks of the resident members only: an evicted map has none on the device, and a
+    // restored one has it at a new address, so the pointer list is rebuilt whenever it changed
+    std::vector<DNgpuVolume*> res;
+    std::vector<DevState*> sts;
+    for (DNgpuVolume* g : b->members)
+        if (!g->evicted && g->st) { res.push_back(g); sts.push_back(g->st); }
+    const uint32_t n = (uint32_t)res.size();
     if (n) {
+        bool changed = b->stsDirty || n != b->gatherCount;
+        if (!changed) changed = memcmp(b->gatherHost.data(), sts.data(), (size_t)n * sizeof(DevState*)) != 0;
+        if (changed) {
+            CK(cudaStreamSynchronize(b->stream));
+            if (n > b->dstsCap) {
+                dfree(b->dsts); dfree(b->dgather);
+                if (b->hgather) cudaFreeHost(b->hgather);
+                b->hgather = nullptr;
+                b->dstsCap = 0;
+                int rc;
+                if ((rc = dalloc(&b->dsts, n)) || (rc = dalloc(&b->dgather, (size_t)n * 4))) return rc;
+                CK(cudaMallocHost((void**)&b->hgather, (size_t)n * 16));
+                b->dstsCap = n;
+            }
+            CK(cudaMemcpy(b->dsts, sts.data(), (size_t)n * sizeof(DevState*), cudaMemcpyHostToDevice));
+            b->gatherHost = sts;
+            b->gatherCount = n;
+            b->stsDirty = false;
+        }
         COUNT_LAUNCH();
         k_batch_gather<<<(n + 255) / 256, 256, 0, b->stream>>>(b->dsts, n, b->dgather);
         CK(cudaGetLastError());
@@ -568,11 +605,11 @@ extern "C" int dn_cuda_batch_finish(DNgpuBatch* b)
     CK(cudaStreamSynchronize(b->side));
     uint32_t bad = 0, first = 0, flags = 0;
     for (uint32_t i = 0; i < n; i++) {
-        DNgpuVolume* g = b->members[i];
+        DNgpuVolume* g = res[i];
         memcpy(g->hst->w, &b->hgather[4 * i], sizeof(g->hst->w));
         if (g->hst->w[ST_ERR]) { if (!bad) { first = i; flags = g->hst->w[ST_ERR]; } bad++; }
     }
-    if (bad) return dn_set_err(DN_CUDA_ERR_KERNEL, "kernel error flags 0x%x on member %u (%u members flagged)", flags, first, bad);
+    if (bad) return dn_set_err(DN_CUDA_ERR_KERNEL, "kernel error flags 0x%x on resident member %u (%u members flagged)", flags, first, bad);
     return DN_CUDA_OK;
 }
 
@@ -609,6 +646,7 @@ extern "C" int dn_cuda_batch_set_tuning(DNgpuBatch* b, const dn_batch_tuning* t)
 {
     if (!b || !t) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (t->streamBatch < 1 || t->streamBatch > 32) return dn_set_err(DN_CUDA_ERR_ARG, "streamBatch %u", t->streamBatch);
+    if (t->kernel != 1u && t->kernel != 2u) return dn_set_err(DN_CUDA_ERR_ARG, "kernel %u (1 streams, 2 packets)", t->kernel);
     if (t->blocksPerSM < 1 || (int)t->blocksPerSM > b->maxBlocksPerSM)
         return dn_set_err(DN_CUDA_ERR_ARG, "blocksPerSM %u (1..%d)", t->blocksPerSM, b->maxBlocksPerSM);
     b->tuning = *t;
@@ -620,6 +658,10 @@ extern "C" int dn_cuda_batch_autotune(DNgpuBatch* b, dn_batch_tuning* chosen)
 {
     if (!b) return dn_set_err(DN_CUDA_ERR_ARG, "null batch");
     if (!b->lastLightValid) return dn_set_err(DN_CUDA_ERR_ARG, "no batched lighting launch to tune on");
+    // the launch re-run names the maps' device arrays as they were at that frame
+    for (const auto& mg : b->lastLightGens)
+        if (mg.first->batch != b || mg.first->evicted || mg.first->gen != mg.second)
+            return dn_set_err(DN_CUDA_ERR_ARG, "a map of the last batched frame changed since; run a frame before tuning");
     CK(cudaSetDevice(b->device));
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -628,31 +670,40 @@ extern "C" int dn_cuda_batch_autotune(DNgpuBatch* b, dn_batch_tuning* chosen)
     CK(cudaMemcpyAsync(b->lsave, b->bst->lstats, sizeof(b->bst->lstats), cudaMemcpyDeviceToDevice, b->stream));
     const dn_batch_tuning keep = b->tuning;
     dn_batch_tuning best = keep;
+    // packets were possible in the last frame only if every lit map's specBounceLimit allowed them
+    const bool packetsOk = b->lastPackets || keep.kernel != 2u;
     float bestMs = 3.4e38f;
-    const uint32_t batches[] = {16u, 20u, 24u, 28u, 32u};
     int rc = DN_CUDA_OK;
-    for (uint32_t bps = 2; bps <= (uint32_t)b->maxBlocksPerSM && bps <= 6 && !rc; bps++) {
-        for (uint32_t sb : batches) {
-            b->tuning.streamBatch = sb;
-            b->tuning.blocksPerSM = bps;
-            BatchLightArgs la = b->lastLight;
-            la.batch = sb;
-            float ms = 3.4e38f;
-            for (int rep = 0; rep < 2 && !rc; rep++) {
-                cudaError_t e = cudaMemsetAsync(b->workCounter, 0, 4, b->stream);
-                if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
-                if (e != cudaSuccess) { rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "autotune: %s", cudaGetErrorString(e)); break; }
-                rc = issue_light(b, la, b->stream);
-                if (rc) break;
-                e = cudaEventRecord(e1, b->stream);
-                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-                float t = 0.0f;
-                if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
-                if (e != cudaSuccess) { rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "autotune: %s", cudaGetErrorString(e)); break; }
-                if (t < ms) ms = t;
-            }
-            if (!rc && ms < bestMs) { bestMs = ms; best = b->tuning; }
+    // times the last frame's lighting launch under tuning t (best of two runs)
+    auto trial = [&](const dn_batch_tuning& t) -> float {
+        b->tuning = t;
+        BatchLightArgs la = b->lastLight;
+        la.batch = t.streamBatch;
+        float ms = 3.4e38f;
+        for (int rep = 0; rep < 2 && !rc; rep++) {
+            cudaError_t e = cudaMemsetAsync(b->workCounter, 0, 4, b->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+            if (e != cudaSuccess) { rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "autotune: %s", cudaGetErrorString(e)); break; }
+            rc = issue_light(b, la, b->stream, t.kernel == 2u && packetsOk);
+            if (rc) break;
+            e = cudaEventRecord(e1, b->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float t_ms = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t_ms, e0, e1);
+            if (e != cudaSuccess) { rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "autotune: %s", cudaGetErrorString(e)); break; }
+            if (t_ms < ms) ms = t_ms;
         }
+        if (!rc && ms < bestMs) { bestMs = ms; best = t; }
+        return ms;
+    };
+    // coordinate descent: kernel, stream batch (ray streams only), then resident blocks per SM
+    trial(keep);
+    { dn_batch_tuning t = best; t.kernel = 3u - t.kernel; if (!rc && (t.kernel == 1u || packetsOk)) trial(t); }
+    const uint32_t batches[] = {12u, 16u, 20u, 24u, 28u, 32u};
+    if (best.kernel == 1u)
+        for (uint32_t sb : batches) { dn_batch_tuning t = best; t.streamBatch = sb; if (!rc) trial(t); }
+    for (uint32_t bps = 2; bps <= (uint32_t)b->maxBlocksPerSM && bps <= 6; bps++) {
+        dn_batch_tuning t = best; t.blocksPerSM = bps; if (!rc) trial(t);
     }
     b->tuning = rc ? keep : best;
     b->tuning.useGraph = keep.useGraph;

@@ -14,6 +14,7 @@
 #include "dn_internal.cuh"
 #include "dn_light.cuh"
 #include "dn_light_stream.cuh"
+#include "dn_light_packet.cuh"
 #include <stdio.h>
 #include <string.h>
 #include <stdlib.h>
@@ -136,6 +137,7 @@ extern "C" void dn_cuda_map_destroy(DNgpuVolume* g)
     dfree(g->dimg); dfree(g->dhit); dfree(g->dface);
     if (g->hstage) cudaFreeHost(g->hstage);
     if (g->hst) cudaFreeHost(g->hst);
+    if (g->evicted) cudaFreeHost(g->evicted);
     if (g->stageFree) cudaEventDestroy(g->stageFree);
     if (g->ownStream) cudaStreamDestroy(g->ownStream);
     delete g;
@@ -202,6 +204,7 @@ extern "C" int dn_cuda_map_create(uint32_t sx, uint32_t sy, uint32_t sz, uint32_
 
 extern "C" int dn_cuda_map_resize(DNgpuVolume* g, uint32_t sx, uint32_t sy, uint32_t sz)
 {
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
     uint64_t n = (uint64_t)sx * sy * sz;
     if (n == 0 || n >= (1ull << 28)) return dn_set_err(DN_CUDA_ERR_ARG, "map size %ux%ux%u", sx, sy, sz);
@@ -227,8 +230,116 @@ template <class T> static int grow_copy(DNgpuVolume* g, T** p, uint64_t oldCount
     return DN_CUDA_OK;
 }
 
+// ------------------------------------------------------------ eviction
+//
+// A map's persistent device state -- tile arrays, records and sample counts, the voxel pool with its FP32
+// lighting, the request list and the status block -- is what DN_sync_gpu, DN_draw and DN_update_lighting
+// read and write between frames.  Eviction moves exactly that to pinned host memory and frees every
+// device array of the map (scratch included); restoring allocates and copies it back.  The map's results
+// after a restore are the ones it would have had without the round trip.
+
+struct PersistentArray { void** ptr; size_t bytes; };
+
+static int persistent_arrays(DNgpuVolume* g, PersistentArray* out)
+{
+    const uint64_t n = g->ntiles;
+    int k = 0;
+    out[k++] = {(void**)&g->tword, n * 4};
+    out[k++] = {(void**)&g->treq, n};
+    out[k++] = {(void**)&g->tvis, n};
+    out[k++] = {(void**)&g->ttouch, n};
+    out[k++] = {(void**)&g->tbits, (n + 31) / 32 * 8};
+    out[k++] = {(void**)&g->tlast, n * 4};
+    out[k++] = {(void**)&g->tpend, n * 4};
+    out[k++] = {(void**)&g->tpendSlot, n * 4};
+    out[k++] = {(void**)&g->rec, (size_t)g->slotCap * sizeof(ChunkRec)};
+    out[k++] = {(void**)&g->nsamples, (size_t)g->slotCap * 4};
+    out[k++] = {(void**)&g->vox, (size_t)g->voxCap * 8};
+    out[k++] = {(void**)&g->diff, (size_t)g->voxCap * 16};
+    out[k++] = {(void**)&g->spec, (size_t)g->voxCap * 16};
+    out[k++] = {(void**)&g->reqs, (size_t)g->reqCap * 4};
+    out[k++] = {(void**)&g->st, sizeof(DevState)};
+    return k;
+}
+
+static size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+extern "C" uint64_t dn_cuda_map_footprint(DNgpuVolume* g)
+{
+    if (!g) return 0;
+    PersistentArray a[16];
+    const int k = persistent_arrays(g, a);
+    uint64_t total = 0;
+    for (int i = 0; i < k; i++) total += a[i].bytes;
+    total += (uint64_t)g->reqCap * 64 * sizeof(float4) + g->dstageCap + (uint64_t)g->dimgCap * 21;
+    return total;
+}
+
+extern "C" int dn_cuda_map_is_resident(DNgpuVolume* g) { return g && !g->evicted; }
+
+extern "C" int dn_cuda_map_evict(DNgpuVolume* g)
+{
+    if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
+    if (g->evicted) return DN_CUDA_OK;
+    CK(cudaSetDevice(g->device));
+    CK(cudaStreamSynchronize(g->stream));
+    PersistentArray a[16];
+    const int k = persistent_arrays(g, a);
+    size_t total = 0;
+    for (int i = 0; i < k; i++) total += align16(a[i].bytes);
+    unsigned char* h = nullptr;
+    CK(cudaMallocHost((void**)&h, total ? total : 1));
+    size_t o = 0;
+    for (int i = 0; i < k; i++) {
+        cudaError_t e = cudaMemcpyAsync(h + o, *a[i].ptr, a[i].bytes, cudaMemcpyDeviceToHost, g->stream);
+        if (e != cudaSuccess) { cudaStreamSynchronize(g->stream); cudaFreeHost(h); return dn_set_err(DN_CUDA_ERR_LAUNCH, "evict: %s", cudaGetErrorString(e)); }
+        o += align16(a[i].bytes);
+    }
+    cudaError_t e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) { cudaFreeHost(h); return dn_set_err(DN_CUDA_ERR_LAUNCH, "evict: %s", cudaGetErrorString(e)); }
+    for (int i = 0; i < k; i++) { cudaFree(*a[i].ptr); *a[i].ptr = nullptr; }
+    dfree(g->lightOut); dfree(g->dstage); dfree(g->dimg); dfree(g->dhit); dfree(g->dface);
+    g->dstageCap = 0; g->dimgCap = 0;
+    g->evicted = h;
+    g->evictedBytes = total;
+    dn_new_generation(g);
+    return DN_CUDA_OK;
+}
+
+extern "C" int dn_cuda_map_restore(DNgpuVolume* g)
+{
+    if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
+    if (!g->evicted) return DN_CUDA_OK;
+    CK(cudaSetDevice(g->device));
+    PersistentArray a[16];
+    const int k = persistent_arrays(g, a);
+    int rc = DN_CUDA_OK;
+    for (int i = 0; i < k && !rc; i++) {
+        cudaError_t e = cudaMalloc(a[i].ptr, a[i].bytes ? a[i].bytes : 1);
+        if (e != cudaSuccess) { *a[i].ptr = nullptr; rc = dn_set_err(DN_CUDA_ERR_NOMEM, "restore: %s", cudaGetErrorString(e)); }
+    }
+    if (!rc) rc = dalloc(&g->lightOut, (size_t)g->reqCap * 64);
+    if (rc) {
+        for (int i = 0; i < k; i++) if (*a[i].ptr) { cudaFree(*a[i].ptr); *a[i].ptr = nullptr; }
+        dfree(g->lightOut);
+        return rc;
+    }
+    size_t o = 0;
+    for (int i = 0; i < k; i++) {
+        CK(cudaMemcpyAsync(*a[i].ptr, g->evicted + o, a[i].bytes, cudaMemcpyHostToDevice, g->stream));
+        o += align16(a[i].bytes);
+    }
+    CK(cudaStreamSynchronize(g->stream));
+    cudaFreeHost(g->evicted);
+    g->evicted = nullptr;
+    g->evictedBytes = 0;
+    dn_new_generation(g);
+    return DN_CUDA_OK;
+}
+
 extern "C" int dn_cuda_reserve(DNgpuVolume* g, uint32_t slotCap, uint64_t voxelCap, uint64_t requestCap)
 {
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
     CK(cudaSetDevice(g->device));
     int rc;
@@ -344,6 +455,37 @@ __global__ void __launch_bounds__(128, DN_STREAM_MIN_BLOCKS) k_light_stream(cons
     stream_loop<false>(&a, nullptr, &sh, jobs[threadIdx.x]);
 }
 
+// The lighting launch with specular and shadow fans traced as warp packets (dn_light_packet.cuh).
+__global__ void __launch_bounds__(128, DN_PACKET_MIN_BLOCKS) k_light_packet(const __grid_constant__ StreamArgs a)
+{
+    __shared__ StreamShared sh;
+    __shared__ PacketWarp warps[4];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) sh.mats[i] = a.mats[i];
+    for (int k = threadIdx.x; k < 65; k += blockDim.x) shadow_dir(a.p, k, sh.sdir[k], sh.sinv[k]);
+    __syncthreads();
+    packet_loop<false>(&a, nullptr, &sh, warps[threadIdx.x >> 5]);
+}
+
+// launches the lighting kernel g_lightKernel selects (1 ray streams, 2 warp packets; packets need
+// specBounceLimit <= PK_MAX_SPEC_SEGMENTS and fall back to streams otherwise)
+static int launch_light(DNgpuVolume* g, const StreamArgs& a)
+{
+    int perSM = 0;
+    if (g_lightKernel == 2 && a.p.specBounceLimit <= PK_MAX_SPEC_SEGMENTS) {
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_packet, 128, 0));
+        if (perSM < 1) perSM = 1;
+        COUNT_LAUNCH();
+        k_light_packet<<<g->numSMs * perSM, 128, 0, g->stream>>>(a);
+    } else {
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_stream, 128, 0));
+        if (perSM < 1) perSM = 1;
+        COUNT_LAUNCH();
+        k_light_stream<<<g->numSMs * perSM, 128, 0, g->stream>>>(a);
+    }
+    CK(cudaGetLastError());
+    return DN_CUDA_OK;
+}
+
 // D1/D2: commit the new lighting after the whole launch, then count the sample
 __global__ void k_commit(DevMap m, const uint32_t* reqs, const DevState* st, const float4* out,
                          float4* diff, float4* spec, uint32_t* nsamples)
@@ -455,6 +597,7 @@ int dn_stage_ops(DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops, const dn_
 extern "C" int dn_cuda_sync_stage(DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops, const dn_chunk_record* records,
                                   uint32_t nrecords, const uint32_t* voxelWords, uint64_t nvoxels)
 {
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     CK(cudaSetDevice(g->device));
     return dn_stage_ops(g, ops, nops, records, nrecords, voxelWords, nvoxels);
@@ -464,6 +607,7 @@ extern "C" int dn_cuda_sync(DNgpuVolume* g, const dn_sync_params* p, const dn_ti
                             const dn_chunk_record* records, uint32_t nrecords, const uint32_t* voxelWords,
                             uint64_t nvoxels)
 {
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !p) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (p->split == 0 || p->op > 2) return dn_set_err(DN_CUDA_ERR_ARG, "bad sync parameters");
     CK(cudaSetDevice(g->device));
@@ -488,6 +632,7 @@ extern "C" int dn_cuda_sync(DNgpuVolume* g, const dn_sync_params* p, const dn_ti
 
 extern "C" int dn_cuda_light(DNgpuVolume* g, const dn_light_params* p, const dn_material* materials)
 {
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !p || !materials) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (p->K < 1 || p->K > 64) return dn_set_err(DN_CUDA_ERR_ARG, "K = %u", p->K);
     CK(cudaSetDevice(g->device));
@@ -515,12 +660,8 @@ extern "C" int dn_cuda_light(DNgpuVolume* g, const dn_light_params* p, const dn_
         a->batch = g_streamBatch;
         a->p = *p;
         memcpy(a->mats, materials, sizeof(a->mats));
-        int perSM = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_stream, 128, 0));
-        if (perSM < 1) perSM = 1;
-        COUNT_LAUNCH();
-        k_light_stream<<<g->numSMs * perSM, 128, 0, g->stream>>>(*a);
-        CK(cudaGetLastError());
+        int rc = launch_light(g, *a);
+        if (rc) return rc;
     }
     COUNT_LAUNCH();
     k_commit<<<g->numSMs * 4, 256, 0, g->stream>>>(dev_map(g), g->reqs, g->st, g->lightOut, g->diff, g->spec, g->nsamples);
@@ -569,6 +710,7 @@ static int noalloc_scratch(int device, float4** out)
 
 extern "C" int dn_cuda_light_noalloc(DNgpuVolume* g, const dn_light_params* p, const dn_material* materials)
 {
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !p || !materials) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (p->K < 1 || p->K > 64) return dn_set_err(DN_CUDA_ERR_ARG, "K = %u", p->K);
     CK(cudaSetDevice(g->device));
@@ -592,12 +734,8 @@ extern "C" int dn_cuda_light_noalloc(DNgpuVolume* g, const dn_light_params* p, c
     a.batch = g_streamBatch;
     a.p = *p;
     memcpy(a.mats, materials, sizeof(a.mats));
-    int perSM = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_stream, 128, 0));
-    if (perSM < 1) perSM = 1;
-    COUNT_LAUNCH();
-    k_light_stream<<<g->numSMs * perSM, 128, 0, g->stream>>>(a);
-    CK(cudaGetLastError());
+    rc = launch_light(g, a);
+    if (rc) return rc;
     COUNT_LAUNCH();
     k_commit<<<g->numSMs * 4, 256, 0, g->stream>>>(dev_map(g), g->reqs, g->st, scratch, g->diff, g->spec, g->nsamples);
     CK(cudaGetLastError());
@@ -636,6 +774,7 @@ static int launch_draw(DNgpuVolume* g, const dn_draw_params* p, const dn_materia
 extern "C" int dn_cuda_draw(DNgpuVolume* g, const dn_draw_params* p, const dn_material* materials, float* colorOut,
                             uint32_t* hitOut, uint8_t* faceOut)
 {
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !p || !materials || !colorOut) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (p->width == 0 || p->height == 0) return dn_set_err(DN_CUDA_ERR_ARG, "empty image");
     CK(cudaSetDevice(g->device));
@@ -645,6 +784,7 @@ extern "C" int dn_cuda_draw(DNgpuVolume* g, const dn_draw_params* p, const dn_ma
 extern "C" int dn_cuda_draw_host(DNgpuVolume* g, const dn_draw_params* p, const dn_material* materials,
                                  float* colorOut, uint32_t* hitOut, uint8_t* faceOut)
 {
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !p || !materials || !colorOut) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (p->width == 0 || p->height == 0) return dn_set_err(DN_CUDA_ERR_ARG, "empty image");
     CK(cudaSetDevice(g->device));
@@ -663,6 +803,7 @@ extern "C" int dn_cuda_draw_host(DNgpuVolume* g, const dn_draw_params* p, const 
 
 extern "C" int dn_cuda_finish(DNgpuVolume* g, uint64_t* numRequests)
 {
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
     CK(cudaSetDevice(g->device));
     CK(cudaMemcpyAsync(g->hst, g->st, sizeof(DevState), cudaMemcpyDeviceToHost, g->stream));
@@ -678,6 +819,7 @@ extern "C" int dn_cuda_finish(DNgpuVolume* g, uint64_t* numRequests)
 
 extern "C" int dn_cuda_stats_kind(DNgpuVolume* g, int kind, dn_stats* out)
 {
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !out || kind < 0 || kind > 2) return dn_set_err(DN_CUDA_ERR_ARG, "bad argument");
     int rc = dn_cuda_finish(g, nullptr);
     if (rc && rc != DN_CUDA_ERR_KERNEL) return rc;
@@ -693,6 +835,7 @@ extern "C" int dn_cuda_stats(DNgpuVolume* g, dn_stats* out) { return dn_cuda_sta
 
 extern "C" int dn_cuda_reset_stats(DNgpuVolume* g)
 {
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
     CK(cudaSetDevice(g->device));
     CK(cudaMemsetAsync(g->st->stats, 0, sizeof(g->st->stats) + sizeof(g->st->lstats), g->stream));
@@ -703,6 +846,7 @@ extern "C" void* dn_cuda_stream(DNgpuVolume* g) { return g ? (void*)g->stream : 
 
 extern "C" int dn_cuda_export_tiles(DNgpuVolume* g, uint8_t* state, uint8_t* vis, uint32_t* lastUsed, uint32_t* samples)
 {
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
     CK(cudaSetDevice(g->device));
     CK(cudaStreamSynchronize(g->stream));
@@ -728,6 +872,7 @@ extern "C" int dn_cuda_export_tiles(DNgpuVolume* g, uint8_t* state, uint8_t* vis
 
 extern "C" int dn_cuda_export_requests(DNgpuVolume* g, uint32_t* out, uint64_t capacity, uint64_t* count)
 {
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !count) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     uint64_t n = 0;
     int rc = dn_cuda_finish(g, &n);
@@ -740,6 +885,7 @@ extern "C" int dn_cuda_export_requests(DNgpuVolume* g, uint32_t* out, uint64_t c
 extern "C" int dn_cuda_export_lighting(DNgpuVolume* g, uint32_t* index, float* diff, float* spec, uint64_t capacity,
                                        uint64_t* count)
 {
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !count) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     CK(cudaSetDevice(g->device));
     CK(cudaStreamSynchronize(g->stream));
@@ -793,6 +939,14 @@ extern "C" int dn_cuda_memcpy_h2d(void* dst, const void* src, size_t bytes) { CK
 extern "C" int dn_cuda_event_create(void** ev) { CK(cudaEventCreate((cudaEvent_t*)ev)); return DN_CUDA_OK; }
 extern "C" int dn_cuda_event_destroy(void* ev) { CK(cudaEventDestroy((cudaEvent_t)ev)); return DN_CUDA_OK; }
 extern "C" int dn_cuda_event_record(void* ev, void* stream) { CK(cudaEventRecord((cudaEvent_t)ev, (cudaStream_t)stream)); return DN_CUDA_OK; }
+extern "C" int dn_cuda_event_query(void* ev)
+{
+    cudaError_t e = cudaEventQuery((cudaEvent_t)ev);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    dn_set_err(DN_CUDA_ERR_LAUNCH, "event query: %s", cudaGetErrorString(e));
+    return -1;
+}
 extern "C" int dn_cuda_event_elapsed_ms(void* s, void* e, float* ms) { CK(cudaEventElapsedTime(ms, (cudaEvent_t)s, (cudaEvent_t)e)); return DN_CUDA_OK; }
 extern "C" int dn_cuda_stream_sync(void* stream) { CK(cudaStreamSynchronize((cudaStream_t)stream)); return DN_CUDA_OK; }
 extern "C" int dn_cuda_device_sync(void) { CK(cudaDeviceSynchronize()); return DN_CUDA_OK; }
@@ -823,6 +977,6 @@ extern "C" int dn_cuda_flush_l2(void* stream, size_t bytes)
 
 extern "C" const char* dn_cuda_kernel_names(void)
 {
-    return "k_draw;k_light;k_light_stream;k_commit;k_sync_stage;k_compact;k_clamp_requests;k_flush;"
-           "k_draw_batch;k_compact_batch;k_batch_reset;k_batch_prep;k_light_stream_batch;k_commit_batch;k_batch_gather";
+    return "k_draw;k_light;k_light_stream;k_light_packet;k_commit;k_sync_stage;k_compact;k_clamp_requests;k_flush;"
+           "k_draw_batch;k_compact_batch;k_batch_reset;k_batch_prep;k_light_stream_batch;k_light_packet_batch;k_commit_batch;k_batch_gather";
 }

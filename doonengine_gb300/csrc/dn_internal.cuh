@@ -58,6 +58,8 @@ struct DNgpuVolume {
     // device staging for host-memory draws
     float4* dimg; uint32_t* dhit; uint8_t* dface; size_t dimgCap;
     int numSMs;
+    // eviction: every persistent device array copied to one pinned host block, device arrays freed
+    unsigned char* evicted; size_t evictedBytes;
 };
 
 extern int g_device;

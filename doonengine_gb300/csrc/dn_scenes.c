@@ -10,6 +10,7 @@
  *                      surface, normals from the height gradient
  *   dn_scene_shapes    seeded boxes and spheres
  *   dn_scene_camera    a camera above the terrain looking across it
+ *   dn_scene_reroll    re-rolls the voxels of chosen chunks (streaming edits)
  * Per-voxel albedo bytes are the sRGB encoding of the material's linear
  * albedo (x^(1/2.2)), so the reference's upload-time linearisation
  * (voxel.c:1441-1447) gives back approximately the palette value.
@@ -166,4 +167,33 @@ void dn_scene_camera(DNvolume* vol, float fx, float fy, float fz, float pitch, f
 	vol->camOrient.y = yaw;
 	vol->camOrient.z = 0.0f;
 	vol->camFOV = fov;
+}
+
+/* streaming edits: re-rolls the voxels of n existing chunks (pos: 3 ints per chunk, chunk units) from
+ * seed -- each solid voxel takes a new solid material or (1 in 8) is removed, each empty voxel becomes
+ * solid with probability 1/32 -- through the public edit API, so every chunk touched is marked for
+ * re-upload at the next DN_sync_gpu */
+void dn_scene_reroll(DNvolume* vol, const int32_t* pos, uint32_t n, uint32_t seed, uint32_t nMaterials)
+{
+	if (nMaterials == 0) nMaterials = 1;
+	for (uint32_t c = 0; c < n; c++) {
+		DNivec3 mp = {pos[3 * c], pos[3 * c + 1], pos[3 * c + 2]};
+		if (!DN_in_map_bounds(vol, mp)) continue;
+		rng r = {((uint64_t)seed << 32) ^ ((uint64_t)c * 0x9E3779B97F4A7C15ull) ^ 0xC4A7ull};
+		for (int32_t z = 0; z < 8; z++)
+		for (int32_t y = 0; y < 8; y++)
+		for (int32_t x = 0; x < 8; x++) {
+			DNivec3 cp = {x, y, z};
+			const uint32_t u = rnext(&r);
+			if (DN_does_voxel_exist(vol, mp, cp)) {
+				if ((u & 7u) == 0u) { DN_remove_voxel(vol, mp, cp); continue; }
+				DNvoxel v = DN_get_voxel(vol, mp, cp);
+				v.material = (uint8_t)((u >> 8) % nMaterials);
+				v.albedo.r = s_palette[v.material][0]; v.albedo.g = s_palette[v.material][1]; v.albedo.b = s_palette[v.material][2];
+				DN_set_voxel(vol, mp, cp, v);
+			} else if ((u & 31u) == 0u) {
+				put(vol, mp.x * 8 + x, mp.y * 8 + y, mp.z * 8 + z, (uint8_t)((u >> 8) % nMaterials), 0.0f, 1.0f, 0.0f);
+			}
+		}
+	}
 }

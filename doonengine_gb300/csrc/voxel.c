@@ -23,6 +23,7 @@
  *     later, voxel.c:1592-1596, 773-782).
  */
 #include "DoonEngine/voxel.h"
+#include "DoonEngine/serve.h"
 #include "dn_cuda.h"
 #include <math.h>
 #include <string.h>
@@ -1079,7 +1080,9 @@ size_t DN_abi_layout(uint64_t* out, size_t n)
 		offsetof(DNvolume, useCubemap), offsetof(DNvolume, frameNum), offsetof(DNvolume, emissiveStrength),
 		offsetof(DNvolume, deviceBudgetBytes), sizeof(DNchunk), sizeof(DNmaterial), sizeof(DNimage),
 		sizeof(DNchunkHandle), sizeof(DNstats), offsetof(DNchunk, voxels), sizeof(DNvoxel),
-		sizeof(DNbatchItem), offsetof(DNbatchItem, view), offsetof(DNbatchItem, op), offsetof(DNbatchItem, time)
+		sizeof(DNbatchItem), offsetof(DNbatchItem, view), offsetof(DNbatchItem, op), offsetof(DNbatchItem, time),
+		sizeof(DNrequest), offsetof(DNrequest, edits), offsetof(DNrequest, user), sizeof(DNcompletion),
+		sizeof(DNvoxelEdit), sizeof(DNserveStats)
 	};
 	size_t k = sizeof(v) / sizeof(v[0]);
 	for (size_t i = 0; i < n && i < k; i++) out[i] = v[i];
@@ -1263,3 +1266,5 @@ bool DN_batch_autotune(DNbatch* b)
 	}
 	return true;
 }
+
+void* DN_batch_stream(DNbatch* b) { return b ? dn_cuda_batch_stream(b->gpu) : NULL; }

@@ -328,15 +328,110 @@ class Batch:
         t = L.DnBatchTuning()
         if self.lib.dn_cuda_batch_get_tuning(self._gpu(), byref(t)) != 0:
             raise RuntimeError("dn_cuda_batch_get_tuning failed")
-        return {"streamBatch": t.streamBatch, "blocksPerSM": t.blocksPerSM, "useGraph": t.useGraph}
+        return {"streamBatch": t.streamBatch, "blocksPerSM": t.blocksPerSM, "useGraph": t.useGraph, "kernel": t.kernel}
 
-    def set_tuning(self, streamBatch=None, blocksPerSM=None, useGraph=None):
+    def set_tuning(self, streamBatch=None, blocksPerSM=None, useGraph=None, kernel=None):
         cur = self.tuning()
         t = L.DnBatchTuning(streamBatch if streamBatch is not None else cur["streamBatch"],
                             blocksPerSM if blocksPerSM is not None else cur["blocksPerSM"],
-                            useGraph if useGraph is not None else cur["useGraph"])
+                            useGraph if useGraph is not None else cur["useGraph"],
+                            kernel if kernel is not None else cur["kernel"])
         if self.lib.dn_cuda_batch_set_tuning(self._gpu(), byref(t)) != 0:
             raise RuntimeError("dn_cuda_batch_set_tuning failed: %s" % self.lib.dn_cuda_last_error().decode())
 
     def stream(self):
         return self.lib.dn_cuda_batch_stream(self._gpu())
+
+
+class Server:
+    """A DNserver (include/DoonEngine/serve.h): requests on many volumes served in batched ticks by the
+    server's own thread, with whole-volume eviction under a device budget."""
+
+    def __init__(self, volumes, budget_bytes=0, max_volumes_per_tick=0, ticks_in_flight=2):
+        self.lib = L.load()
+        cfg = L.DNserveConfig(budget_bytes, max_volumes_per_tick, ticks_in_flight)
+        self.ptr = self.lib.DN_server_create(byref(cfg))
+        if not self.ptr:
+            raise RuntimeError("DN_server_create failed: %s" % self.lib.dn_cuda_last_error().decode())
+        self.volumes = list(volumes)
+        for v in self.volumes:
+            if self.lib.DN_server_add_volume(self.ptr, v.ptr) < 0:
+                raise RuntimeError("DN_server_add_volume failed")
+        self._keep = []
+
+    def start(self):
+        if not self.lib.DN_server_start(self.ptr):
+            raise RuntimeError("DN_server_start failed")
+
+    @staticmethod
+    def draw_request(volume, image, view, proj, user=0):
+        r = L.DNrequest()
+        r.kind, r.volume, r.output, r.view, r.projection, r.user = L.REQUEST_DRAW, volume, image.ptr, view, proj, user
+        return r
+
+    @staticmethod
+    def relight_request(volume, num_diffuse=1, max_diffuse=1000, time=0.0, user=0):
+        r = L.DNrequest()
+        r.kind, r.volume, r.user = L.REQUEST_RELIGHT, volume, user
+        r.numDiffuseSamples, r.maxDiffuseSamples, r.time = num_diffuse, max_diffuse, time
+        return r
+
+    def edit_request(self, volume, edits, user=0):
+        """edits: iterable of (mapPos, chunkPos, material, normal, albedo, remove)."""
+        arr = (L.DNvoxelEdit * max(1, len(edits)))()
+        for i, (mp, cp, mat, nrm, alb, rem) in enumerate(edits):
+            arr[i].mapPos, arr[i].chunkPos = L.DNivec3(*mp), L.DNivec3(*cp)
+            arr[i].voxel = L.DNvoxel(mat, L.DNvec3(*nrm), L.DNcolor(*alb))
+            arr[i].remove = 1 if rem else 0
+        self._keep.append(arr)
+        r = L.DNrequest()
+        r.kind, r.volume, r.user = L.REQUEST_EDIT, volume, user
+        r.edits, r.numEdits = ctypes.cast(arr, POINTER(L.DNvoxelEdit)), len(edits)
+        return r
+
+    def submit(self, req):
+        rid = self.lib.DN_server_submit(self.ptr, byref(req))
+        if not rid:
+            raise RuntimeError("DN_server_submit rejected the request")
+        return rid
+
+    def replay(self, reqs, offsets):
+        arr = (L.DNrequest * len(reqs))(*reqs)
+        off = np.ascontiguousarray(offsets, np.float64)
+        return self.lib.DN_server_replay(self.ptr, arr, off.ctypes.data_as(POINTER(ctypes.c_double)), len(reqs))
+
+    def drain(self, timeout=600.0):
+        return bool(self.lib.DN_server_drain(self.ptr, timeout))
+
+    def poll(self, cap=1 << 16):
+        out = []
+        buf = (L.DNcompletion * cap)()
+        while True:
+            n = self.lib.DN_server_poll(self.ptr, buf, cap)
+            out += [dict(id=buf[i].id, user=buf[i].user or 0, kind=buf[i].kind, volume=buf[i].volume,
+                         arrival=buf[i].arrival, admitted=buf[i].admitted, finished=buf[i].finished, ok=buf[i].ok)
+                    for i in range(n)]
+            if n < cap:
+                return out
+
+    def stats(self):
+        st = L.DNserveStats()
+        self.lib.DN_server_get_stats(self.ptr, byref(st))
+        return {k: int(getattr(st, k)) for k, _ in L.DNserveStats._fields_}
+
+    def batch_stats(self):
+        s = L.DNstats()
+        self.lib.DN_batch_get_stats(self.lib.DN_server_batch(self.ptr), byref(s))
+        return {k: int(getattr(s, k)) for k, _ in L.DNstats._fields_}
+
+    def close(self):
+        if self.ptr:
+            self.lib.DN_server_destroy(self.ptr)
+            self.ptr = None
+            self._keep = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

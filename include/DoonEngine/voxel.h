@@ -141,7 +141,7 @@ typedef struct DNvolume
 	uint32_t rngMode;                /* READ-WRITE | 0 = per-ray integer hash (default), 1 = reference sin-fract */
 	uint32_t mapId;                  /* READ-WRITE | random-stream key of this map */
 	uint32_t truncateDispatch;       /* READ-WRITE | 1 = skip the right/bottom pixels the reference's w/16 x h/16 dispatch drops */
-	uint64_t deviceBudgetBytes;      /* READ-WRITE | 0 = unlimited; otherwise staged chunks are evicted LRU above it */
+	uint64_t deviceBudgetBytes;      /* READ-WRITE | reserved (0); the device pool grows instead of evicting chunks; whole-volume eviction under a device budget is the serving layer's (serve.h) */
 } DNvolume;
 
 /* voxel.h:145-150 */
@@ -299,6 +299,8 @@ void DN_batch_reset_stats(DNbatch* batch);
 /* picks the batched lighting launch's stream batch and blocks per SM by timing the last frame's
  * lighting under each candidate; results are unaffected */
 bool DN_batch_autotune(DNbatch* batch);
+/* the CUDA stream (cudaStream_t) all work of the batch and its members runs on */
+void* DN_batch_stream(DNbatch* batch);
 
 #ifdef __cplusplus
 }

@@ -175,6 +175,7 @@ typedef struct dn_batch_tuning {
     uint32_t streamBatch;       /* lanes of a warp that wait before per-segment work runs, 1..32 */
     uint32_t blocksPerSM;       /* resident lighting blocks per SM, 1..4 */
     uint32_t useGraph;          /* replay repeated frames as a CUDA graph */
+    uint32_t kernel;            /* lighting kernel: 1 per-lane ray streams, 2 warp packets of ray fans */
 } dn_batch_tuning;
 
 int dn_cuda_batch_create(struct DNgpuBatch** out);
@@ -198,6 +199,18 @@ int dn_cuda_batch_set_tuning(struct DNgpuBatch* b, const dn_batch_tuning* t);
 int dn_cuda_batch_autotune(struct DNgpuBatch* b, dn_batch_tuning* chosen);
 /* request groups of the map's last sync, as read by its last dn_cuda_finish or dn_cuda_batch_finish */
 uint64_t dn_cuda_requests_of(struct DNgpuVolume* g);
+
+/* --- residency (no counterpart in the reference; used by the serving loop's admission control) ---
+ * A map's device bytes (persistent arrays plus scratch).  Eviction waits for the map's work, copies its
+ * persistent state (tiles, records, voxel pool and FP32 lighting, request list, status) to pinned host
+ * memory and frees all its device memory; restore brings it back, after which the map behaves exactly as
+ * if it had never left.  Other entries reject an evicted map with DN_CUDA_ERR_ARG. */
+uint64_t dn_cuda_map_footprint(struct DNgpuVolume* g);
+int dn_cuda_map_is_resident(struct DNgpuVolume* g);
+int dn_cuda_map_evict(struct DNgpuVolume* g);
+int dn_cuda_map_restore(struct DNgpuVolume* g);
+/* 1 when the work recorded by ev has completed, 0 while pending, negative on error */
+int dn_cuda_event_query(void* ev);
 
 /* --- synchronisation, counters, introspection (additions) --- */
 int dn_cuda_finish(struct DNgpuVolume* g, uint64_t* numRequests);
