@@ -724,7 +724,9 @@ def run_serving(args):
                "evictions": st1["evictions"] - st0["evictions"], "restores": st1["restores"] - st0["restores"]}
         log("rate %g: %s" % (rate, {k: row[k] for k in ("completed", "achieved_rps", "p50_ms", "p99_ms", "rays_per_s")}))
         sweep.append(row)
-        if not ok:
+        # past saturation the queue only grows: stop the sweep there
+        if not ok or (row["achieved_rps"] or 0.0) < 0.9 * rate:
+            row["saturated"] = True
             break
     st = server.stats()
     good = [r for r in sweep if r["p99_ms"] is not None and r["p99_ms"] <= 33.0 and r["drained"]]
@@ -837,11 +839,12 @@ def main():
                     help="plain: one map per step (the headline); batched: many maps per step")
     ap.add_argument("--maps", type=int, default=64, help="maps of the batched workload")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--rates", default="500,1000,2000,5000,10000,20000", help="serving: offered req/s")
+    ap.add_argument("--rates", default="100,200,300,400,500,600,700,850,1000,1500,2000,5000,10000,20000",
+                    help="serving: offered req/s, swept upwards until the server saturates")
     ap.add_argument("--seconds", type=float, default=4.0, help="serving: seconds of arrivals per rate")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device budget")
     ap.add_argument("--image-ring", type=int, default=16, help="serving: draw targets per resolution")
-    ap.add_argument("--drain-timeout", type=float, default=120.0)
+    ap.add_argument("--drain-timeout", type=float, default=20.0)
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3 (at least three untimed steps)")

@@ -70,9 +70,9 @@ void dn_new_generation(DNgpuVolume* g) { g->gen = __atomic_add_fetch(&g_generati
 
 extern "C" uint64_t dn_cuda_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
-// lighting kernel selection and stream batch threshold (DN_LIGHT_KERNEL=0 lockstep, 1 streams;
-// DN_STREAM_BATCH lanes, 1..32), read once at init
-int g_lightKernel = 1;
+// lighting kernel selection and stream batch threshold (DN_LIGHT_KERNEL=0 lockstep, 1 per-lane ray streams,
+// 2 warp packets of ray fans; DN_STREAM_BATCH lanes, 1..32), read once at init
+int g_lightKernel = 2;
 uint32_t g_streamBatch = 24;
 
 extern "C" int dn_cuda_init(int device)

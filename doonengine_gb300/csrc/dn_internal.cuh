@@ -65,7 +65,7 @@ struct DNgpuVolume {
 extern int g_device;
 extern int g_numSMs;
 extern unsigned long long g_launches;   // kernels launched by this library (all threads)
-extern int g_lightKernel;               // 0 lockstep, 1 per-lane ray streams
+extern int g_lightKernel;               // 0 lockstep, 1 per-lane ray streams, 2 warp packets (default)
 extern uint32_t g_streamBatch;          // lanes that wait before per-segment work runs (1..32)
 #define COUNT_LAUNCH() __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED)
 

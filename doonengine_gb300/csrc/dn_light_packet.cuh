@@ -118,6 +118,13 @@ __device__ __forceinline__ int pass_voxel(uint32_t mask, uint32_t base, uint32_t
     return __ffs(mm) - 1;
 }
 
+enum : uint32_t { PP_SPEC = 0, PP_FIRST = 1, PP_FAN = 2, PP_DIFF = 3, PP_DONE = 4 };
+
+// The request groups of one launch.  Per group the warp runs four passes -- specular fans, first-sample
+// shadow rays, shadow fans, diffuse paths -- as a state machine around a single stepping loop: each pass
+// unit (a pack of voxels for the fans, all voxels for the others) starts one segment per lane, the lanes
+// step together until every segment ended, the pass shades the ended segments and starts follow-up
+// segments, and when no lane has work the unit's sums are formed and the next unit starts.
 template <bool MANY>
 __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLightArgs* many, const StreamShared* sh,
                                             PacketWarp& W)
@@ -162,289 +169,296 @@ __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLi
         const uint32_t myFlags = W.v[lane].flags;
         const uint32_t rounds = K <= 32u ? 1u : (K + 31u) / 32u;
         const uint32_t vpp = K <= 32u ? 32u / K : 1u;
+        const uint32_t specAll = __ballot_sync(0xFFFFFFFFu, (myFlags & (PV_VALID | PV_SPEC)) == (PV_VALID | PV_SPEC));
+        const uint32_t specMask = p.specBounceLimit > 0u ? specAll : 0u;
+        // no specular segments: the sum stays zero and is still divided by K
+        if (!specMask && ((specAll >> lane) & 1u)) W.v[lane].spec = divs(mk(0.0f, 0.0f, 0.0f), (float)K);
+        const uint32_t diffMask = __ballot_sync(0xFFFFFFFFu, (myFlags & (PV_VALID | PV_DIFF)) == (PV_VALID | PV_DIFF));
+        const uint32_t firstMask = diffMask & __ballot_sync(0xFFFFFFFFu, (myFlags & PV_FIRST) != 0u);
+        const uint32_t fanMask = diffMask & ~firstMask;
+        const uint32_t nSpec = (uint32_t)__popc(specMask), nFan = (uint32_t)__popc(fanMask);
 
-        // ---- specular fans (voxelLighting.comp:83-146), segments stored per lane for the ordered sum
-        const uint32_t specMask = __ballot_sync(0xFFFFFFFFu, (myFlags & (PV_VALID | PV_SPEC)) == (PV_VALID | PV_SPEC));
-        if (specMask && p.specBounceLimit > 0u) {
-            for (uint32_t base = 0; base < (uint32_t)__popc(specMask); base += vpp) {
-                f3 acc = mk(0.0f, 0.0f, 0.0f);
-                int vi = -1;
-                uint32_t sg = 0;
-                for (uint32_t round = 0; round < rounds; round++) {
-                    uint32_t kk;
-                    vi = pass_voxel(specMask, base, K, lane, round, kk, sg);
-                    const bool act = vi >= 0;
-                    Seg s;
-                    f3 jA, jB;
-                    uint32_t jU = 0, b = 0, ncon = 0, hs = 0, hitIdx = 0;
-                    bool live = act, stepping = false;
-                    if (act) {
-                        const PacketVoxel& pv = W.v[vi];
-                        const Material& tm = mats[pv.tmat];
-                        jA = pv.talbedo; jB = pv.pos0; jU = tm.reflectType;
-                        const f3 P = mk(p.spherePts[kk][0], p.spherePts[kk][1], p.spherePts[kk][2]);
-                        const f3 sd = adds(normalize(add(muls(pv.refl, (float)tm.shininess), P)), EPS);
-                        seg_begin(s, pv.pos0, sd, rcp3(sd));
-                        c.rays++;
-                        stepping = true;
-                    }
-                    while (__any_sync(0xFFFFFFFFu, live)) {
-                        packet_trace(stepping, s, m, mats, p.sunStrength, c, hs, hitIdx);
-                        stepping = false;
-                        if (live) {
-                            // specular_ray body after step_map (voxelLighting.comp:98-144)
-                            const PacketVoxel& pv = W.v[vi];
-                            bool more = false, add_ = false;
-                            f3 cc = mk(0.0f, 0.0f, 0.0f);
-                            if (hs == 1u) {
-                                Voxel hv;
-                                decompress(m, hitIdx, hv);
-                                const i3 hp{f2i(truncf(s.pos.x)), f2i(truncf(s.pos.y)), f2i(truncf(s.pos.z))};
-                                if (in_map(m, hp)) {
-                                    uint8_t* vp = &m.tvis[map_index(m, hp)];
-                                    if (*vp == 0) *vp = 1;
+        // per-lane state, shared by the passes
+        Seg s;
+        uint32_t hs = 0, hitIdx = 0;
+        bool live = false, stepping = false;
+        int vi = -1;                 // voxel of this lane's ray in the current unit
+        uint32_t kk = 0, sg = 0;     // ray index, segment of the pack
+        f3 pacc = mk(0.0f, 0.0f, 0.0f), cc = pacc;
+        uint32_t pi = 0, ncon = 0;
+        bool has = false;
+        // the ray job's state: specular mult / last position / reflect type / bounce, or diffuse_dir's view of
+        // this lane's path (lane == voxel in the diffuse pass)
+        Job jd;
+
+        uint32_t pass = PP_SPEC, base = 0, round = 0;
+        bool unitOpen = false;
+        for (int guard = 0; guard < (1 << 30); guard++) {
+            if (!__any_sync(0xFFFFFFFFu, live)) {
+                // ---- close the unit: ordered sums
+                if (unitOpen) {
+                    if (pass == PP_SPEC) {
+                        W.ncon[lane] = vi >= 0 ? ncon : 0u;
+                        __syncwarp();
+                        if (vi >= 0) {
+                            const uint32_t nk = K <= 32u ? K : ((K - 32u * round) < 32u ? (K - 32u * round) : 32u);
+                            for (uint32_t k2 = 0; k2 < nk; k2++) {
+                                const uint32_t src = K <= 32u ? sg * K + k2 : k2;
+                                const uint32_t n = W.ncon[src];
+                                for (uint32_t jj = 0; jj < n; jj++) {
+                                    pacc.x = pacc.x + W.con[src][jj][0];
+                                    pacc.y = pacc.y + W.con[src][jj][1];
+                                    pacc.z = pacc.z + W.con[src][jj][2];
                                 }
-                                const f3 d = vabs(sub(vfloor(muls(s.pos, 8.0f)), vfloor(muls(jB, 8.0f))));
-                                if (!(dot(d, d) <= 1.0f)) {
-                                    const Material& hm = mats[hv.material];
-                                    const f3 hd = muls(hv.diff, 1.0f - hm.specular);
-                                    add_ = true;
-                                    if (hm.emissive) {
-                                        cc.x = ((hv.albedo.x * p.emissiveStrength * s.cmul + s.cadd.x) * jA.x) * pv.talbedo.x;
-                                        cc.y = ((hv.albedo.y * p.emissiveStrength * s.cmul + s.cadd.y) * jA.y) * pv.talbedo.y;
-                                        cc.z = ((hv.albedo.z * p.emissiveStrength * s.cmul + s.cadd.z) * jA.z) * pv.talbedo.z;
-                                    } else {
-                                        const f3 hc = mul(hd, hv.albedo);
-                                        cc.x = (hc.x * s.cmul + s.cadd.x) * jA.x;
-                                        cc.y = (hc.y * s.cmul + s.cadd.y) * jA.y;
-                                        cc.z = (hc.z * s.cmul + s.cadd.z) * jA.z;
-                                        if (hm.specular != 0.0f) {
-                                            jA.x = jA.x * (hv.albedo.x * s.cmul * hm.specular);
-                                            jA.y = jA.y * (hv.albedo.y * s.cmul * hm.specular);
-                                            jA.z = jA.z * (hv.albedo.z * s.cmul * hm.specular);
-                                            jU = hm.reflectType;
-                                            jB = s.pos;
-                                            const f3 nd = reflect(s.dir, hv.normal);
-                                            b++;
-                                            if (b < p.specBounceLimit) {
-                                                const TState keep = s.ts;
-                                                seg_begin(s, s.pos, nd, rcp3(nd));
-                                                s.ts = keep;   // one ray job: bounces keep the transparency state
-                                                c.rays++;
-                                                more = true;
-                                            }
-                                        }
-                                    }
-                                }
-                            } else if (dot(s.dir, sunDir) > 0.99f) {
-                                add_ = true;
-                                cc.x = sun.x * s.cmul + s.cadd.x;
-                                cc.y = sun.y * s.cmul + s.cadd.y;
-                                cc.z = sun.z * s.cmul + s.cadd.z;
-                            } else {
-                                const f3 sc = (jU == 1u) ? sky_color(mk(p.skyBot[0], p.skyBot[1], p.skyBot[2]),
-                                                                    mk(p.skyTop[0], p.skyTop[1], p.skyTop[2]), s.dir) : sun;
-                                add_ = true;
-                                cc.x = (sc.x * s.cmul + s.cadd.x) * jA.x;
-                                cc.y = (sc.y * s.cmul + s.cadd.y) * jA.y;
-                                cc.z = (sc.z * s.cmul + s.cadd.z) * jA.z;
                             }
-                            if (add_ && ncon < PK_MAX_SPEC_SEGMENTS) {   // at most one per segment; host checks the limit
-                                W.con[lane][ncon][0] = cc.x; W.con[lane][ncon][1] = cc.y; W.con[lane][ncon][2] = cc.z;
-                                ncon++;
-                            }
-                            hs = 0;
-                            if (more) stepping = true; else live = false;
                         }
-                    }
-                    W.ncon[lane] = act ? ncon : 0u;
-                    __syncwarp();
-                    // the voxel's sum in ray order, then segment order (the reference's accumulation order)
-                    if (vi >= 0) {
+                        __syncwarp();
+                        if (round + 1u == rounds && vi >= 0 && (K > 32u ? lane == 0u : lane == sg * K))
+                            W.v[vi].spec = divs(pacc, (float)K);
+                    } else if (pass == PP_FIRST) {
+                        if ((firstMask >> lane) & 1u) W.v[lane].direct = divs(pacc, 1.0f);
+                    } else if (pass == PP_FAN) {
+                        const uint32_t hasMask = __ballot_sync(0xFFFFFFFFu, has);
                         const uint32_t nk = K <= 32u ? K : ((K - 32u * round) < 32u ? (K - 32u * round) : 32u);
                         for (uint32_t k2 = 0; k2 < nk; k2++) {
                             const uint32_t src = K <= 32u ? sg * K + k2 : k2;
-                            const uint32_t n = W.ncon[src];
-                            for (uint32_t j = 0; j < n; j++) {
-                                acc.x = acc.x + W.con[src][j][0];
-                                acc.y = acc.y + W.con[src][j][1];
-                                acc.z = acc.z + W.con[src][j][2];
-                            }
+                            const float x = __shfl_sync(0xFFFFFFFFu, cc.x, src);
+                            const float y = __shfl_sync(0xFFFFFFFFu, cc.y, src);
+                            const float z = __shfl_sync(0xFFFFFFFFu, cc.z, src);
+                            if (vi >= 0 && ((hasMask >> src) & 1u)) { pacc.x = pacc.x + x; pacc.y = pacc.y + y; pacc.z = pacc.z + z; }
                         }
+                        if (round + 1u == rounds && vi >= 0 && (K > 32u ? lane == 0u : lane == sg * K))
+                            W.v[vi].direct = divs(pacc, (float)K);
+                    } else {
+                        break;                 // the diffuse unit is the last
                     }
                     __syncwarp();
+                    // ---- next unit
+                    if (++round >= ((pass == PP_SPEC || pass == PP_FAN) ? rounds : 1u)) {
+                        round = 0;
+                        base += (pass == PP_SPEC || pass == PP_FAN) ? vpp : 32u;
+                    }
                 }
-                if (vi >= 0 && (K > 32u ? lane == 0u : lane == sg * K)) W.v[vi].spec = divs(acc, (float)K);
-                __syncwarp();
+                // skip finished or empty passes
+                for (;;) {
+                    const uint32_t nUnits = pass == PP_SPEC ? nSpec : pass == PP_FIRST ? (firstMask ? 1u : 0u)
+                                          : pass == PP_FAN ? nFan : (diffMask ? 1u : 0u);
+                    if (pass == PP_DONE || base < ((pass == PP_SPEC || pass == PP_FAN) ? nUnits : nUnits * 32u)) break;
+                    pass++;
+                    base = 0;
+                    round = 0;
+                }
+                if (pass == PP_DONE) break;
+                unitOpen = true;
+                // ---- open the unit: one segment per lane
+                live = false;
+                hs = 0;
+                vi = -1;
+                if (pass == PP_SPEC || pass == PP_FAN) {
+                    vi = pass_voxel(pass == PP_SPEC ? specMask : fanMask, base, K, lane, round, kk, sg);
+                    if (round == 0u) pacc = mk(0.0f, 0.0f, 0.0f);
+                    has = false;
+                    cc = mk(0.0f, 0.0f, 0.0f);
+                    if (vi >= 0) {
+                        const PacketVoxel& pv = W.v[vi];
+                        if (pass == PP_SPEC) {
+                            const Material& tm = mats[pv.tmat];
+                            jd.jA = pv.talbedo; jd.jB = pv.pos0; jd.jU = tm.reflectType; jd.b = 0; ncon = 0;
+                            const f3 P = mk(p.spherePts[kk][0], p.spherePts[kk][1], p.spherePts[kk][2]);
+                            const f3 sd = adds(normalize(add(muls(pv.refl, (float)tm.shininess), P)), EPS);
+                            seg_begin(s, pv.pos0, sd, rcp3(sd));
+                        } else {
+                            seg_begin(s, pv.pos0, mk(sdir[kk][0], sdir[kk][1], sdir[kk][2]),
+                                      mk(sinv[kk][0], sinv[kk][1], sinv[kk][2]));
+                        }
+                        c.rays++;
+                        live = true;
+                    }
+                } else if (pass == PP_FIRST) {
+                    pacc = mk(0.0f, 0.0f, 0.0f);
+                    if ((firstMask >> lane) & 1u) {
+                        seg_begin(s, W.v[lane].pos0, mk(sdir[64][0], sdir[64][1], sdir[64][2]),
+                                  mk(sinv[64][0], sinv[64][1], sinv[64][2]));
+                        c.rays++;
+                        live = true;
+                    }
+                } else {
+                    // diffuse: lane = voxel; the first path's first segment (or the paths without segments)
+                    pacc = mk(0.0f, 0.0f, 0.0f);
+                    if ((diffMask >> lane) & 1u) {
+                        const PacketVoxel& pv = W.v[lane];
+                        jd.key = pv.key; jd.tnormal = pv.tnormal; jd.tmat = pv.tmat;
+                        jd.firstSample = (pv.flags & PV_FIRST) != 0u;
+                        pi = 0;
+                        live = true;
+                        hs = 3u;             // "start the next path" (see the shading below)
+                    }
+                }
+                stepping = live && hs == 0u;
             }
-        } else if (specMask) {
-            // no specular segments: the sum stays zero and is still divided by K
-            if ((specMask >> lane) & 1u) W.v[lane].spec = divs(mk(0.0f, 0.0f, 0.0f), (float)K);
-        }
-        __syncwarp();
-
-        // ---- direct light: one ray along sunDir + EPS on the first sample, else the K-ray shadow fan (D8)
-        const uint32_t diffMask = __ballot_sync(0xFFFFFFFFu, (myFlags & (PV_VALID | PV_DIFF)) == (PV_VALID | PV_DIFF));
-        const uint32_t firstMask = diffMask & __ballot_sync(0xFFFFFFFFu, (myFlags & PV_FIRST) != 0u);
-        if (firstMask) {
-            const bool act = (firstMask >> lane) & 1u;
-            Seg s;
-            uint32_t hs = 0, hitIdx = 0;
-            if (act) {
-                seg_begin(s, W.v[lane].pos0, mk(sdir[64][0], sdir[64][1], sdir[64][2]),
-                          mk(sinv[64][0], sinv[64][1], sinv[64][2]));
-                c.rays++;
-            }
-            packet_trace(act, s, m, mats, p.sunStrength, c, hs, hitIdx);
-            if (act) {
-                f3 acc = mk(0.0f, 0.0f, 0.0f);
-                if (hs == 2u) {
-                    acc.x = acc.x + (sun.x * s.cmul + s.cadd.x);
-                    acc.y = acc.y + (sun.y * s.cmul + s.cadd.y);
-                    acc.z = acc.z + (sun.z * s.cmul + s.cadd.z);
-                }
-                W.v[lane].direct = divs(acc, 1.0f);
-            }
-        }
-        const uint32_t fanMask = diffMask & ~firstMask;
-        for (uint32_t base = 0; base < (uint32_t)__popc(fanMask); base += vpp) {
-            f3 acc = mk(0.0f, 0.0f, 0.0f);
-            int vi = -1;
-            uint32_t sg = 0;
-            for (uint32_t round = 0; round < rounds; round++) {
-                uint32_t kk;
-                vi = pass_voxel(fanMask, base, K, lane, round, kk, sg);
-                const bool act = vi >= 0;
-                Seg s;
-                uint32_t hs = 0, hitIdx = 0;
-                if (act) {
-                    seg_begin(s, W.v[vi].pos0, mk(sdir[kk][0], sdir[kk][1], sdir[kk][2]),
-                              mk(sinv[kk][0], sinv[kk][1], sinv[kk][2]));
-                    c.rays++;
-                }
-                packet_trace(act, s, m, mats, p.sunStrength, c, hs, hitIdx);
-                // shadow_ray: unoccluded rays add sunStrength * colorMult + colorAdd
-                const bool has = act && hs == 2u;
-                f3 cc = mk(0.0f, 0.0f, 0.0f);
-                if (has) {
-                    cc.x = sun.x * s.cmul + s.cadd.x;
-                    cc.y = sun.y * s.cmul + s.cadd.y;
-                    cc.z = sun.z * s.cmul + s.cadd.z;
-                }
-                const uint32_t hasMask = __ballot_sync(0xFFFFFFFFu, has);
-                const uint32_t nk = K <= 32u ? K : ((K - 32u * round) < 32u ? (K - 32u * round) : 32u);
-                for (uint32_t k2 = 0; k2 < nk; k2++) {
-                    const uint32_t src = K <= 32u ? sg * K + k2 : k2;
-                    const float x = __shfl_sync(0xFFFFFFFFu, cc.x, src);
-                    const float y = __shfl_sync(0xFFFFFFFFu, cc.y, src);
-                    const float z = __shfl_sync(0xFFFFFFFFu, cc.z, src);
-                    if ((hasMask >> src) & 1u) { acc.x = acc.x + x; acc.y = acc.y + y; acc.z = acc.z + z; }
+            // ---- step every started segment to its end (the single stepping loop)
+            while (__any_sync(0xFFFFFFFFu, stepping)) {
+                if (stepping) {
+                    const uint32_t rr = seg_step(s, m, mats, p.sunStrength, c, hitIdx);
+                    if (rr) { stepping = false; hs = rr; }
                 }
             }
-            if (vi >= 0 && (K > 32u ? lane == 0u : lane == sg * K)) W.v[vi].direct = divs(acc, (float)K);
-            __syncwarp();
-        }
-        __syncwarp();
-
-        // ---- diffuse paths (voxelLighting.comp:149-203), one lane per voxel, then the running average
-        const bool mine = (diffMask >> lane) & 1u;
-        f3 acc = mk(0.0f, 0.0f, 0.0f);
-        if (__any_sync(0xFFFFFFFFu, mine)) {
-            const PacketVoxel& pv = W.v[lane];
-            const f3 amb = mk(p.ambient[0], p.ambient[1], p.ambient[2]);
-            Job j;                        // the fields diffuse_dir reads
-            j.key = pv.key; j.tnormal = pv.tnormal; j.tmat = pv.tmat;
-            j.firstSample = (pv.flags & PV_FIRST) != 0u;
-            j.i = 0; j.b = 0;
-            const f3 direct = pv.direct;
-            Seg s;
-            uint32_t hs = 0, hitIdx = 0;
-            bool live = mine, stepping = false;
-            // starts the next path of this lane (or finishes the lane); true when a segment began
-            auto next_path = [&]() -> bool {
-                while (j.i < p.numDiffuse) {
-                    acc = add(acc, amb);
-                    if (p.diffuseBounceLimit == 0u) { acc = add(acc, direct); j.i++; continue; }
-                    j.b = 0;
-                    j.jA = mk(1.0f, 1.0f, 1.0f);
-                    j.jB = adds(j.tnormal, EPS);
-                    j.jC = mk(0.0f, 0.0f, 0.0f);
-                    j.jU = j.tmat;
-                    const f3 nd = diffuse_dir(j, p, mats, rngSin);
-                    seg_begin(s, pv.pos0, nd, rcp3(nd));
-                    c.rays++;
-                    return true;
-                }
-                return false;
-            };
-            if (live) { stepping = next_path(); live = stepping; }
-            while (__any_sync(0xFFFFFFFFu, live)) {
-                packet_trace(stepping, s, m, mats, p.sunStrength, c, hs, hitIdx);
-                stepping = false;
-                if (live) {
-                    bool pathDone = true;
-                    if (hs == 1u) {
-                        Voxel hv;
-                        decompress(m, hitIdx, hv);
-                        j.jB = hv.normal;
-                        j.jU = hv.material;
-                        const f3 d = vabs(sub(vfloor(muls(pv.pos0, 8.0f)), vfloor(muls(s.pos, 8.0f))));
-                        if (!(dot(d, d) < 1.0f)) {
-                            const Material& hm = mats[hv.material];
-                            if (hm.emissive) {
-                                acc.x = acc.x + j.jA.x * (hv.albedo.x * p.emissiveStrength * s.cmul + s.cadd.x);
-                                acc.y = acc.y + j.jA.y * (hv.albedo.y * p.emissiveStrength * s.cmul + s.cadd.y);
-                                acc.z = acc.z + j.jA.z * (hv.albedo.z * p.emissiveStrength * s.cmul + s.cadd.z);
-                            } else {
-                                j.jA.x = j.jA.x * (hv.albedo.x * s.cmul + s.cadd.x);
-                                j.jA.y = j.jA.y * (hv.albedo.y * s.cmul + s.cadd.y);
-                                j.jA.z = j.jA.z * (hv.albedo.z * s.cmul + s.cadd.z);
-                                j.jC = s.dir;
-                                j.b++;
-                                if (j.b < p.diffuseBounceLimit) {
-                                    const f3 nd = diffuse_dir(j, p, mats, rngSin);
+            // ---- shade the ended segments
+            if (!live || hs == 0u) continue;
+            if (pass == PP_SPEC) {
+                // specular_ray body after step_map (voxelLighting.comp:98-144)
+                const PacketVoxel& pv = W.v[vi];
+                bool more = false, add_ = false;
+                f3 sc = mk(0.0f, 0.0f, 0.0f);
+                if (hs == 1u) {
+                    Voxel hv;
+                    decompress(m, hitIdx, hv);
+                    const i3 hp{f2i(truncf(s.pos.x)), f2i(truncf(s.pos.y)), f2i(truncf(s.pos.z))};
+                    if (in_map(m, hp)) {
+                        uint8_t* vp = &m.tvis[map_index(m, hp)];
+                        if (*vp == 0) *vp = 1;
+                    }
+                    const f3 d = vabs(sub(vfloor(muls(s.pos, 8.0f)), vfloor(muls(jd.jB, 8.0f))));
+                    if (!(dot(d, d) <= 1.0f)) {
+                        const Material& hm = mats[hv.material];
+                        const f3 hd = muls(hv.diff, 1.0f - hm.specular);
+                        add_ = true;
+                        if (hm.emissive) {
+                            sc.x = ((hv.albedo.x * p.emissiveStrength * s.cmul + s.cadd.x) * jd.jA.x) * pv.talbedo.x;
+                            sc.y = ((hv.albedo.y * p.emissiveStrength * s.cmul + s.cadd.y) * jd.jA.y) * pv.talbedo.y;
+                            sc.z = ((hv.albedo.z * p.emissiveStrength * s.cmul + s.cadd.z) * jd.jA.z) * pv.talbedo.z;
+                        } else {
+                            const f3 hc = mul(hd, hv.albedo);
+                            sc.x = (hc.x * s.cmul + s.cadd.x) * jd.jA.x;
+                            sc.y = (hc.y * s.cmul + s.cadd.y) * jd.jA.y;
+                            sc.z = (hc.z * s.cmul + s.cadd.z) * jd.jA.z;
+                            if (hm.specular != 0.0f) {
+                                jd.jA.x = jd.jA.x * (hv.albedo.x * s.cmul * hm.specular);
+                                jd.jA.y = jd.jA.y * (hv.albedo.y * s.cmul * hm.specular);
+                                jd.jA.z = jd.jA.z * (hv.albedo.z * s.cmul * hm.specular);
+                                jd.jU = hm.reflectType;
+                                jd.jB = s.pos;
+                                const f3 nd = reflect(s.dir, hv.normal);
+                                jd.b++;
+                                if (jd.b < p.specBounceLimit) {
                                     const TState keep = s.ts;
                                     seg_begin(s, s.pos, nd, rcp3(nd));
-                                    s.ts = keep;
+                                    s.ts = keep;   // one ray job: bounces keep the transparency state
                                     c.rays++;
-                                    pathDone = false;
+                                    more = true;
                                 }
                             }
                         }
-                    } else {
-                        const float kd = gmax(dot(s.dir, sunDir), 0.0f);
-                        acc.x = acc.x + (j.jA.x * kd * sun.x * s.cmul + s.cadd.x);
-                        acc.y = acc.y + (j.jA.y * kd * sun.y * s.cmul + s.cadd.y);
-                        acc.z = acc.z + (j.jA.z * kd * sun.z * s.cmul + s.cadd.z);
                     }
-                    hs = 0;
-                    if (pathDone) {
-                        acc = add(acc, direct);
-                        j.i++;
-                        j.b = 0;
-                        stepping = next_path();
-                        live = stepping;
-                    } else {
+                } else if (dot(s.dir, sunDir) > 0.99f) {
+                    add_ = true;
+                    sc.x = sun.x * s.cmul + s.cadd.x;
+                    sc.y = sun.y * s.cmul + s.cadd.y;
+                    sc.z = sun.z * s.cmul + s.cadd.z;
+                } else {
+                    const f3 sky = (jd.jU == 1u) ? sky_color(mk(p.skyBot[0], p.skyBot[1], p.skyBot[2]),
+                                                         mk(p.skyTop[0], p.skyTop[1], p.skyTop[2]), s.dir) : sun;
+                    add_ = true;
+                    sc.x = (sky.x * s.cmul + s.cadd.x) * jd.jA.x;
+                    sc.y = (sky.y * s.cmul + s.cadd.y) * jd.jA.y;
+                    sc.z = (sky.z * s.cmul + s.cadd.z) * jd.jA.z;
+                }
+                if (add_ && ncon < PK_MAX_SPEC_SEGMENTS) {   // at most one per segment; the host checks the limit
+                    W.con[lane][ncon][0] = sc.x; W.con[lane][ncon][1] = sc.y; W.con[lane][ncon][2] = sc.z;
+                    ncon++;
+                }
+                hs = 0;
+                if (more) stepping = true; else live = false;
+            } else if (pass == PP_FIRST || pass == PP_FAN) {
+                // shadow_ray: an unoccluded ray adds sunStrength * colorMult + colorAdd
+                if (hs == 2u) {
+                    cc.x = sun.x * s.cmul + s.cadd.x;
+                    cc.y = sun.y * s.cmul + s.cadd.y;
+                    cc.z = sun.z * s.cmul + s.cadd.z;
+                    has = true;
+                    if (pass == PP_FIRST) { pacc.x = pacc.x + cc.x; pacc.y = pacc.y + cc.y; pacc.z = pacc.z + cc.z; }
+                }
+                hs = 0;
+                live = false;
+            } else {
+                // diffuse_ray body after step_map (voxelLighting.comp:176-201); hs == 3: start the next path
+                const PacketVoxel& pv = W.v[lane];
+                bool pathDone = hs != 3u;
+                if (hs == 1u) {
+                    Voxel hv;
+                    decompress(m, hitIdx, hv);
+                    jd.jB = hv.normal;
+                    jd.jU = hv.material;
+                    const f3 d = vabs(sub(vfloor(muls(pv.pos0, 8.0f)), vfloor(muls(s.pos, 8.0f))));
+                    if (!(dot(d, d) < 1.0f)) {
+                        const Material& hm = mats[hv.material];
+                        if (hm.emissive) {
+                            pacc.x = pacc.x + jd.jA.x * (hv.albedo.x * p.emissiveStrength * s.cmul + s.cadd.x);
+                            pacc.y = pacc.y + jd.jA.y * (hv.albedo.y * p.emissiveStrength * s.cmul + s.cadd.y);
+                            pacc.z = pacc.z + jd.jA.z * (hv.albedo.z * p.emissiveStrength * s.cmul + s.cadd.z);
+                        } else {
+                            jd.jA.x = jd.jA.x * (hv.albedo.x * s.cmul + s.cadd.x);
+                            jd.jA.y = jd.jA.y * (hv.albedo.y * s.cmul + s.cadd.y);
+                            jd.jA.z = jd.jA.z * (hv.albedo.z * s.cmul + s.cadd.z);
+                            jd.jC = s.dir;
+                            jd.b++;
+                            if (jd.b < p.diffuseBounceLimit) {
+                                const f3 nd = diffuse_dir(jd, p, mats, rngSin);
+                                const TState keep = s.ts;
+                                seg_begin(s, s.pos, nd, rcp3(nd));
+                                s.ts = keep;
+                                c.rays++;
+                                pathDone = false;
+                                stepping = true;
+                            }
+                        }
+                    }
+                } else if (hs == 2u) {
+                    const float kd = gmax(dot(s.dir, sunDir), 0.0f);
+                    pacc.x = pacc.x + (jd.jA.x * kd * sun.x * s.cmul + s.cadd.x);
+                    pacc.y = pacc.y + (jd.jA.y * kd * sun.y * s.cmul + s.cadd.y);
+                    pacc.z = pacc.z + (jd.jA.z * kd * sun.z * s.cmul + s.cadd.z);
+                }
+                if (pathDone) { pacc = add(pacc, pv.direct); pi++; }
+                hs = 0;
+                if (!stepping) {
+                    // the next path of this voxel, if any (paths without segments finish at once)
+                    live = false;
+                    while (pi < p.numDiffuse) {
+                        pacc = add(pacc, mk(p.ambient[0], p.ambient[1], p.ambient[2]));
+                        if (p.diffuseBounceLimit == 0u) { pacc = add(pacc, pv.direct); pi++; continue; }
+                        jd.i = pi; jd.b = 0;
+                        jd.jA = mk(1.0f, 1.0f, 1.0f);
+                        jd.jB = adds(jd.tnormal, EPS);
+                        jd.jC = mk(0.0f, 0.0f, 0.0f);
+                        jd.jU = jd.tmat;
+                        const f3 nd = diffuse_dir(jd, p, mats, rngSin);
+                        seg_begin(s, pv.pos0, nd, rcp3(nd));
+                        c.rays++;
+                        live = true;
                         stepping = true;
+                        break;
                     }
                 }
             }
-            if (mine) {
-                const float4 prev = __ldg(&m.diff[pv.vidx]);
-                const float den = pv.indirect + (float)p.numDiffuse;
-                acc.x = (prev.x * pv.indirect + acc.x) / den;
-                acc.y = (prev.y * pv.indirect + acc.y) / den;
-                acc.z = (prev.z * pv.indirect + acc.z) / den;
-            }
         }
-        // ---- write the voxel's new lighting (voxelLighting.comp:266-278, FP32)
+        // ---- write the voxel's new lighting (voxelLighting.comp:266-288, FP32)
+        __syncwarp();
         if (myFlags & PV_VALID) {
             const PacketVoxel& pv = W.v[lane];
+            f3 dacc = mk(0.0f, 0.0f, 0.0f);
+            if (myFlags & PV_DIFF) {
+                const float4 prev = __ldg(&m.diff[pv.vidx]);
+                const float den = pv.indirect + (float)p.numDiffuse;
+                dacc.x = (prev.x * pv.indirect + pacc.x) / den;
+                dacc.y = (prev.y * pv.indirect + pacc.y) / den;
+                dacc.z = (prev.z * pv.indirect + pacc.z) / den;
+            }
             const f3 sp = (myFlags & PV_SPEC) ? pv.spec : mk(0.0f, 0.0f, 0.0f);
             const float4 outS = make_float4(gmin(gmax(sp.x, 0.0f), 1.0f), gmin(gmax(sp.y, 0.0f), 1.0f),
                                             gmin(gmax(sp.z, 0.0f), 1.0f), 0.0f);
-            const float4 outD = make_float4(gmin(gmax(acc.x, 0.0f), 1.0f), gmin(gmax(acc.y, 0.0f), 1.0f),
-                                            gmin(gmax(acc.z, 0.0f), 1.0f), 0.0f);
+            const float4 outD = make_float4(gmin(gmax(dacc.x, 0.0f), 1.0f), gmin(gmax(dacc.y, 0.0f), 1.0f),
+                                            gmin(gmax(dacc.z, 0.0f), 1.0f), 0.0f);
             const uint64_t o = ((uint64_t)req * 32u + lane) * 2u;
             out[o] = outD;
             out[o + 1] = outS;

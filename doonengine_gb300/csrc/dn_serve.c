@@ -64,6 +64,7 @@ struct DNserver
 	size_t ndone, doneCap;
 	pthread_t thread;
 	int started, stop;
+	int cancel;                      /* stop serving queued requests: they complete with ok = 0 */
 	Tick ticks[2];
 	unsigned int tickHead, tickCount;
 	uint64_t tickNo;
@@ -402,6 +403,28 @@ static void* serve_main(void* arg)
 			slot->tail = in;
 			in = next;
 		}
+		if (s->cancel) {
+			/* queued requests are not served any more: complete them as failed */
+			pthread_mutex_lock(&s->lock);
+			for (unsigned int i = 0; i < s->nslots; i++) {
+				for (Pending* p = s->slots[i].head; p;) {
+					Pending* n = p->next;
+					if (grow((void**)&s->done, &s->doneCap, s->ndone + 1, sizeof(DNcompletion))) {
+						DNcompletion* c = &s->done[s->ndone++];
+						c->id = p->id; c->user = p->req.user; c->kind = p->req.kind; c->volume = p->req.volume;
+						c->arrival = p->arrival; c->admitted = -1.0; c->finished = DN_server_clock(); c->ok = 0;
+					}
+					s->stats.completed++;
+					s->stats.failed++;
+					s->outstanding--;
+					free_pending(p);
+					p = n;
+				}
+				s->slots[i].head = s->slots[i].tail = NULL;
+			}
+			pthread_cond_broadcast(&s->cond);
+			pthread_mutex_unlock(&s->lock);
+		}
 		int progressed = 0;
 		if (s->tickCount < s->cfg.maxTicksInFlight && launch_tick(s) != 0) progressed = 1;
 		if (retire_tick(s, s->tickCount >= s->cfg.maxTicksInFlight)) progressed = 1;
@@ -481,6 +504,7 @@ void DN_server_destroy(DNserver* s)
 	if (s->started) {
 		pthread_mutex_lock(&s->lock);
 		s->stop = 1;
+		s->cancel = 1;
 		pthread_cond_broadcast(&s->cond);
 		pthread_mutex_unlock(&s->lock);
 		pthread_join(s->thread, NULL);

@@ -83,7 +83,8 @@ typedef struct DNserveStats
 } DNserveStats;
 
 DNserver* DN_server_create(const DNserveConfig* config);
-/* stops the serving thread (after draining) and frees the server; the volumes stay the caller's */
+/* stops the serving thread and frees the server: ticks in flight finish, requests still queued are
+ * dropped (call DN_server_drain first to serve them); the volumes stay the caller's, resident */
 void DN_server_destroy(DNserver* server);
 /* registers a device volume (it joins the server's batch); returns its index, or -1 */
 int DN_server_add_volume(DNserver* server, DNvolume* vol);
