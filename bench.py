@@ -253,7 +253,7 @@ def run_ours(args):
         "rays_per_step": rays_total / K,
         "wall_s": wall,
         "gpu_launches": int(allreduce_sum(pg, launches)),
-        "roofline": {"bound": "hbm", "kernel": "k_light+k_commit (DN_update_lighting)", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": "k_light_packet+k_commit (DN_update_lighting)", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": traffic, "algorithmic_bytes_per_launch": per_launch_bytes,
                      "launch_ms": per_launch_s * 1e3},
@@ -380,8 +380,10 @@ def run_batched(args):
         return tot
 
     # plain per-scene form
-    for _ in range(args.warmup):
+    for w in range(args.warmup):
+        t1 = time.perf_counter()
         plain_frame()
+        log("plain warm-up frame %d: %.2f s" % (w, time.perf_counter() - t1))
     for vol, *_ in maps:
         vol.reset_stats()
     lib.dn_cuda_device_sync()
@@ -390,17 +392,21 @@ def run_batched(args):
         plain_frame()
     plain_s = time.perf_counter() - t0
     pr = plain_rays()
+    log("plain: %d frames in %.2f s, %.3g rays" % (args.steps, plain_s, pr["rays"]))
 
     # batched form
     batch = dn.Batch([m[0] for m in maps])
     stream = batch.stream()
     for w in range(args.warmup):
+        t1 = time.perf_counter()
         batch.run(batch_items())
         frame[0] += 1
         assert batch.finish(), lib.dn_cuda_last_error().decode()
+        log("batched warm-up frame %d: %.2f s" % (w, time.perf_counter() - t1))
         if w == 0 and not args.no_autotune:
+            t1 = time.perf_counter()
             tuned = batch.autotune()
-            log("autotuned: %s" % tuned)
+            log("autotuned in %.2f s: %s" % (time.perf_counter() - t1, tuned))
     K = args.steps
     evs = []
     for _ in range(2 * K):

@@ -236,7 +236,20 @@ struct RayCtx {
     bool refraction;
     f3 orgRayPos;
     Counters c;
+    uint32_t segSteps;        // cells visited by the current step_map call (D16)
+    bool capped;
 };
+
+// D16: a traversal segment that has visited this many cells ends as a miss.  A ray whose direction has a
+// finite, non-zero component on every axis leaves the map long before (every DDA step advances one axis
+// monotonically: at most sx+sy+sz chunk cells and 24 voxel cells per chunk entered); the cap ends only
+// degenerate rays -- a direction component exactly zero or NaN makes the reference's side distances NaN
+// after one step (0 * inf), after which no axis may be stepped again and its loop would never end.
+__device__ __forceinline__ uint32_t step_cap(uint32_t sx, uint32_t sy, uint32_t sz)
+{
+    const uint64_t c = 256ull * ((uint64_t)sx + sy + sz) + 4096ull;
+    return c > (1ull << 23) ? (1u << 23) : (uint32_t)c;
+}
 
 // step_chunk, voxelShared.comp:328-418
 static __device__ __noinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapPos, uint32_t slot, uint32_t tile,
@@ -250,7 +263,10 @@ static __device__ __noinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapPos,
     refracted = false;
     i3 pos, step; f3 delta, side, lastSide = mk(0.0f, 0.0f, 0.0f);
     init_dda(rayDir, inv, rayPos, pos, delta, step, side);
+    const uint32_t cap = step_cap(m.sx, m.sy, m.sz);
     while (in_chunk(pos)) {
+        if (c.segSteps >= cap) { c.capped = true; return false; }
+        c.segSteps++;
         c.c.inner++;
         uint32_t li = (uint32_t)(pos.x + 8 * (pos.y + 8 * pos.z));
         bool exists = (__ldg(&r->mask[li >> 5]) >> (li & 31)) & 1u;
@@ -323,9 +339,14 @@ static __device__ __noinline__ bool step_map(RayCtx& c, TState& ts, f3& rayDir, 
     colorAdd = mk(0.0f, 0.0f, 0.0f);
     colorMult = 1.0f;
     c.c.rays++;
+    c.segSteps = 0;
+    c.capped = false;
+    const uint32_t cap = step_cap(m.sx, m.sy, m.sz);
     i3 pos, step; f3 delta, side, lastSide = mk(0.0f, 0.0f, 0.0f);
     init_dda(rayDir, inv, rayPos, pos, delta, step, side);
     while (in_map(m, pos)) {
+        if (c.segSteps >= cap) return false;
+        c.segSteps++;
         c.c.outer++;
         uint32_t t = map_index(m, pos);
         uint32_t w = __ldg(&m.tword[t]);
@@ -344,6 +365,7 @@ static __device__ __noinline__ bool step_map(RayCtx& c, TState& ts, f3& rayDir, 
                 rayPos = add(mk((float)pos.x, (float)pos.y, (float)pos.z), muls(cp, INV_CHUNK));
                 return true;
             }
+            if (c.capped) return false;
             if (refracted) {
                 rayPos = add(mk((float)pos.x, (float)pos.y, (float)pos.z), muls(cp, INV_CHUNK));
                 init_dda(rayDir, inv, rayPos, pos, delta, step, side);

@@ -53,7 +53,8 @@ struct Seg {
     f3 cside, clast, oside, olast, cp;
     const ChunkRec* rec;
     uint32_t base;
-    uint32_t flags;      // bit0 inner level, bit1 ignore (current level), bit2 saved outer ignore, bit3 requested
+    uint32_t flags;      // bit0 inner level, bit1 ignore (current level), bit2 saved outer ignore, bit3 requested,
+                         // bits 8-31 cells visited by the segment (D16 step cap)
     f3 cadd;
     float cmul;
     TState ts;
@@ -84,6 +85,12 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
     const bool inner = (s.flags & 1u) != 0u;
     const uint32_t bx = inner ? 8u : m.sx, by = inner ? 8u : m.sy, bz = inner ? 8u : m.sz;
     const bool inb = (uint32_t)s.cpos.x < bx && (uint32_t)s.cpos.y < by && (uint32_t)s.cpos.z < bz;
+    // D16: every visited cell (each outer or inner iteration of step_map / step_chunk) counts; a segment
+    // that reached the cap ends as a miss
+    if (inb) {
+        if ((s.flags >> 8) >= step_cap(m.sx, m.sy, m.sz)) return 2u;
+        s.flags += 256u;
+    }
     const uint32_t idx = (uint32_t)s.cpos.x + bx * ((uint32_t)s.cpos.y + by * (uint32_t)s.cpos.z);
     uint32_t w = 0;
     if (inb) w = __ldg(inner ? &s.rec->mask[idx >> 5] : &m.tbits[idx >> 4]);

@@ -361,7 +361,19 @@ typedef struct ctx {
     int refraction;
     v3 orgRayPos;
     dno_counters c;
+    uint32_t segSteps;  /* cells visited by the current step_map call (D16) */
+    int capped;
 } ctx;
+
+/* D16: a step_map call that has visited this many cells (outer plus inner iterations) ends as a miss.
+ * Rays with a finite, non-zero direction component on every axis leave the map long before; only
+ * degenerate rays (a zero or NaN component: 0 * inf makes a side distance NaN, after which the
+ * reference's loop never ends) reach it. */
+static inline uint32_t step_cap(uint32_t sx, uint32_t sy, uint32_t sz)
+{
+    uint64_t c = 256ull * ((uint64_t)sx + sy + sz) + 4096ull;
+    return c > (1ull << 23) ? (1u << 23) : (uint32_t)c;
+}
 
 static inline void store_u8(uint8_t* p, uint8_t v) { __atomic_store_n(p, v, __ATOMIC_RELAXED); }
 static inline uint8_t load_u8(const uint8_t* p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
@@ -473,7 +485,10 @@ static int step_chunk(ctx* c, tstate* ts, iv3 mapPos, uint32_t tile, v3* rayDir,
     *refracted = 0;
     iv3 pos, step; v3 delta, side, lastSide = V(0.0f, 0.0f, 0.0f);
     init_dda(*rayDir, *inv, *rayPos, &pos, &delta, &step, &side);
+    const uint32_t cap = step_cap(c->m->sx, c->m->sy, c->m->sz);
     while (in_chunk(pos)) {
+        if (c->segSteps >= cap) { c->capped = 1; return 0; }
+        c->segSteps++;
         c->c.innerSteps++;
         if (vox_exists(r, pos) && !ignoreFirst) {
             uint32_t rank = vox_rank(r, pos);
@@ -542,9 +557,14 @@ static int step_map(ctx* c, tstate* ts, v3* rayDir, v3 inv, v3* rayPos, int igno
     *colorAdd = V(0.0f, 0.0f, 0.0f);
     *colorMult = 1.0f;
     c->c.rays++;
+    c->segSteps = 0;
+    c->capped = 0;
+    const uint32_t cap = step_cap(m->sx, m->sy, m->sz);
     iv3 pos, step; v3 delta, side, lastSide = V(0.0f, 0.0f, 0.0f);
     init_dda(*rayDir, inv, *rayPos, &pos, &delta, &step, &side);
     while (in_map(m, pos)) {
+        if (c->segSteps >= cap) return 0;
+        c->segSteps++;
         c->c.outerSteps++;
         uint32_t t = map_index(m, pos);
         uint8_t st = load_u8(&m->state[t]);
@@ -562,6 +582,7 @@ static int step_map(ctx* c, tstate* ts, v3* rayDir, v3 inv, v3* rayPos, int igno
                 *rayPos = vadd(V((float)pos.x, (float)pos.y, (float)pos.z), vmuls(cp, INV_CHUNK));
                 return 1;
             }
+            if (c->capped) return 0;
             if (refracted) {
                 *rayPos = vadd(V((float)pos.x, (float)pos.y, (float)pos.z), vmuls(cp, INV_CHUNK));
                 init_dda(*rayDir, inv, *rayPos, &pos, &delta, &step, &side);

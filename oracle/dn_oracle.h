@@ -21,7 +21,7 @@
  * deterministic sine rather than a GPU's.
  *
  * Deterministic semantics where the reference races or is undefined
- * (numbered D1..D15, each applied identically here and in the kernels):
+ * (numbered D1..D16, each applied identically here and in the kernels):
  *   D1  lighting reads the previous frame's committed lighting; results are
  *       committed after the whole launch (reference reads/writes in place,
  *       voxelLighting.comp:113,122 vs 276-278).
@@ -69,6 +69,12 @@
  *       0xFFFFFFFF on a miss.
  *   D15 the GLSL <= multi-axis tie step (voxelShared.comp:313) is
  *       authoritative; the CPU picking ray keeps its own strict < (voxel.c:1241).
+ *   D16 a traversal segment (one step_map call) that has visited
+ *       256 * (sx + sy + sz) + 4096 cells (outer plus inner iterations, at
+ *       most 2^23) ends as a miss.  Ordinary rays leave the map long before;
+ *       a zero or NaN direction component makes a side distance NaN
+ *       (0 * inf) after one step, after which the reference's loop
+ *       (voxelShared.comp:339, 435) would never end.
  */
 #ifndef DN_ORACLE_H
 #define DN_ORACLE_H

@@ -182,3 +182,61 @@ def test_camera_inside_map_and_host_image(gpu_ready):
         host.close()
     finally:
         pair.close()
+
+
+class _DrawParams(__import__("ctypes").Structure):
+    """dn_draw_params of include/dn_cuda.h"""
+    import ctypes as _c
+    _fields_ = [("origin", _c.c_float * 3), ("dirMat", (_c.c_float * 4) * 4), ("width", _c.c_uint32),
+                ("height", _c.c_uint32), ("viewMode", _c.c_uint32), ("truncate16", _c.c_uint32),
+                ("sunStrength", _c.c_float * 3), ("skyBot", _c.c_float * 3), ("skyTop", _c.c_float * 3),
+                ("emissiveStrength", _c.c_float)]
+
+
+def test_degenerate_ray_is_capped(gpu_ready):
+    """A primary ray whose direction has an exactly zero x component: normalize((-1e-4, 0.6, 0.8)) + EPS
+    gives x = 0 in float32, so the DDA's x side distance becomes 0 * inf = NaN after one step and the
+    reference's loop could never finish.  Both sides end it as a miss after the D16 step cap, with the
+    same pixels and the same counters."""
+    import ctypes
+    from doonengine_gb300 import _lib
+    lib = dn.load()
+    pair = Pair("tiny")
+    try:
+        pair.sync()                       # load the chunks so the ray walks through loaded ones too
+        W, H = 8, 4
+        iv, icv, ip = _lib.DNmat4(), _lib.DNmat4(), _lib.DNmat4()
+        for c in range(4):
+            icv.m[c][c] = 1.0
+            iv.m[c][c] = 1.0
+        iv.m[3][0], iv.m[3][1], iv.m[3][2] = 2.5, 1.5, 2.5           # camera inside the map (chunk units)
+        ip.m[3][0], ip.m[3][1], ip.m[3][2], ip.m[3][3] = -1e-4, 0.6, 0.8, 1.0
+        M = lib.DN_mat4_mult(icv, ip)
+        p = _DrawParams()
+        p.origin[:] = [2.5, 1.5, 2.5]
+        for c in range(4):
+            for r in range(4):
+                p.dirMat[c][r] = M.m[c][r]
+        p.width, p.height = W, H
+        s = pair.vol.s
+        p.sunStrength[:] = s.sunStrength.tolist()
+        p.skyBot[:] = s.skyGradientBot.tolist()
+        p.skyTop[:] = s.skyGradientTop.tolist()
+        p.emissiveStrength = s.emissiveStrength
+        img = dn.Image(W, H, on_device=True)
+        pair.vol.reset_stats()
+        assert lib.dn_cuda_draw(s.gpu, ctypes.byref(p), ctypes.cast(s.materials, ctypes.c_void_p),
+                                ctypes.cast(img.ptr.contents.color, ctypes.c_void_p),
+                                ctypes.cast(img.ptr.contents.hitIndex, ctypes.c_void_p),
+                                ctypes.cast(img.ptr.contents.hitFace, ctypes.c_void_p)) == 0
+        assert pair.vol.finish()
+        gpu = img.numpy()
+        ora = pair.om.draw(s, iv, icv, ip, W, H)
+        compare_draw(gpu, ora, "degenerate ray")
+        st = pair.vol.stats_kind(1)
+        sx, sy, sz = pair.vol.map_size
+        cap = 256 * (sx + sy + sz) + 4096
+        assert st["outerSteps"] + st["innerSteps"] == W * H * cap, st     # every pixel's ray reached the cap
+        img.close()
+    finally:
+        pair.close()
