@@ -199,8 +199,9 @@ extern "C" int dn_cuda_batch_create(DNgpuBatch** out)
     b->workCounter = nullptr; b->bst = nullptr; b->hbst = nullptr; b->lsave = nullptr;
     b->dsts = nullptr; b->dstsCap = 0; b->stsDirty = true; b->dgather = nullptr; b->hgather = nullptr;
     b->gatherCount = 0;
-    b->tuning.streamBatch = g_streamBatch; b->tuning.blocksPerSM = DN_STREAM_MIN_BLOCKS; b->tuning.useGraph = 1;
     b->tuning.kernel = g_lightKernel == 2 ? 2u : 1u;
+    b->tuning.streamBatch = b->tuning.kernel == 2u ? g_packetBatch : g_streamBatch;
+    b->tuning.blocksPerSM = DN_STREAM_MIN_BLOCKS; b->tuning.useGraph = 1;
     b->lastPackets = false;
     b->graph = nullptr;
     b->lastLightValid = false;
@@ -696,12 +697,16 @@ extern "C" int dn_cuda_batch_autotune(DNgpuBatch* b, dn_batch_tuning* chosen)
         if (!rc && ms < bestMs) { bestMs = ms; best = t; }
         return ms;
     };
-    // coordinate descent: kernel, stream batch (ray streams only), then resident blocks per SM
+    // coordinate descent: kernel, batch threshold, then resident blocks per SM
     trial(keep);
-    { dn_batch_tuning t = best; t.kernel = 3u - t.kernel; if (!rc && (t.kernel == 1u || packetsOk)) trial(t); }
-    const uint32_t batches[] = {12u, 16u, 20u, 24u, 28u, 32u};
-    if (best.kernel == 1u)
-        for (uint32_t sb : batches) { dn_batch_tuning t = best; t.streamBatch = sb; if (!rc) trial(t); }
+    {
+        dn_batch_tuning t = best;
+        t.kernel = 3u - t.kernel;
+        t.streamBatch = t.kernel == 2u ? g_packetBatch : g_streamBatch;
+        if (!rc && (t.kernel == 1u || packetsOk)) trial(t);
+    }
+    const uint32_t batches[] = {4u, 8u, 12u, 16u, 20u, 24u, 28u, 32u};
+    for (uint32_t sb : batches) { dn_batch_tuning t = best; t.streamBatch = sb; if (!rc) trial(t); }
     for (uint32_t bps = 2; bps <= (uint32_t)b->maxBlocksPerSM && bps <= 6; bps++) {
         dn_batch_tuning t = best; t.blocksPerSM = bps; if (!rc) trial(t);
     }

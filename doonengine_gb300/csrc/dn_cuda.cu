@@ -74,6 +74,7 @@ extern "C" uint64_t dn_cuda_launch_count(void) { return __atomic_load_n(&g_launc
 // 2 warp packets of ray fans; DN_STREAM_BATCH lanes, 1..32), read once at init
 int g_lightKernel = 2;
 uint32_t g_streamBatch = 24;
+uint32_t g_packetBatch = 12;   // lanes with an ended segment before the packet kernel shades (measured best)
 
 extern "C" int dn_cuda_init(int device)
 {
@@ -81,6 +82,10 @@ extern "C" int dn_cuda_init(int device)
     if (const char* e = getenv("DN_STREAM_BATCH")) {
         int b = atoi(e);
         g_streamBatch = (uint32_t)(b < 1 ? 1 : (b > 32 ? 32 : b));
+    }
+    if (const char* e = getenv("DN_PACKET_BATCH")) {
+        int b = atoi(e);
+        g_packetBatch = (uint32_t)(b < 1 ? 1 : (b > 32 ? 32 : b));
     }
     int n = 0;
     cudaError_t e = cudaGetDeviceCount(&n);
@@ -467,18 +472,20 @@ __global__ void __launch_bounds__(128, DN_PACKET_MIN_BLOCKS) k_light_packet(cons
 }
 
 // launches the lighting kernel g_lightKernel selects (1 ray streams, 2 warp packets; packets need
-// specBounceLimit <= PK_MAX_SPEC_SEGMENTS and fall back to streams otherwise)
-static int launch_light(DNgpuVolume* g, const StreamArgs& a)
+// specBounceLimit <= PK_MAX_SPEC_SEGMENTS and fall back to streams otherwise) with its batch threshold
+static int launch_light(DNgpuVolume* g, StreamArgs& a)
 {
     int perSM = 0;
     if (g_lightKernel == 2 && a.p.specBounceLimit <= PK_MAX_SPEC_SEGMENTS) {
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_packet, 128, 0));
         if (perSM < 1) perSM = 1;
+        a.batch = g_packetBatch;
         COUNT_LAUNCH();
         k_light_packet<<<g->numSMs * perSM, 128, 0, g->stream>>>(a);
     } else {
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_stream, 128, 0));
         if (perSM < 1) perSM = 1;
+        a.batch = g_streamBatch;
         COUNT_LAUNCH();
         k_light_stream<<<g->numSMs * perSM, 128, 0, g->stream>>>(a);
     }

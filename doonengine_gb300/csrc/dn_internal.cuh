@@ -66,7 +66,8 @@ extern int g_device;
 extern int g_numSMs;
 extern unsigned long long g_launches;   // kernels launched by this library (all threads)
 extern int g_lightKernel;               // 0 lockstep, 1 per-lane ray streams, 2 warp packets (default)
-extern uint32_t g_streamBatch;          // lanes that wait before per-segment work runs (1..32)
+extern uint32_t g_streamBatch;          // lanes that wait before per-segment work runs (1..32), ray streams
+extern uint32_t g_packetBatch;          // the same threshold for the packet kernel's ray pools
 #define COUNT_LAUNCH() __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED)
 
 template <class T> static int dalloc(T** p, size_t count)

@@ -37,10 +37,14 @@ struct PacketVoxel {
 };
 enum : uint32_t { PV_VALID = 1u, PV_FIRST = 2u, PV_SPEC = 4u, PV_DIFF = 8u };
 
+constexpr uint32_t PK_POOL_FAN = 64;          // rays per fan kind in one pool: voxels per pool = 64 / K
+
 struct PacketWarp {
     PacketVoxel v[32];
-    float con[32][PK_MAX_SPEC_SEGMENTS][3];   // specular contributions of each lane's ray, in segment order
-    uint32_t ncon[32];
+    float con[PK_POOL_FAN][PK_MAX_SPEC_SEGMENTS][3];   // specular contributions of each pooled ray, in segment order
+    float sh[PK_POOL_FAN][3];                          // shadow contribution of each pooled ray
+    uint8_t ncon[PK_POOL_FAN];                         // contributions of each specular ray
+    uint8_t shHas[PK_POOL_FAN];                        // the shadow ray was unoccluded
 };
 
 // sets up voxel (req, lane) of the group (voxel_setup of dn_light_stream.cuh); invalid slots get zero output
@@ -118,13 +122,13 @@ __device__ __forceinline__ int pass_voxel(uint32_t mask, uint32_t base, uint32_t
     return __ffs(mm) - 1;
 }
 
-enum : uint32_t { PP_SPEC = 0, PP_FIRST = 1, PP_FAN = 2, PP_DIFF = 3, PP_DONE = 4 };
-
-// The request groups of one launch.  Per group the warp runs four passes -- specular fans, first-sample
-// shadow rays, shadow fans, diffuse paths -- as a state machine around a single stepping loop: each pass
-// unit (a pack of voxels for the fans, all voxels for the others) starts one segment per lane, the lanes
-// step together until every segment ended, the pass shades the ended segments and starts follow-up
-// segments, and when no lane has work the unit's sums are formed and the next unit starts.
+// The request groups of one launch.  Per group: (1) pools of 64/K voxels (at least one): every ray of their
+// specular fans, first-sample shadow rays and shadow fans is traced by whichever lane is free -- a lane
+// takes the pool's next ray as soon as its own ended, and the shading of ended segments runs once `batch`
+// lanes have one, so no lane waits for the slowest ray of a fan; each ray's contributions go to shared
+// memory, and when the pool is empty every voxel's sums are formed in the reference's order; (2) the
+// diffuse paths, one lane per voxel; (3) the running average and the write-out.  One stepping loop
+// serves both traced phases.
 template <bool MANY>
 __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLightArgs* many, const StreamShared* sh,
                                             PacketWarp& W)
@@ -134,6 +138,7 @@ __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLi
     if constexpr (MANY) nreq = *(volatile const uint32_t*)&many->reqStart[many->nmaps];
     else nreq = *(volatile const uint32_t*)one->nreqPtr;
     uint32_t* const counter = MANY ? many->workCounter : one->workCounter;
+    const uint32_t batch = MANY ? many->batch : one->batch;
     Counters c{0, 0, 0, 0, 0};
     uint32_t lit = 0;
     for (;;) {
@@ -167,282 +172,298 @@ __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLi
         packet_setup(W.v[lane], req, lane, m, p, mats, MANY ? e->reqs : one->reqs, MANY ? e->nsamples : one->nsamples, out);
         __syncwarp();
         const uint32_t myFlags = W.v[lane].flags;
-        const uint32_t rounds = K <= 32u ? 1u : (K + 31u) / 32u;
-        const uint32_t vpp = K <= 32u ? 32u / K : 1u;
         const uint32_t specAll = __ballot_sync(0xFFFFFFFFu, (myFlags & (PV_VALID | PV_SPEC)) == (PV_VALID | PV_SPEC));
         const uint32_t specMask = p.specBounceLimit > 0u ? specAll : 0u;
         // no specular segments: the sum stays zero and is still divided by K
         if (!specMask && ((specAll >> lane) & 1u)) W.v[lane].spec = divs(mk(0.0f, 0.0f, 0.0f), (float)K);
         const uint32_t diffMask = __ballot_sync(0xFFFFFFFFu, (myFlags & (PV_VALID | PV_DIFF)) == (PV_VALID | PV_DIFF));
         const uint32_t firstMask = diffMask & __ballot_sync(0xFFFFFFFFu, (myFlags & PV_FIRST) != 0u);
-        const uint32_t fanMask = diffMask & ~firstMask;
-        const uint32_t nSpec = (uint32_t)__popc(specMask), nFan = (uint32_t)__popc(fanMask);
+        const uint32_t workMask = specMask | diffMask;
+        const uint32_t nWork = (uint32_t)__popc(workMask);
+        const uint32_t perPool = K < PK_POOL_FAN ? PK_POOL_FAN / K : 1u;
 
-        // per-lane state, shared by the passes
+        // per-lane ray state
         Seg s;
         uint32_t hs = 0, hitIdx = 0;
         bool live = false, stepping = false;
-        int vi = -1;                 // voxel of this lane's ray in the current unit
-        uint32_t kk = 0, sg = 0;     // ray index, segment of the pack
-        f3 pacc = mk(0.0f, 0.0f, 0.0f), cc = pacc;
-        uint32_t pi = 0, ncon = 0;
-        bool has = false;
-        // the ray job's state: specular mult / last position / reflect type / bounce, or diffuse_dir's view of
-        // this lane's path (lane == voxel in the diffuse pass)
-        Job jd;
+        uint32_t rid = 0, ncon = 0;       // the lane's ray: index in its fan array; contributions so far
+        bool isSpec = false;
+        int vi = -1;                      // the ray's voxel
+        Job jd;                           // specular: jA mult, jB last position, jU reflect type, b bounce
 
-        uint32_t pass = PP_SPEC, base = 0, round = 0;
-        bool unitOpen = false;
-        for (int guard = 0; guard < (1 << 30); guard++) {
-            if (!__any_sync(0xFFFFFFFFu, live)) {
-                // ---- close the unit: ordered sums
-                if (unitOpen) {
-                    if (pass == PP_SPEC) {
-                        W.ncon[lane] = vi >= 0 ? ncon : 0u;
-                        __syncwarp();
-                        if (vi >= 0) {
-                            const uint32_t nk = K <= 32u ? K : ((K - 32u * round) < 32u ? (K - 32u * round) : 32u);
-                            for (uint32_t k2 = 0; k2 < nk; k2++) {
-                                const uint32_t src = K <= 32u ? sg * K + k2 : k2;
-                                const uint32_t n = W.ncon[src];
-                                for (uint32_t jj = 0; jj < n; jj++) {
-                                    pacc.x = pacc.x + W.con[src][jj][0];
-                                    pacc.y = pacc.y + W.con[src][jj][1];
-                                    pacc.z = pacc.z + W.con[src][jj][2];
-                                }
-                            }
-                        }
-                        __syncwarp();
-                        if (round + 1u == rounds && vi >= 0 && (K > 32u ? lane == 0u : lane == sg * K))
-                            W.v[vi].spec = divs(pacc, (float)K);
-                    } else if (pass == PP_FIRST) {
-                        if ((firstMask >> lane) & 1u) W.v[lane].direct = divs(pacc, 1.0f);
-                    } else if (pass == PP_FAN) {
-                        const uint32_t hasMask = __ballot_sync(0xFFFFFFFFu, has);
-                        const uint32_t nk = K <= 32u ? K : ((K - 32u * round) < 32u ? (K - 32u * round) : 32u);
-                        for (uint32_t k2 = 0; k2 < nk; k2++) {
-                            const uint32_t src = K <= 32u ? sg * K + k2 : k2;
-                            const float x = __shfl_sync(0xFFFFFFFFu, cc.x, src);
-                            const float y = __shfl_sync(0xFFFFFFFFu, cc.y, src);
-                            const float z = __shfl_sync(0xFFFFFFFFu, cc.z, src);
-                            if (vi >= 0 && ((hasMask >> src) & 1u)) { pacc.x = pacc.x + x; pacc.y = pacc.y + y; pacc.z = pacc.z + z; }
-                        }
-                        if (round + 1u == rounds && vi >= 0 && (K > 32u ? lane == 0u : lane == sg * K))
-                            W.v[vi].direct = divs(pacc, (float)K);
-                    } else {
-                        break;                 // the diffuse unit is the last
-                    }
-                    __syncwarp();
-                    // ---- next unit
-                    if (++round >= ((pass == PP_SPEC || pass == PP_FAN) ? rounds : 1u)) {
-                        round = 0;
-                        base += (pass == PP_SPEC || pass == PP_FAN) ? vpp : 32u;
-                    }
-                }
-                // skip finished or empty passes
-                for (;;) {
-                    const uint32_t nUnits = pass == PP_SPEC ? nSpec : pass == PP_FIRST ? (firstMask ? 1u : 0u)
-                                          : pass == PP_FAN ? nFan : (diffMask ? 1u : 0u);
-                    if (pass == PP_DONE || base < ((pass == PP_SPEC || pass == PP_FAN) ? nUnits : nUnits * 32u)) break;
-                    pass++;
-                    base = 0;
-                    round = 0;
-                }
-                if (pass == PP_DONE) break;
-                unitOpen = true;
-                // ---- open the unit: one segment per lane
-                live = false;
-                hs = 0;
-                vi = -1;
-                if (pass == PP_SPEC || pass == PP_FAN) {
-                    vi = pass_voxel(pass == PP_SPEC ? specMask : fanMask, base, K, lane, round, kk, sg);
-                    if (round == 0u) pacc = mk(0.0f, 0.0f, 0.0f);
-                    has = false;
-                    cc = mk(0.0f, 0.0f, 0.0f);
-                    if (vi >= 0) {
-                        const PacketVoxel& pv = W.v[vi];
-                        if (pass == PP_SPEC) {
+        // ---- (1) pools of specular and shadow fans
+        for (uint32_t base = 0; base < nWork; base += perPool) {
+            // the pool's voxels: slots j < np of workMask, from bit 'base' on; ray layout:
+            // [specular rays of voxel 0, 1, ...] then [shadow rays of voxel 0, 1, ...]
+            uint32_t rest = workMask;
+            for (uint32_t t = 0; t < base; t++) rest &= rest - 1u;
+            const uint32_t np = (nWork - base) < perPool ? (nWork - base) : perPool;
+            uint32_t poolMask = 0, rm = rest;
+            for (uint32_t t = 0; t < np; t++) { poolMask |= rm & (0u - rm); rm &= rm - 1u; }
+            const uint32_t nSpecRays = (uint32_t)__popc(poolMask & specMask) * K;
+            const uint32_t nFanVox = (uint32_t)__popc(poolMask & diffMask & ~firstMask);
+            const uint32_t nFirst = (uint32_t)__popc(poolMask & firstMask);
+            const uint32_t nShRays = nFanVox * K + nFirst;   // shadow rays in voxel order (1 or K per voxel)
+            const uint32_t total = nSpecRays + nShRays;
+            uint32_t next = 0;
+            for (int guard = 0; guard < (1 << 30); guard++) {
+                // lanes without a ray take the pool's next rays in order
+                const unsigned need = __ballot_sync(0xFFFFFFFFu, !live);
+                if (next < total && need) {
+                    const uint32_t rank = __popc(need & ((1u << lane) - 1u));
+                    if (!live && next + rank < total) {
+                        const uint32_t q = next + rank;
+                        if (q < nSpecRays) {
+                            // specular ray kk of the pool's (q / K)-th specular voxel
+                            isSpec = true;
+                            rid = q;
+                            const uint32_t kk = q % K;
+                            uint32_t mm = poolMask & specMask;
+                            for (uint32_t t = 0; t < q / K; t++) mm &= mm - 1u;
+                            vi = __ffs(mm) - 1;
+                            const PacketVoxel& pv = W.v[vi];
                             const Material& tm = mats[pv.tmat];
                             jd.jA = pv.talbedo; jd.jB = pv.pos0; jd.jU = tm.reflectType; jd.b = 0; ncon = 0;
                             const f3 P = mk(p.spherePts[kk][0], p.spherePts[kk][1], p.spherePts[kk][2]);
                             const f3 sd = adds(normalize(add(muls(pv.refl, (float)tm.shininess), P)), EPS);
                             seg_begin(s, pv.pos0, sd, rcp3(sd));
                         } else {
-                            seg_begin(s, pv.pos0, mk(sdir[kk][0], sdir[kk][1], sdir[kk][2]),
+                            // shadow ray: voxels of the pool in slot order, K rays each (1 on the first sample)
+                            isSpec = false;
+                            rid = q - nSpecRays;
+                            uint32_t mm = poolMask & diffMask, off = 0, kk = 0;
+                            vi = -1;
+                            while (mm) {
+                                const int v = __ffs(mm) - 1;
+                                mm &= mm - 1u;
+                                const uint32_t n = ((firstMask >> v) & 1u) ? 1u : K;
+                                if (rid < off + n) { vi = v; kk = ((firstMask >> v) & 1u) ? 64u : rid - off; break; }
+                                off += n;
+                            }
+                            seg_begin(s, W.v[vi].pos0, mk(sdir[kk][0], sdir[kk][1], sdir[kk][2]),
                                       mk(sinv[kk][0], sinv[kk][1], sinv[kk][2]));
                         }
                         c.rays++;
                         live = true;
+                        stepping = true;
+                        hs = 0;
                     }
-                } else if (pass == PP_FIRST) {
-                    pacc = mk(0.0f, 0.0f, 0.0f);
-                    if ((firstMask >> lane) & 1u) {
-                        seg_begin(s, W.v[lane].pos0, mk(sdir[64][0], sdir[64][1], sdir[64][2]),
-                                  mk(sinv[64][0], sinv[64][1], sinv[64][2]));
-                        c.rays++;
-                        live = true;
-                    }
-                } else {
-                    // diffuse: lane = voxel; the first path's first segment (or the paths without segments)
-                    pacc = mk(0.0f, 0.0f, 0.0f);
-                    if ((diffMask >> lane) & 1u) {
-                        const PacketVoxel& pv = W.v[lane];
-                        jd.key = pv.key; jd.tnormal = pv.tnormal; jd.tmat = pv.tmat;
-                        jd.firstSample = (pv.flags & PV_FIRST) != 0u;
-                        pi = 0;
-                        live = true;
-                        hs = 3u;             // "start the next path" (see the shading below)
+                    next = (next + (uint32_t)__popc(need)) < total ? next + (uint32_t)__popc(need) : total;
+                }
+                if (!__any_sync(0xFFFFFFFFu, live)) break;
+                // step until 'batch' lanes have an ended segment (or none is left stepping)
+                for (;;) {
+                    const unsigned st = __ballot_sync(0xFFFFFFFFu, stepping);
+                    if (!st) break;
+                    if ((uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, live && !stepping)) >= batch) break;
+                    if (stepping) {
+                        const uint32_t rr = seg_step(s, m, mats, p.sunStrength, c, hitIdx);
+                        if (rr) { stepping = false; hs = rr; }
                     }
                 }
-                stepping = live && hs == 0u;
-            }
-            // ---- step every started segment to its end (the single stepping loop)
-            while (__any_sync(0xFFFFFFFFu, stepping)) {
-                if (stepping) {
-                    const uint32_t rr = seg_step(s, m, mats, p.sunStrength, c, hitIdx);
-                    if (rr) { stepping = false; hs = rr; }
-                }
-            }
-            // ---- shade the ended segments
-            if (!live || hs == 0u) continue;
-            if (pass == PP_SPEC) {
-                // specular_ray body after step_map (voxelLighting.comp:98-144)
-                const PacketVoxel& pv = W.v[vi];
-                bool more = false, add_ = false;
-                f3 sc = mk(0.0f, 0.0f, 0.0f);
-                if (hs == 1u) {
-                    Voxel hv;
-                    decompress(m, hitIdx, hv);
-                    const i3 hp{f2i(truncf(s.pos.x)), f2i(truncf(s.pos.y)), f2i(truncf(s.pos.z))};
-                    if (in_map(m, hp)) {
-                        uint8_t* vp = &m.tvis[map_index(m, hp)];
-                        if (*vp == 0) *vp = 1;
-                    }
-                    const f3 d = vabs(sub(vfloor(muls(s.pos, 8.0f)), vfloor(muls(jd.jB, 8.0f))));
-                    if (!(dot(d, d) <= 1.0f)) {
-                        const Material& hm = mats[hv.material];
-                        const f3 hd = muls(hv.diff, 1.0f - hm.specular);
-                        add_ = true;
-                        if (hm.emissive) {
-                            sc.x = ((hv.albedo.x * p.emissiveStrength * s.cmul + s.cadd.x) * jd.jA.x) * pv.talbedo.x;
-                            sc.y = ((hv.albedo.y * p.emissiveStrength * s.cmul + s.cadd.y) * jd.jA.y) * pv.talbedo.y;
-                            sc.z = ((hv.albedo.z * p.emissiveStrength * s.cmul + s.cadd.z) * jd.jA.z) * pv.talbedo.z;
-                        } else {
-                            const f3 hc = mul(hd, hv.albedo);
-                            sc.x = (hc.x * s.cmul + s.cadd.x) * jd.jA.x;
-                            sc.y = (hc.y * s.cmul + s.cadd.y) * jd.jA.y;
-                            sc.z = (hc.z * s.cmul + s.cadd.z) * jd.jA.z;
-                            if (hm.specular != 0.0f) {
-                                jd.jA.x = jd.jA.x * (hv.albedo.x * s.cmul * hm.specular);
-                                jd.jA.y = jd.jA.y * (hv.albedo.y * s.cmul * hm.specular);
-                                jd.jA.z = jd.jA.z * (hv.albedo.z * s.cmul * hm.specular);
-                                jd.jU = hm.reflectType;
-                                jd.jB = s.pos;
-                                const f3 nd = reflect(s.dir, hv.normal);
-                                jd.b++;
-                                if (jd.b < p.specBounceLimit) {
-                                    const TState keep = s.ts;
-                                    seg_begin(s, s.pos, nd, rcp3(nd));
-                                    s.ts = keep;   // one ray job: bounces keep the transparency state
-                                    c.rays++;
-                                    more = true;
+                // shade the ended segments
+                if (!live || stepping) continue;
+                if (isSpec) {
+                    // specular_ray body after step_map (voxelLighting.comp:98-144)
+                    const PacketVoxel& pv = W.v[vi];
+                    bool more = false, add_ = false;
+                    f3 sc = mk(0.0f, 0.0f, 0.0f);
+                    if (hs == 1u) {
+                        Voxel hv;
+                        decompress(m, hitIdx, hv);
+                        const i3 hp{f2i(truncf(s.pos.x)), f2i(truncf(s.pos.y)), f2i(truncf(s.pos.z))};
+                        if (in_map(m, hp)) {
+                            uint8_t* vp = &m.tvis[map_index(m, hp)];
+                            if (*vp == 0) *vp = 1;
+                        }
+                        const f3 d = vabs(sub(vfloor(muls(s.pos, 8.0f)), vfloor(muls(jd.jB, 8.0f))));
+                        if (!(dot(d, d) <= 1.0f)) {
+                            const Material& hm = mats[hv.material];
+                            const f3 hd = muls(hv.diff, 1.0f - hm.specular);
+                            add_ = true;
+                            if (hm.emissive) {
+                                sc.x = ((hv.albedo.x * p.emissiveStrength * s.cmul + s.cadd.x) * jd.jA.x) * pv.talbedo.x;
+                                sc.y = ((hv.albedo.y * p.emissiveStrength * s.cmul + s.cadd.y) * jd.jA.y) * pv.talbedo.y;
+                                sc.z = ((hv.albedo.z * p.emissiveStrength * s.cmul + s.cadd.z) * jd.jA.z) * pv.talbedo.z;
+                            } else {
+                                const f3 hc = mul(hd, hv.albedo);
+                                sc.x = (hc.x * s.cmul + s.cadd.x) * jd.jA.x;
+                                sc.y = (hc.y * s.cmul + s.cadd.y) * jd.jA.y;
+                                sc.z = (hc.z * s.cmul + s.cadd.z) * jd.jA.z;
+                                if (hm.specular != 0.0f) {
+                                    jd.jA.x = jd.jA.x * (hv.albedo.x * s.cmul * hm.specular);
+                                    jd.jA.y = jd.jA.y * (hv.albedo.y * s.cmul * hm.specular);
+                                    jd.jA.z = jd.jA.z * (hv.albedo.z * s.cmul * hm.specular);
+                                    jd.jU = hm.reflectType;
+                                    jd.jB = s.pos;
+                                    const f3 nd = reflect(s.dir, hv.normal);
+                                    jd.b++;
+                                    if (jd.b < p.specBounceLimit) {
+                                        const TState keep = s.ts;
+                                        seg_begin(s, s.pos, nd, rcp3(nd));
+                                        s.ts = keep;   // one ray job: bounces keep the transparency state
+                                        c.rays++;
+                                        more = true;
+                                    }
                                 }
                             }
                         }
+                    } else if (dot(s.dir, sunDir) > 0.99f) {
+                        add_ = true;
+                        sc.x = sun.x * s.cmul + s.cadd.x;
+                        sc.y = sun.y * s.cmul + s.cadd.y;
+                        sc.z = sun.z * s.cmul + s.cadd.z;
+                    } else {
+                        const f3 sky = (jd.jU == 1u) ? sky_color(mk(p.skyBot[0], p.skyBot[1], p.skyBot[2]),
+                                                                mk(p.skyTop[0], p.skyTop[1], p.skyTop[2]), s.dir) : sun;
+                        add_ = true;
+                        sc.x = (sky.x * s.cmul + s.cadd.x) * jd.jA.x;
+                        sc.y = (sky.y * s.cmul + s.cadd.y) * jd.jA.y;
+                        sc.z = (sky.z * s.cmul + s.cadd.z) * jd.jA.z;
                     }
-                } else if (dot(s.dir, sunDir) > 0.99f) {
-                    add_ = true;
-                    sc.x = sun.x * s.cmul + s.cadd.x;
-                    sc.y = sun.y * s.cmul + s.cadd.y;
-                    sc.z = sun.z * s.cmul + s.cadd.z;
+                    if (add_ && ncon < PK_MAX_SPEC_SEGMENTS) {   // at most one per segment; the host checks the limit
+                        W.con[rid][ncon][0] = sc.x; W.con[rid][ncon][1] = sc.y; W.con[rid][ncon][2] = sc.z;
+                        ncon++;
+                    }
+                    hs = 0;
+                    if (more) stepping = true;
+                    else { W.ncon[rid] = (uint8_t)ncon; live = false; }
                 } else {
-                    const f3 sky = (jd.jU == 1u) ? sky_color(mk(p.skyBot[0], p.skyBot[1], p.skyBot[2]),
-                                                         mk(p.skyTop[0], p.skyTop[1], p.skyTop[2]), s.dir) : sun;
-                    add_ = true;
-                    sc.x = (sky.x * s.cmul + s.cadd.x) * jd.jA.x;
-                    sc.y = (sky.y * s.cmul + s.cadd.y) * jd.jA.y;
-                    sc.z = (sky.z * s.cmul + s.cadd.z) * jd.jA.z;
+                    // shadow_ray: an unoccluded ray adds sunStrength * colorMult + colorAdd
+                    const bool miss = hs == 2u;
+                    W.sh[rid][0] = sun.x * s.cmul + s.cadd.x;
+                    W.sh[rid][1] = sun.y * s.cmul + s.cadd.y;
+                    W.sh[rid][2] = sun.z * s.cmul + s.cadd.z;
+                    W.shHas[rid] = miss ? 1 : 0;
+                    hs = 0;
+                    live = false;
                 }
-                if (add_ && ncon < PK_MAX_SPEC_SEGMENTS) {   // at most one per segment; the host checks the limit
-                    W.con[lane][ncon][0] = sc.x; W.con[lane][ncon][1] = sc.y; W.con[lane][ncon][2] = sc.z;
-                    ncon++;
+            }
+            __syncwarp();
+            // the pool's sums in the reference's order: lane 2j sums voxel j's specular rays (ray, then
+            // segment order), lane 2j+1 its shadow rays
+            {
+                const uint32_t j = lane >> 1;
+                if (j < np) {
+                    uint32_t mm = poolMask;
+                    for (uint32_t t = 0; t < j; t++) mm &= mm - 1u;
+                    const int v = __ffs(mm) - 1;
+                    f3 acc = mk(0.0f, 0.0f, 0.0f);
+                    if ((lane & 1u) == 0u) {
+                        if ((specMask >> v) & 1u) {
+                            const uint32_t r0 = (uint32_t)__popc(poolMask & specMask & ((1u << v) - 1u)) * K;
+                            for (uint32_t k2 = 0; k2 < K; k2++) {
+                                const uint32_t n = W.ncon[r0 + k2];
+                                for (uint32_t jj = 0; jj < n; jj++) {
+                                    acc.x = acc.x + W.con[r0 + k2][jj][0];
+                                    acc.y = acc.y + W.con[r0 + k2][jj][1];
+                                    acc.z = acc.z + W.con[r0 + k2][jj][2];
+                                }
+                            }
+                            W.v[v].spec = divs(acc, (float)K);
+                        }
+                    } else if ((diffMask >> v) & 1u) {
+                        uint32_t r0 = 0, mm2 = poolMask & diffMask & ((1u << v) - 1u);
+                        while (mm2) {
+                            const int u = __ffs(mm2) - 1;
+                            mm2 &= mm2 - 1u;
+                            r0 += ((firstMask >> u) & 1u) ? 1u : K;
+                        }
+                        const uint32_t n = ((firstMask >> v) & 1u) ? 1u : K;
+                        for (uint32_t k2 = 0; k2 < n; k2++)
+                            if (W.shHas[r0 + k2]) {
+                                acc.x = acc.x + W.sh[r0 + k2][0];
+                                acc.y = acc.y + W.sh[r0 + k2][1];
+                                acc.z = acc.z + W.sh[r0 + k2][2];
+                            }
+                        W.v[v].direct = divs(acc, (float)n);
+                    }
                 }
-                hs = 0;
-                if (more) stepping = true; else live = false;
-            } else if (pass == PP_FIRST || pass == PP_FAN) {
-                // shadow_ray: an unoccluded ray adds sunStrength * colorMult + colorAdd
-                if (hs == 2u) {
-                    cc.x = sun.x * s.cmul + s.cadd.x;
-                    cc.y = sun.y * s.cmul + s.cadd.y;
-                    cc.z = sun.z * s.cmul + s.cadd.z;
-                    has = true;
-                    if (pass == PP_FIRST) { pacc.x = pacc.x + cc.x; pacc.y = pacc.y + cc.y; pacc.z = pacc.z + cc.z; }
-                }
-                hs = 0;
-                live = false;
-            } else {
-                // diffuse_ray body after step_map (voxelLighting.comp:176-201); hs == 3: start the next path
-                const PacketVoxel& pv = W.v[lane];
-                bool pathDone = hs != 3u;
-                if (hs == 1u) {
-                    Voxel hv;
-                    decompress(m, hitIdx, hv);
-                    jd.jB = hv.normal;
-                    jd.jU = hv.material;
-                    const f3 d = vabs(sub(vfloor(muls(pv.pos0, 8.0f)), vfloor(muls(s.pos, 8.0f))));
-                    if (!(dot(d, d) < 1.0f)) {
-                        const Material& hm = mats[hv.material];
-                        if (hm.emissive) {
-                            pacc.x = pacc.x + jd.jA.x * (hv.albedo.x * p.emissiveStrength * s.cmul + s.cadd.x);
-                            pacc.y = pacc.y + jd.jA.y * (hv.albedo.y * p.emissiveStrength * s.cmul + s.cadd.y);
-                            pacc.z = pacc.z + jd.jA.z * (hv.albedo.z * p.emissiveStrength * s.cmul + s.cadd.z);
-                        } else {
-                            jd.jA.x = jd.jA.x * (hv.albedo.x * s.cmul + s.cadd.x);
-                            jd.jA.y = jd.jA.y * (hv.albedo.y * s.cmul + s.cadd.y);
-                            jd.jA.z = jd.jA.z * (hv.albedo.z * s.cmul + s.cadd.z);
-                            jd.jC = s.dir;
-                            jd.b++;
-                            if (jd.b < p.diffuseBounceLimit) {
-                                const f3 nd = diffuse_dir(jd, p, mats, rngSin);
-                                const TState keep = s.ts;
-                                seg_begin(s, s.pos, nd, rcp3(nd));
-                                s.ts = keep;
-                                c.rays++;
-                                pathDone = false;
-                                stepping = true;
+            }
+            __syncwarp();
+        }
+
+        // ---- (2) diffuse paths (voxelLighting.comp:149-203), one lane per voxel
+        f3 pacc = mk(0.0f, 0.0f, 0.0f);
+        if (diffMask) {
+            const bool mine = (diffMask >> lane) & 1u;
+            const PacketVoxel& pv = W.v[lane];
+            jd.key = pv.key; jd.tnormal = pv.tnormal; jd.tmat = pv.tmat;
+            jd.firstSample = (pv.flags & PV_FIRST) != 0u;
+            uint32_t pi = 0;
+            live = mine;
+            stepping = false;
+            hs = 3u;                       // "start the next path"
+            for (int guard = 0; guard < (1 << 30); guard++) {
+                if (live && !stepping) {
+                    bool pathDone = hs != 3u;
+                    if (hs == 1u) {
+                        Voxel hv;
+                        decompress(m, hitIdx, hv);
+                        jd.jB = hv.normal;
+                        jd.jU = hv.material;
+                        const f3 d = vabs(sub(vfloor(muls(pv.pos0, 8.0f)), vfloor(muls(s.pos, 8.0f))));
+                        if (!(dot(d, d) < 1.0f)) {
+                            const Material& hm = mats[hv.material];
+                            if (hm.emissive) {
+                                pacc.x = pacc.x + jd.jA.x * (hv.albedo.x * p.emissiveStrength * s.cmul + s.cadd.x);
+                                pacc.y = pacc.y + jd.jA.y * (hv.albedo.y * p.emissiveStrength * s.cmul + s.cadd.y);
+                                pacc.z = pacc.z + jd.jA.z * (hv.albedo.z * p.emissiveStrength * s.cmul + s.cadd.z);
+                            } else {
+                                jd.jA.x = jd.jA.x * (hv.albedo.x * s.cmul + s.cadd.x);
+                                jd.jA.y = jd.jA.y * (hv.albedo.y * s.cmul + s.cadd.y);
+                                jd.jA.z = jd.jA.z * (hv.albedo.z * s.cmul + s.cadd.z);
+                                jd.jC = s.dir;
+                                jd.b++;
+                                if (jd.b < p.diffuseBounceLimit) {
+                                    const f3 nd = diffuse_dir(jd, p, mats, rngSin);
+                                    const TState keep = s.ts;
+                                    seg_begin(s, s.pos, nd, rcp3(nd));
+                                    s.ts = keep;
+                                    c.rays++;
+                                    pathDone = false;
+                                    stepping = true;
+                                }
                             }
                         }
+                    } else if (hs == 2u) {
+                        const float kd = gmax(dot(s.dir, sunDir), 0.0f);
+                        pacc.x = pacc.x + (jd.jA.x * kd * sun.x * s.cmul + s.cadd.x);
+                        pacc.y = pacc.y + (jd.jA.y * kd * sun.y * s.cmul + s.cadd.y);
+                        pacc.z = pacc.z + (jd.jA.z * kd * sun.z * s.cmul + s.cadd.z);
                     }
-                } else if (hs == 2u) {
-                    const float kd = gmax(dot(s.dir, sunDir), 0.0f);
-                    pacc.x = pacc.x + (jd.jA.x * kd * sun.x * s.cmul + s.cadd.x);
-                    pacc.y = pacc.y + (jd.jA.y * kd * sun.y * s.cmul + s.cadd.y);
-                    pacc.z = pacc.z + (jd.jA.z * kd * sun.z * s.cmul + s.cadd.z);
+                    if (pathDone) { pacc = add(pacc, pv.direct); pi++; }
+                    hs = 0;
+                    if (!stepping) {
+                        // the voxel's next path, if any (paths without segments finish at once)
+                        live = false;
+                        while (pi < p.numDiffuse) {
+                            pacc = add(pacc, mk(p.ambient[0], p.ambient[1], p.ambient[2]));
+                            if (p.diffuseBounceLimit == 0u) { pacc = add(pacc, pv.direct); pi++; continue; }
+                            jd.i = pi; jd.b = 0;
+                            jd.jA = mk(1.0f, 1.0f, 1.0f);
+                            jd.jB = adds(jd.tnormal, EPS);
+                            jd.jC = mk(0.0f, 0.0f, 0.0f);
+                            jd.jU = jd.tmat;
+                            const f3 nd = diffuse_dir(jd, p, mats, rngSin);
+                            seg_begin(s, pv.pos0, nd, rcp3(nd));
+                            c.rays++;
+                            live = true;
+                            stepping = true;
+                            break;
+                        }
+                    }
                 }
-                if (pathDone) { pacc = add(pacc, pv.direct); pi++; }
-                hs = 0;
-                if (!stepping) {
-                    // the next path of this voxel, if any (paths without segments finish at once)
-                    live = false;
-                    while (pi < p.numDiffuse) {
-                        pacc = add(pacc, mk(p.ambient[0], p.ambient[1], p.ambient[2]));
-                        if (p.diffuseBounceLimit == 0u) { pacc = add(pacc, pv.direct); pi++; continue; }
-                        jd.i = pi; jd.b = 0;
-                        jd.jA = mk(1.0f, 1.0f, 1.0f);
-                        jd.jB = adds(jd.tnormal, EPS);
-                        jd.jC = mk(0.0f, 0.0f, 0.0f);
-                        jd.jU = jd.tmat;
-                        const f3 nd = diffuse_dir(jd, p, mats, rngSin);
-                        seg_begin(s, pv.pos0, nd, rcp3(nd));
-                        c.rays++;
-                        live = true;
-                        stepping = true;
-                        break;
+                if (!__any_sync(0xFFFFFFFFu, live)) break;
+                while (__any_sync(0xFFFFFFFFu, stepping)) {
+                    if (stepping) {
+                        const uint32_t rr = seg_step(s, m, mats, p.sunStrength, c, hitIdx);
+                        if (rr) { stepping = false; hs = rr; }
                     }
                 }
             }
         }
-        // ---- write the voxel's new lighting (voxelLighting.comp:266-288, FP32)
+        // ---- (3) write the voxel's new lighting (voxelLighting.comp:266-288, FP32)
         __syncwarp();
         if (myFlags & PV_VALID) {
             const PacketVoxel& pv = W.v[lane];
