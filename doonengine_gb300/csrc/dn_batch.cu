@@ -51,7 +51,8 @@ struct DNgpuBatch {
     std::vector<DevState*> gatherHost;  // the pointer list last copied to dsts
     uint32_t gatherCount;
     dn_batch_tuning tuning;
-    int maxBlocksPerSM;
+    int maxBlocksPerSM;         // of the ray-stream kernel
+    int maxBlocksPacket;        // of the packet kernel
     std::vector<uint64_t> lastKey;
     std::vector<uint64_t> graphKey;
     cudaGraphExec_t graph;
@@ -228,9 +229,10 @@ extern "C" int dn_cuda_batch_create(DNgpuBatch** out)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_stream_batch, 128, 0);
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM2, k_light_packet_batch, 128, 0);
         if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "occupancy: %s", cudaGetErrorString(e));
-        if (perSM2 < perSM) perSM = perSM2;
         b->maxBlocksPerSM = perSM < 1 ? 1 : perSM;
-        if ((int)b->tuning.blocksPerSM > b->maxBlocksPerSM) b->tuning.blocksPerSM = (uint32_t)b->maxBlocksPerSM;
+        b->maxBlocksPacket = perSM2 < 1 ? 1 : perSM2;
+        // every resident block the kernel allows
+        b->tuning.blocksPerSM = (uint32_t)(b->tuning.kernel == 2u ? b->maxBlocksPacket : b->maxBlocksPerSM);
     }
     if (rc) { dn_cuda_batch_destroy(b); return rc; }
     *out = b;
@@ -648,8 +650,9 @@ extern "C" int dn_cuda_batch_set_tuning(DNgpuBatch* b, const dn_batch_tuning* t)
     if (!b || !t) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (t->streamBatch < 1 || t->streamBatch > 32) return dn_set_err(DN_CUDA_ERR_ARG, "streamBatch %u", t->streamBatch);
     if (t->kernel != 1u && t->kernel != 2u) return dn_set_err(DN_CUDA_ERR_ARG, "kernel %u (1 streams, 2 packets)", t->kernel);
-    if (t->blocksPerSM < 1 || (int)t->blocksPerSM > b->maxBlocksPerSM)
-        return dn_set_err(DN_CUDA_ERR_ARG, "blocksPerSM %u (1..%d)", t->blocksPerSM, b->maxBlocksPerSM);
+    const int maxBlocks = t->kernel == 2u ? b->maxBlocksPacket : b->maxBlocksPerSM;
+    if (t->blocksPerSM < 1 || (int)t->blocksPerSM > maxBlocks)
+        return dn_set_err(DN_CUDA_ERR_ARG, "blocksPerSM %u (1..%d)", t->blocksPerSM, maxBlocks);
     b->tuning = *t;
     b->tuning.useGraph = t->useGraph ? 1u : 0u;
     return DN_CUDA_OK;
@@ -703,11 +706,13 @@ extern "C" int dn_cuda_batch_autotune(DNgpuBatch* b, dn_batch_tuning* chosen)
         dn_batch_tuning t = best;
         t.kernel = 3u - t.kernel;
         t.streamBatch = t.kernel == 2u ? g_packetBatch : g_streamBatch;
+        t.blocksPerSM = (uint32_t)(t.kernel == 2u ? b->maxBlocksPacket : b->maxBlocksPerSM);
         if (!rc && (t.kernel == 1u || packetsOk)) trial(t);
     }
     const uint32_t batches[] = {4u, 8u, 12u, 16u, 20u, 24u, 28u, 32u};
     for (uint32_t sb : batches) { dn_batch_tuning t = best; t.streamBatch = sb; if (!rc) trial(t); }
-    for (uint32_t bps = 2; bps <= (uint32_t)b->maxBlocksPerSM && bps <= 6; bps++) {
+    const uint32_t bpsMax = (uint32_t)(best.kernel == 2u ? b->maxBlocksPacket : b->maxBlocksPerSM);
+    for (uint32_t bps = 2; bps <= bpsMax && bps <= 8; bps++) {
         dn_batch_tuning t = best; t.blocksPerSM = bps; if (!rc) trial(t);
     }
     b->tuning = rc ? keep : best;

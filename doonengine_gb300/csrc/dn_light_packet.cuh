@@ -22,10 +22,11 @@
 namespace dn {
 
 #ifndef DN_PACKET_MIN_BLOCKS
-#define DN_PACKET_MIN_BLOCKS 4
+#define DN_PACKET_MIN_BLOCKS 6   // 6 blocks of 4 warps per SM (measured best on the large map: 5 and 4 are slower)
 #endif
 
-constexpr uint32_t PK_MAX_SPEC_SEGMENTS = 4;   // specBounceLimit handled here; larger limits use the stream kernel
+// specBounceLimit handled here (the reference's default is 2); larger limits use the stream kernel
+constexpr uint32_t PK_MAX_SPEC_SEGMENTS = 2;
 
 // per-voxel data of the warp's request group (shared memory, written by the voxel's lane)
 struct PacketVoxel {
