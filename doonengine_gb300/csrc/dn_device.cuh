@@ -149,6 +149,7 @@ struct Counters {             // per-thread traversal counters
 
 struct DevMap {
     uint32_t sx, sy, sz;
+    uint32_t stepCap;                    // D16: cells a traversal segment may visit (step_cap of the size)
     const uint32_t* __restrict__ tword;  // state << 30 | slot
     const uint32_t* __restrict__ tbits;  // 2 bits per tile: 0 absent, 1 unloaded, 2 loaded
     uint8_t* treq;

@@ -83,6 +83,8 @@ static inline dn::DevMap dev_map(const DNgpuVolume* g)
 {
     dn::DevMap m;
     m.sx = g->sx; m.sy = g->sy; m.sz = g->sz;
+    const uint64_t cap = 256ull * ((uint64_t)g->sx + g->sy + g->sz) + 4096ull;   // step_cap (dn_device.cuh)
+    m.stepCap = cap > (1ull << 23) ? (1u << 23) : (uint32_t)cap;
     m.tword = g->tword; m.tbits = g->tbits; m.treq = g->treq; m.ttouch = g->ttouch; m.tvis = g->tvis;
     m.rec = g->rec; m.vox = g->vox; m.diff = g->diff; m.spec = g->spec;
     return m;

@@ -251,12 +251,13 @@ __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLi
                     }
                     next = (next + (uint32_t)__popc(need)) < total ? next + (uint32_t)__popc(need) : total;
                 }
-                if (!__any_sync(0xFFFFFFFFu, live)) break;
-                // step until 'batch' lanes have an ended segment (or none is left stepping)
+                const unsigned liveMask = __ballot_sync(0xFFFFFFFFu, live);
+                if (!liveMask) break;
+                // step until 'batch' lanes have an ended segment (or none is left stepping); the live lanes
+                // do not change while stepping, so one vote per step tells both
                 for (;;) {
                     const unsigned st = __ballot_sync(0xFFFFFFFFu, stepping);
-                    if (!st) break;
-                    if ((uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, live && !stepping)) >= batch) break;
+                    if (!st || (uint32_t)__popc(liveMask & ~st) >= batch) break;
                     if (stepping) {
                         const uint32_t rr = seg_step(s, m, mats, p.sunStrength, c, hitIdx);
                         if (rr) { stepping = false; hs = rr; }

@@ -88,7 +88,7 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
     // D16: every visited cell (each outer or inner iteration of step_map / step_chunk) counts; a segment
     // that reached the cap ends as a miss
     if (inb) {
-        if ((s.flags >> 8) >= step_cap(m.sx, m.sy, m.sz)) return 2u;
+        if ((s.flags >> 8) >= m.stepCap) return 2u;
         s.flags += 256u;
     }
     const uint32_t idx = (uint32_t)s.cpos.x + bx * ((uint32_t)s.cpos.y + by * (uint32_t)s.cpos.z);
