@@ -670,8 +670,24 @@ extern "C" int dn_cuda_batch_autotune(DNgpuBatch* b, dn_batch_tuning* chosen)
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    // the reruns write only the lighting scratch and idempotent flags; keep the launch counters out of them
+    // The reruns read the committed lighting and sample counts, so voxels lit for the first time in that
+    // frame now trace their later-sample rays: the requested / touched / visible flags they set are saved
+    // here and restored afterwards, as are the launch counters; the scratch they write is overwritten by
+    // the next frame.
     CK(cudaMemcpyAsync(b->lsave, b->bst->lstats, sizeof(b->bst->lstats), cudaMemcpyDeviceToDevice, b->stream));
+    size_t flagBytes = 0;
+    for (const auto& mg : b->lastLightGens) flagBytes += 3 * mg.first->ntiles;
+    unsigned char* saved = nullptr;
+    CK(cudaMalloc((void**)&saved, flagBytes ? flagBytes : 1));
+    {
+        size_t o = 0;
+        for (const auto& mg : b->lastLightGens) {
+            const DNgpuVolume* g = mg.first;
+            CK(cudaMemcpyAsync(saved + o, g->treq, g->ntiles, cudaMemcpyDeviceToDevice, b->stream)); o += g->ntiles;
+            CK(cudaMemcpyAsync(saved + o, g->ttouch, g->ntiles, cudaMemcpyDeviceToDevice, b->stream)); o += g->ntiles;
+            CK(cudaMemcpyAsync(saved + o, g->tvis, g->ntiles, cudaMemcpyDeviceToDevice, b->stream)); o += g->ntiles;
+        }
+    }
     const dn_batch_tuning keep = b->tuning;
     dn_batch_tuning best = keep;
     // packets were possible in the last frame only if every lit map's specBounceLimit allowed them
@@ -717,10 +733,20 @@ extern "C" int dn_cuda_batch_autotune(DNgpuBatch* b, dn_batch_tuning* chosen)
     }
     b->tuning = rc ? keep : best;
     b->tuning.useGraph = keep.useGraph;
+    {
+        size_t o = 0;
+        for (const auto& mg : b->lastLightGens) {
+            DNgpuVolume* g = mg.first;
+            cudaMemcpyAsync(g->treq, saved + o, g->ntiles, cudaMemcpyDeviceToDevice, b->stream); o += g->ntiles;
+            cudaMemcpyAsync(g->ttouch, saved + o, g->ntiles, cudaMemcpyDeviceToDevice, b->stream); o += g->ntiles;
+            cudaMemcpyAsync(g->tvis, saved + o, g->ntiles, cudaMemcpyDeviceToDevice, b->stream); o += g->ntiles;
+        }
+    }
     cudaMemcpyAsync(b->bst->lstats, b->lsave, sizeof(b->bst->lstats), cudaMemcpyDeviceToDevice, b->stream);
     cudaStreamSynchronize(b->stream);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    cudaFree(saved);
     if (rc) return rc;
     b->lastKey.clear();
     if (chosen) *chosen = b->tuning;

@@ -193,9 +193,10 @@ int dn_cuda_batch_reset_stats(struct DNgpuBatch* b);
 void* dn_cuda_batch_stream(struct DNgpuBatch* b);
 int dn_cuda_batch_get_tuning(struct DNgpuBatch* b, dn_batch_tuning* out);
 int dn_cuda_batch_set_tuning(struct DNgpuBatch* b, const dn_batch_tuning* t);
-/* Times the lighting launch of the last batched frame under each candidate tuning (re-running it leaves
- * every map's state as it was: it writes only scratch and idempotent flags), keeps the fastest and
- * returns it in chosen (may be NULL).  Call after a frame with DN_BATCH_LIGHT items. */
+/* Times the lighting launch of the last batched frame under each candidate tuning, keeps the fastest and
+ * returns it in chosen (may be NULL).  Every map's state is left as it was: the reruns write only scratch,
+ * and the requested / touched / visible flags they set are saved before and restored after.  Call after a
+ * frame with DN_BATCH_LIGHT items. */
 int dn_cuda_batch_autotune(struct DNgpuBatch* b, dn_batch_tuning* chosen);
 /* request groups of the map's last sync, as read by its last dn_cuda_finish or dn_cuda_batch_finish */
 uint64_t dn_cuda_requests_of(struct DNgpuVolume* g);
