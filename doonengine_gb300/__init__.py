@@ -7,7 +7,7 @@ there is no CPU fallback (operations on a machine without a GPU fail with an err
 """
 from . import build as _build_mod
 from ._lib import load, library_path, check_layout, exported_names
-from .volume import Volume, Image, Batch, Server, init, install_message_callback, messages, DN_READ, DN_WRITE, DN_READ_WRITE
+from .volume import Volume, Image, Texture, Batch, Server, init, install_message_callback, messages, DN_READ, DN_WRITE, DN_READ_WRITE
 
 
 def build(force=False):
@@ -15,5 +15,5 @@ def build(force=False):
     return _build_mod.build(force=force)
 
 
-__all__ = ["build", "load", "library_path", "check_layout", "exported_names", "Volume", "Image", "Batch", "Server", "init",
+__all__ = ["build", "load", "library_path", "check_layout", "exported_names", "Volume", "Image", "Texture", "Batch", "Server", "init",
            "install_message_callback", "messages", "DN_READ", "DN_WRITE", "DN_READ_WRITE"]

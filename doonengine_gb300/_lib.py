@@ -95,6 +95,16 @@ class DnLightParams(Structure):
                 ("mapId", c_uint32), ("spherePts", (c_float * 3) * 64)]
 
 
+class DnDrawParams(Structure):
+    """dn_draw_params of include/dn_cuda.h"""
+    _fields_ = [("origin", c_float * 3), ("dirMat", (c_float * 4) * 4), ("width", c_uint32), ("height", c_uint32),
+                ("viewMode", c_uint32), ("truncate16", c_uint32), ("sunStrength", c_float * 3),
+                ("skyBot", c_float * 3), ("skyTop", c_float * 3), ("emissiveStrength", c_float),
+                ("invProj", (c_float * 4) * 4), ("rasterColor", c_void_p), ("rasterDepth", c_void_p),
+                ("rasterColorW", c_uint32), ("rasterColorH", c_uint32), ("rasterDepthW", c_uint32),
+                ("rasterDepthH", c_uint32), ("compose", c_uint32)]
+
+
 MESSAGE_CALLBACK = ctypes.CFUNCTYPE(None, c_int, c_int, c_char_p)
 VOLP = POINTER(DNvolume)
 
@@ -105,7 +115,8 @@ class DNbatchItem(Structure):
     """DNbatchItem of include/DoonEngine/voxel.h"""
     _fields_ = [("vol", VOLP), ("phases", c_uint32), ("output", POINTER(DNimage)), ("view", DNmat4),
                 ("projection", DNmat4), ("op", c_int), ("lightingSplit", c_int), ("numDiffuseSamples", c_int),
-                ("maxDiffuseSamples", c_int), ("time", c_float)]
+                ("maxDiffuseSamples", c_int), ("time", c_float), ("rasterColorTexture", c_int),
+                ("rasterDepthTexture", c_int)]
 
 
 REQUEST_DRAW, REQUEST_RELIGHT, REQUEST_EDIT = 0, 1, 2
@@ -120,7 +131,8 @@ class DNrequest(Structure):
     """DNrequest of include/DoonEngine/serve.h"""
     _fields_ = [("kind", c_int), ("volume", c_uint32), ("output", POINTER(DNimage)), ("view", DNmat4),
                 ("projection", DNmat4), ("numDiffuseSamples", c_int), ("maxDiffuseSamples", c_int), ("time", c_float),
-                ("edits", POINTER(DNvoxelEdit)), ("numEdits", c_uint32), ("user", c_void_p)]
+                ("edits", POINTER(DNvoxelEdit)), ("numEdits", c_uint32), ("user", c_void_p),
+                ("rasterColorTexture", c_int), ("rasterDepthTexture", c_int)]
 
 
 class DNcompletion(Structure):
@@ -178,6 +190,11 @@ _SIGS = [
     ("DN_decompress_voxel", DNvoxel, [DNcompressedVoxel]),
     ("DN_finish", c_bool, [VOLP]),
     ("DN_image_create", POINTER(DNimage), [c_uint32, c_uint32, c_int, c_int]),
+    ("DN_texture_create", c_int, [c_uint32, c_uint32, c_int]),
+    ("DN_texture_destroy", None, [c_int]),
+    ("DN_texture_upload", c_bool, [c_int, c_void_p]),
+    ("DN_texture_format", c_int, [c_int]),
+    ("DN_texture_device_pointer", c_void_p, [c_int, POINTER(c_uint32), POINTER(c_uint32)]),
     ("DN_image_destroy", None, [POINTER(DNimage)]),
     ("DN_draw_matrices", None, [DNmat4, DNmat4, POINTER(DNmat4), POINTER(DNmat4), POINTER(DNmat4)]),
     ("DN_get_stats", c_bool, [VOLP, POINTER(DNstats)]),
@@ -319,5 +336,7 @@ def check_layout(lib=None):
             ctypes.sizeof(DNstats), DNchunk.voxels.offset, ctypes.sizeof(DNvoxel),
             ctypes.sizeof(DNbatchItem), DNbatchItem.view.offset, DNbatchItem.op.offset, DNbatchItem.time.offset,
             ctypes.sizeof(DNrequest), DNrequest.edits.offset, DNrequest.user.offset, ctypes.sizeof(DNcompletion),
-            ctypes.sizeof(DNvoxelEdit), ctypes.sizeof(DNserveStats)]
+            ctypes.sizeof(DNvoxelEdit), ctypes.sizeof(DNserveStats), DNbatchItem.rasterColorTexture.offset,
+            DNrequest.rasterColorTexture.offset, ctypes.sizeof(DnDrawParams), DnDrawParams.compose.offset,
+            ctypes.sizeof(DnLightParams)]
     return [(i, int(buf[i]), w) for i, w in enumerate(want[:n]) if int(buf[i]) != w]

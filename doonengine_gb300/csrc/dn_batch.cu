@@ -431,6 +431,8 @@ extern "C" int dn_cuda_batch_frame(DNgpuBatch* b, const dn_batch_item* items, ui
         if (it.phases & DN_BATCH_DRAW) {
             if (!it.colorOut || it.draw.width == 0 || it.draw.height == 0)
                 return dn_set_err(DN_CUDA_ERR_ARG, "item %u: bad image", i);
+            const int rc = dn_check_raster(&it.draw);
+            if (rc) return rc;
             if (it.hostImage) {
                 hostImages = true;
                 int rc = dn_reserve_image_staging(g, (size_t)it.draw.width * it.draw.height);

@@ -761,9 +761,31 @@ int dn_reserve_image_staging(DNgpuVolume* g, size_t n)
     return DN_CUDA_OK;
 }
 
+// The raster inputs of a draw: compose 0, or compose 1 with two buffers of device memory and non-zero
+// sizes.  Checked before any launch, so that a bad pointer is an argument error, not a device fault.
+int dn_check_raster(const dn_draw_params* p)
+{
+    if (p->compose == 0u) return DN_CUDA_OK;
+    if (p->compose != 1u || !p->rasterColor || !p->rasterDepth || !p->rasterColorW || !p->rasterColorH ||
+        !p->rasterDepthW || !p->rasterDepthH)
+        return dn_set_err(DN_CUDA_ERR_ARG, "draw: invalid raster composition arguments (compose %u)", p->compose);
+    const void* ptrs[2] = {p->rasterColor, p->rasterDepth};
+    for (const void* q : ptrs) {
+        cudaPointerAttributes at;
+        const cudaError_t e = cudaPointerGetAttributes(&at, q);
+        if (e != cudaSuccess || (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)) {
+            (void)cudaGetLastError();
+            return dn_set_err(DN_CUDA_ERR_ARG, "draw: raster texture %p is not device memory", q);
+        }
+    }
+    return DN_CUDA_OK;
+}
+
 static int launch_draw(DNgpuVolume* g, const dn_draw_params* p, const dn_material* materials, float4* color,
                        uint32_t* hit, uint8_t* face)
 {
+    const int rc = dn_check_raster(p);
+    if (rc) return rc;
     static thread_local DrawArgs* a = nullptr;
     if (!a) a = new DrawArgs();
     a->d.m = dev_map(g);
@@ -942,7 +964,14 @@ extern "C" int dn_cuda_free(void* p) { if (p) CK(cudaFree(p)); return DN_CUDA_OK
 extern "C" int dn_cuda_malloc_host(void** p, size_t bytes) { CK(cudaMallocHost(p, bytes ? bytes : 1)); return DN_CUDA_OK; }
 extern "C" int dn_cuda_free_host(void* p) { if (p) CK(cudaFreeHost(p)); return DN_CUDA_OK; }
 extern "C" int dn_cuda_memcpy_d2h(void* dst, const void* src, size_t bytes) { CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost)); return DN_CUDA_OK; }
-extern "C" int dn_cuda_memcpy_h2d(void* dst, const void* src, size_t bytes) { CK(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice)); return DN_CUDA_OK; }
+// cudaMemcpy from pageable memory may return before the DMA has landed; the legacy-stream synchronise makes
+// the bytes visible to work issued afterwards on the library's non-blocking streams
+extern "C" int dn_cuda_memcpy_h2d(void* dst, const void* src, size_t bytes)
+{
+    CK(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+    CK(cudaStreamSynchronize(cudaStreamLegacy));
+    return DN_CUDA_OK;
+}
 extern "C" int dn_cuda_event_create(void** ev) { CK(cudaEventCreate((cudaEvent_t*)ev)); return DN_CUDA_OK; }
 extern "C" int dn_cuda_event_destroy(void* ev) { CK(cudaEventDestroy((cudaEvent_t)ev)); return DN_CUDA_OK; }
 extern "C" int dn_cuda_event_record(void* ev, void* stream) { CK(cudaEventRecord((cudaEvent_t)ev, (cudaStream_t)stream)); return DN_CUDA_OK; }

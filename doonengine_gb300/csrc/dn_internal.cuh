@@ -95,6 +95,8 @@ int dn_stage_ops(DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops, const dn_
                  uint32_t nrecords, const uint32_t* voxelWords, uint64_t nvoxels);
 // grows the device staging of host-memory draws to n pixels
 int dn_reserve_image_staging(DNgpuVolume* g, size_t n);
+// checks a draw's raster composition arguments (host side, before any launch)
+int dn_check_raster(const dn_draw_params* p);
 // gives g a new process-wide unique generation (after any device array of g is reallocated)
 void dn_new_generation(DNgpuVolume* g);
 
@@ -142,6 +144,36 @@ struct DrawArgs {
     dn::Material mats[256];
 };
 
+// Texel index of floor coordinate f under GL_REPEAT wrapping on a texture n texels wide.
+__device__ __forceinline__ uint32_t repeat_texel(float f, uint32_t n)
+{
+    const int k = (int)f % (int)n;
+    return (uint32_t)(k < 0 ? k + (int)n : k);
+}
+
+// GL_LINEAR sample with GL_REPEAT wrapping at texture coordinate (s, t), the filtering of the reference's
+// raster textures (main.c:313-322; wrap left at its default).  The steps are the OpenGL 4.3 formula
+// (section 8.14.2): u = s*w - 1/2, i0 = wrap(floor(u)), i1 = wrap(floor(u) + 1), alpha = u - floor(u),
+// the same along t, then (1-a)(1-b) T00 + a(1-b) T10 + (1-a)b T01 + ab T11 summed in that order.  C floats
+// per texel; the first N are returned.
+template <int C, int N>
+__device__ __forceinline__ void raster_sample(const float* tex, uint32_t w, uint32_t h, float s, float t, float* out)
+{
+    const float u = s * (float)w - 0.5f, v = t * (float)h - 0.5f;
+    const float fu = floorf(u), fv = floorf(v);
+    const float a = u - fu, b = v - fv;
+    const uint32_t i0 = repeat_texel(fu, w), j0 = repeat_texel(fv, h);
+    const uint32_t i1 = i0 + 1u == w ? 0u : i0 + 1u, j1 = j0 + 1u == h ? 0u : j0 + 1u;
+    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    const float* t00 = tex + ((size_t)j0 * w + i0) * C;
+    const float* t10 = tex + ((size_t)j0 * w + i1) * C;
+    const float* t01 = tex + ((size_t)j1 * w + i0) * C;
+    const float* t11 = tex + ((size_t)j1 * w + i1) * C;
+#pragma unroll
+    for (int k = 0; k < N; k++)
+        out[k] = w00 * __ldg(t00 + k) + w10 * __ldg(t10 + k) + w01 * __ldg(t01 + k) + w11 * __ldg(t11 + k);
+}
+
 // One primary ray (voxelDraw.comp:24-147): pixel (x, y) of the image described by a; smat holds the map's
 // materials.  Returns 1 when a primary ray was traced.
 __device__ __forceinline__ uint32_t draw_pixel(const DrawMap& a, const dn::Material* smat, uint32_t x, uint32_t y,
@@ -176,9 +208,38 @@ __device__ __forceinline__ uint32_t draw_pixel(const DrawMap& a, const dn::Mater
                        M[0][2] * sx + M[1][2] * sy + M[2][2] * 0.0f + M[3][2] * 1.0f);
             f3 rayDir = adds(normalize(rd), EPS);
             f3 inv = mk(1.0f / rayDir.x, 1.0f / rayDir.y, 1.0f / rayDir.z);
-            const float maxDepth = -1.0f;
+            // raster depth as a distance from the camera (voxelDraw.comp:86-101); negative: not tested
+            float maxDepth = -1.0f;
+            float texS = 0.0f, texT = 0.0f;
+            if (p.compose) {
+                texS = (float)x / (float)p.rasterColorW;
+                texT = (float)y / (float)p.rasterColorH;
+                float d;
+                raster_sample<1, 1>(p.rasterDepth, p.rasterDepthW, p.rasterDepthH, texS, texT, &d);
+                maxDepth = d * 2.0f - 1.0f;
+                if (maxDepth < 1.0f) {
+                    const float (*P)[4] = p.invProj;
+                    float vs[4];
+#pragma unroll
+                    for (int r = 0; r < 4; r++) vs[r] = P[0][r] * sx + P[1][r] * sy + P[2][r] * maxDepth + P[3][r] * 1.0f;
+                    const float wv = vs[3];
+                    const f3 vsp = mk(vs[0] / wv, vs[1] / wv, vs[2] / wv);
+                    maxDepth = sqrtf(dot(vsp, vsp));
+                } else {
+                    maxDepth = -1.0f;
+                }
+            }
+            // background_color (voxelDraw.comp:24-30): the sky, or the raster colour where a depth is tested
+            auto background = [&](f3 dir) -> f3 {
+                if (maxDepth < 0.0f) {
+                    const f3 s = sky_color(mk(p.skyBot[0], p.skyBot[1], p.skyBot[2]), mk(p.skyTop[0], p.skyTop[1], p.skyTop[2]), dir);
+                    return mk(powf(s.x, 2.2f), powf(s.y, 2.2f), powf(s.z, 2.2f));
+                }
+                float rc[3];
+                raster_sample<4, 3>(p.rasterColor, p.rasterColorW, p.rasterColorH, texS, texT, rc);
+                return mk(rc[0], rc[1], rc[2]);
+            };
             const f3 mapMax = mk((float)a.m.sx, (float)a.m.sy, (float)a.m.sz);
-            const f3 skyBot = mk(p.skyBot[0], p.skyBot[1], p.skyBot[2]), skyTop = mk(p.skyTop[0], p.skyTop[1], p.skyTop[2]);
             // intersect_AABB, voxelShared.comp:261-273
             f3 tMin = mul(sub(mk(0.0f, 0.0f, 0.0f), rayPos), inv);
             f3 tMax = mul(sub(mapMax, rayPos), inv);
@@ -189,8 +250,7 @@ __device__ __forceinline__ uint32_t draw_pixel(const DrawMap& a, const dn::Mater
             f3 fc;
             float depth = -1.0f;
             if (tNear > tFar || tFar < 0.0f) {
-                f3 s = sky_color(skyBot, skyTop, rayDir);
-                fc = mk(powf(s.x, 2.2f), powf(s.y, 2.2f), powf(s.z, 2.2f));
+                fc = background(rayDir);
             } else {
                 if (tNear > 0.0f) rayPos = add(rayPos, muls(rayDir, tNear + EPS));
                 // normal_AABB, voxelShared.comp:276-284
@@ -213,34 +273,39 @@ __device__ __forceinline__ uint32_t draw_pixel(const DrawMap& a, const dn::Mater
                     }
                     f3 dv = sub(rayPos, c.orgRayPos);
                     depth = sqrtf(dot(dv, dv));
-                    // voxel_color, voxelDraw.comp:32-61
-                    const Material& mt = smat[fv.material];
-                    f3 sp = muls(fv.spec, mt.specular);
-                    f3 df = muls(fv.diff, 1.0f - mt.specular);
-                    switch (p.viewMode) {
-                    case 0: {
-                        f3 solid = mt.emissive ? muls(fv.albedo, c.emissive) : add(mul(df, fv.albedo), sp);
-                        fc = add(muls(solid, cmul), cadd);
-                        break;
+                    if (maxDepth > 0.0f && depth > maxDepth) {
+                        // the rasterised scene is in front of the voxel (voxelDraw.comp:127-131): the pixel shows
+                        // it, so no voxel is reported as hit
+                        fc = add(muls(background(rayDir), cmul), cadd);
+                        depth = maxDepth;
+                    } else {
+                        // voxel_color, voxelDraw.comp:32-61
+                        const Material& mt = smat[fv.material];
+                        f3 sp = muls(fv.spec, mt.specular);
+                        f3 df = muls(fv.diff, 1.0f - mt.specular);
+                        switch (p.viewMode) {
+                        case 0: {
+                            f3 solid = mt.emissive ? muls(fv.albedo, c.emissive) : add(mul(df, fv.albedo), sp);
+                            fc = add(muls(solid, cmul), cadd);
+                            break;
+                        }
+                        case 1: fc = fv.albedo; break;
+                        case 2: fc = mt.emissive ? fv.albedo : df; break;
+                        case 3: fc = mt.emissive ? fv.albedo : sp; break;
+                        case 4: fc = vabs(fv.normal); break;
+                        case 5: fc = vabs(hitNormal); break;
+                        default: fc = mk(0.0f, 0.0f, 0.0f); break;
+                        }
+                        const uint32_t tx = hi.tile % a.m.sx, ty = (hi.tile / a.m.sx) % a.m.sy, tz = hi.tile / (a.m.sx * a.m.sy);
+                        const uint32_t gx = tx * 8u + (uint32_t)hi.local.x, gy = ty * 8u + (uint32_t)hi.local.y,
+                                       gz = tz * 8u + (uint32_t)hi.local.z;
+                        hitIdx = gx + (a.m.sx * 8u) * (gy + (a.m.sy * 8u) * gz);
+                        if (hitNormal.x > 0.0f) face = 0; else if (hitNormal.x < 0.0f) face = 1;
+                        else if (hitNormal.y > 0.0f) face = 2; else if (hitNormal.y < 0.0f) face = 3;
+                        else if (hitNormal.z > 0.0f) face = 4; else if (hitNormal.z < 0.0f) face = 5;
                     }
-                    case 1: fc = fv.albedo; break;
-                    case 2: fc = mt.emissive ? fv.albedo : df; break;
-                    case 3: fc = mt.emissive ? fv.albedo : sp; break;
-                    case 4: fc = vabs(fv.normal); break;
-                    case 5: fc = vabs(hitNormal); break;
-                    default: fc = mk(0.0f, 0.0f, 0.0f); break;
-                    }
-                    const uint32_t tx = hi.tile % a.m.sx, ty = (hi.tile / a.m.sx) % a.m.sy, tz = hi.tile / (a.m.sx * a.m.sy);
-                    const uint32_t gx = tx * 8u + (uint32_t)hi.local.x, gy = ty * 8u + (uint32_t)hi.local.y,
-                                   gz = tz * 8u + (uint32_t)hi.local.z;
-                    hitIdx = gx + (a.m.sx * 8u) * (gy + (a.m.sy * 8u) * gz);
-                    if (hitNormal.x > 0.0f) face = 0; else if (hitNormal.x < 0.0f) face = 1;
-                    else if (hitNormal.y > 0.0f) face = 2; else if (hitNormal.y < 0.0f) face = 3;
-                    else if (hitNormal.z > 0.0f) face = 4; else if (hitNormal.z < 0.0f) face = 5;
                 } else {
-                    f3 s = sky_color(skyBot, skyTop, rayDir);
-                    f3 bg = mk(powf(s.x, 2.2f), powf(s.y, 2.2f), powf(s.z, 2.2f));
-                    fc = add(muls(bg, cmul), cadd);
+                    fc = add(muls(background(rayDir), cmul), cadd);
                     depth = maxDepth;
                 }
             }

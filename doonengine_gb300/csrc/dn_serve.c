@@ -143,6 +143,10 @@ uint64_t DN_server_submit(DNserver* s, const DNrequest* r)
 	if (!s || !r || r->volume >= s->nslots) return 0;
 	if (r->kind == DN_REQUEST_DRAW && (!r->output || !r->output->color || !r->output->width || !r->output->height)) return 0;
 	if (r->kind == DN_REQUEST_EDIT && r->numEdits && !r->edits) return 0;
+	/* a draw composed with raster textures names one texture of each kind (as DN_draw checks) */
+	if (r->kind == DN_REQUEST_DRAW && r->rasterColorTexture > 0 && r->rasterDepthTexture > 0 &&
+	    (DN_texture_format(r->rasterColorTexture) != DN_TEXTURE_RGBA32F ||
+	     DN_texture_format(r->rasterDepthTexture) != DN_TEXTURE_DEPTH32F)) return 0;
 	if (r->kind > DN_REQUEST_EDIT) return 0;
 	Pending* p = (Pending*)calloc(1, sizeof(Pending));
 	if (!p) return 0;
@@ -302,6 +306,7 @@ static int launch_tick(DNserver* s)
 				if (pos >= 1) break;
 				it->phases |= DN_PHASE_DRAW;
 				it->output = r->output; it->view = r->view; it->projection = r->projection;
+				it->rasterColorTexture = r->rasterColorTexture; it->rasterDepthTexture = r->rasterDepthTexture;
 				pos = 1;
 			} else {
 				if (pos >= 2) break;

@@ -28,6 +28,7 @@
 #include <math.h>
 #include <string.h>
 #include <stdarg.h>
+#include <pthread.h>
 
 /* ------------------------------------------------------------- globals */
 
@@ -900,6 +901,122 @@ static void draw_prepare(DNvolume* vol, const DNimage* output, DNmat4 view, DNma
 	memcpy(dp->skyBot, vol->skyGradientBot.v, 12);
 	memcpy(dp->skyTop, vol->skyGradientTop.v, 12);
 	dp->emissiveStrength = vol->emissiveStrength;
+	memcpy(dp->invProj, ip.m, sizeof(dp->invProj));
+}
+
+/* ---- raster textures: device buffers standing in for the GL textures of the raster pass ---- */
+
+#define DN_MAX_TEXTURES 4096
+
+typedef struct DNtextureSlot
+{
+	float* dev;
+	uint32_t width, height;
+	DNtextureFormat format;
+} DNtextureSlot;
+
+static DNtextureSlot g_textures[DN_MAX_TEXTURES];   /* handle h is slot h - 1; dev == NULL: free */
+static pthread_mutex_t g_textureLock = PTHREAD_MUTEX_INITIALIZER;
+
+static size_t texel_floats(DNtextureFormat f) { return f == DN_TEXTURE_RGBA32F ? 4 : 1; }
+
+int DN_texture_create(uint32_t width, uint32_t height, DNtextureFormat format)
+{
+	if (width == 0 || height == 0 || (format != DN_TEXTURE_RGBA32F && format != DN_TEXTURE_DEPTH32F)) {
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "DN_texture_create: invalid size or format");
+		return -1;
+	}
+	float* dev = NULL;
+	if (dn_cuda_malloc((void**)&dev, (size_t)width * height * texel_floats(format) * sizeof(float)) != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "failed to allocate a texture: %s", dn_cuda_last_error());
+		return -1;
+	}
+	pthread_mutex_lock(&g_textureLock);
+	int h = -1;
+	for (int i = 0; i < DN_MAX_TEXTURES; i++)
+		if (!g_textures[i].dev) {
+			g_textures[i].dev = dev; g_textures[i].width = width; g_textures[i].height = height;
+			g_textures[i].format = format;
+			h = i + 1;
+			break;
+		}
+	pthread_mutex_unlock(&g_textureLock);
+	if (h < 0) {
+		dn_cuda_free(dev);
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "DN_texture_create: all %d texture handles are in use", DN_MAX_TEXTURES);
+	}
+	return h;
+}
+
+/* copies slot h's description; false for a handle that names no texture */
+static bool texture_get(int h, DNtextureSlot* out)
+{
+	if (h < 1 || h > DN_MAX_TEXTURES) return false;
+	pthread_mutex_lock(&g_textureLock);
+	*out = g_textures[h - 1];
+	pthread_mutex_unlock(&g_textureLock);
+	return out->dev != NULL;
+}
+
+void DN_texture_destroy(int texture)
+{
+	DNtextureSlot t;
+	if (!texture_get(texture, &t)) return;
+	pthread_mutex_lock(&g_textureLock);
+	memset(&g_textures[texture - 1], 0, sizeof(DNtextureSlot));
+	pthread_mutex_unlock(&g_textureLock);
+	dn_cuda_free(t.dev);   /* waits for device work in flight */
+}
+
+bool DN_texture_upload(int texture, const float* texels)
+{
+	DNtextureSlot t;
+	if (!texels || !texture_get(texture, &t)) {
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "DN_texture_upload: invalid texture or data");
+		return false;
+	}
+	if (dn_cuda_memcpy_h2d(t.dev, texels, (size_t)t.width * t.height * texel_floats(t.format) * sizeof(float)) != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "texture upload failed: %s", dn_cuda_last_error());
+		return false;
+	}
+	return true;
+}
+
+int DN_texture_format(int texture)
+{
+	DNtextureSlot t;
+	return texture_get(texture, &t) ? (int)t.format : -1;
+}
+
+float* DN_texture_device_pointer(int texture, uint32_t* width, uint32_t* height)
+{
+	DNtextureSlot t;
+	if (!texture_get(texture, &t)) return NULL;
+	if (width) *width = t.width;
+	if (height) *height = t.height;
+	return t.dev;
+}
+
+/* raster composition of a draw: the reference composes when both handles are >= 0 (voxel.c:833-842); a
+ * handle of 0 or below names no texture here (as GL never names a created texture 0).  False (with an
+ * error message) when a positive handle names no texture of the right format. */
+static bool raster_prepare(int colorTex, int depthTex, dn_draw_params* dp, const char* who)
+{
+	dp->compose = 0;
+	if (colorTex <= 0 || depthTex <= 0) return true;
+	DNtextureSlot c, d;
+	if (!texture_get(colorTex, &c) || c.format != DN_TEXTURE_RGBA32F) {
+		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_ERROR, "%s: raster colour texture %d is not an RGBA32F texture", who, colorTex);
+		return false;
+	}
+	if (!texture_get(depthTex, &d) || d.format != DN_TEXTURE_DEPTH32F) {
+		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_ERROR, "%s: raster depth texture %d is not a DEPTH32F texture", who, depthTex);
+		return false;
+	}
+	dp->compose = 1;
+	dp->rasterColor = c.dev; dp->rasterColorW = c.width; dp->rasterColorH = c.height;
+	dp->rasterDepth = d.dev; dp->rasterDepthW = d.width; dp->rasterDepthH = d.height;
+	return true;
 }
 
 void DN_draw(DNvolume* vol, DNimage* output, DNmat4 view, DNmat4 projection, int rasterColorTexture, int rasterDepthTexture)
@@ -910,12 +1027,11 @@ void DN_draw(DNvolume* vol, DNimage* output, DNmat4 view, DNmat4 projection, int
 		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_ERROR, "DN_draw: invalid output image");
 		return;
 	}
-	if (rasterColorTexture >= 0 && rasterDepthTexture >= 0)
-		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_NOTE, "raster composition is not available; drawing without it");
 	if (vol->useCubemap)
 		dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_NOTE, "cube-map sky is not available; using the sky gradient");
 	dn_draw_params dp;
 	draw_prepare(vol, output, view, projection, &dp);
+	if (!raster_prepare(rasterColorTexture, rasterDepthTexture, &dp, "DN_draw")) return;
 	int rc = output->onDevice
 		? dn_cuda_draw(vol->gpu, &dp, (const dn_material*)vol->materials, output->color, output->hitIndex, output->hitFace)
 		: dn_cuda_draw_host(vol->gpu, &dp, (const dn_material*)vol->materials, output->color, output->hitIndex, output->hitFace);
@@ -1082,7 +1198,9 @@ size_t DN_abi_layout(uint64_t* out, size_t n)
 		sizeof(DNchunkHandle), sizeof(DNstats), offsetof(DNchunk, voxels), sizeof(DNvoxel),
 		sizeof(DNbatchItem), offsetof(DNbatchItem, view), offsetof(DNbatchItem, op), offsetof(DNbatchItem, time),
 		sizeof(DNrequest), offsetof(DNrequest, edits), offsetof(DNrequest, user), sizeof(DNcompletion),
-		sizeof(DNvoxelEdit), sizeof(DNserveStats)
+		sizeof(DNvoxelEdit), sizeof(DNserveStats), offsetof(DNbatchItem, rasterColorTexture),
+		offsetof(DNrequest, rasterColorTexture), sizeof(dn_draw_params), offsetof(dn_draw_params, compose),
+		sizeof(dn_light_params)
 	};
 	size_t k = sizeof(v) / sizeof(v[0]);
 	for (size_t i = 0; i < n && i < k; i++) out[i] = v[i];
@@ -1194,6 +1312,9 @@ bool DN_batch_run(DNbatch* b, const DNbatchItem* items, unsigned int count)
 			dn_msg(DN_MESSAGE_SHADER, DN_MESSAGE_ERROR, "DN_batch_run: item %u has an invalid output image", i);
 			return false;
 		}
+		dn_draw_params probe;
+		if ((it->phases & DN_PHASE_DRAW) && !raster_prepare(it->rasterColorTexture, it->rasterDepthTexture, &probe, "DN_batch_run"))
+			return false;
 	}
 	/* host halves in item order: draw parameters, chunk staging (issued now on the batch's stream; the
 	 * staged records are published by the sync pass, after the draw), lighting parameters */
@@ -1208,6 +1329,7 @@ bool DN_batch_run(DNbatch* b, const DNbatchItem* items, unsigned int count)
 		if (it->phases & DN_PHASE_DRAW) {
 			const DNimage* out = it->output;
 			draw_prepare(vol, out, it->view, it->projection, &d->draw);
+			if (!raster_prepare(it->rasterColorTexture, it->rasterDepthTexture, &d->draw, "DN_batch_run")) return false;
 			d->hostImage = out->onDevice ? 0u : 1u;
 			d->colorOut = out->color; d->hitOut = out->hitIndex; d->faceOut = out->hitFace;
 		}

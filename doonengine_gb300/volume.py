@@ -92,6 +92,46 @@ class Image:
         return color, hit, face
 
 
+class Texture:
+    """A raster texture (DN_texture_create): RGBA32F colour or DEPTH32F window depth, in device memory."""
+
+    RGBA32F, DEPTH32F = 0, 1
+
+    def __init__(self, width, height, fmt):
+        self.lib = L.load()
+        self.handle = self.lib.DN_texture_create(width, height, fmt)
+        if self.handle <= 0:
+            raise RuntimeError("DN_texture_create failed")
+        self.width, self.height, self.fmt = width, height, fmt
+
+    def upload(self, texels):
+        """texels: (height, width, 4) for colour, (height, width) for depth; converted to float32."""
+        shape = (self.height, self.width, 4) if self.fmt == self.RGBA32F else (self.height, self.width)
+        a = np.ascontiguousarray(texels, dtype=np.float32)
+        if a.shape != shape:
+            raise ValueError("texture data of shape %s, expected %s" % (a.shape, shape))
+        if not self.lib.DN_texture_upload(self.handle, a.ctypes.data):
+            raise RuntimeError("DN_texture_upload failed")
+
+    def close(self):
+        if self.handle > 0:
+            self.lib.DN_texture_destroy(self.handle)
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _raster_handles(raster):
+    """(colour Texture, depth Texture) or None -> the two DN_draw handles"""
+    if raster is None:
+        return -1, -1
+    return raster[0].handle, raster[1].handle
+
+
 class Volume:
     """Owns one DNvolume."""
 
@@ -170,8 +210,9 @@ class Volume:
         self.lib.DN_set_view_projection_matrices(self.ptr, aspect, near, far, byref(v), byref(p))
         return v, p
 
-    def draw(self, image, view, proj):
-        self.lib.DN_draw(self.ptr, image.ptr, view, proj, -1, -1)
+    def draw(self, image, view, proj, raster=None):
+        """raster: None, or (colour Texture, depth Texture) to compose with"""
+        self.lib.DN_draw(self.ptr, image.ptr, view, proj, *_raster_handles(raster))
 
     def sync(self, op=DN_READ_WRITE, split=1):
         self.lib.DN_sync_gpu(self.ptr, op, split)
@@ -280,8 +321,9 @@ class Batch:
             pass
 
     @staticmethod
-    def item(vol, image=None, view=None, proj=None, sync=None, light=None):
-        """One DNbatchItem: draw into image with (view, proj); sync=(op, split); light=(numDiffuse, maxDiffuse, time)."""
+    def item(vol, image=None, view=None, proj=None, sync=None, light=None, raster=None):
+        """One DNbatchItem: draw into image with (view, proj) composed with raster=(colour, depth) Textures;
+        sync=(op, split); light=(numDiffuse, maxDiffuse, time)."""
         it = L.DNbatchItem()
         it.vol = vol.ptr
         ph = 0
@@ -289,6 +331,7 @@ class Batch:
             ph |= L.PHASE_DRAW
             it.output = image.ptr
             it.view, it.projection = view, proj
+            it.rasterColorTexture, it.rasterDepthTexture = _raster_handles(raster)
         if sync is not None:
             ph |= L.PHASE_SYNC
             it.op, it.lightingSplit = sync
@@ -364,9 +407,10 @@ class Server:
             raise RuntimeError("DN_server_start failed")
 
     @staticmethod
-    def draw_request(volume, image, view, proj, user=0):
+    def draw_request(volume, image, view, proj, user=0, raster=None):
         r = L.DNrequest()
         r.kind, r.volume, r.output, r.view, r.projection, r.user = L.REQUEST_DRAW, volume, image.ptr, view, proj, user
+        r.rasterColorTexture, r.rasterDepthTexture = _raster_handles(raster)
         return r
 
     @staticmethod

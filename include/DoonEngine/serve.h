@@ -7,7 +7,7 @@
  * arrive while earlier ticks are on the GPU are admitted into the next tick and run beside the other
  * volumes' requests.  A volume's requests run in arrival order, and each kind is a fixed sequence of the
  * reference's calls:
- *   draw     DN_draw(vol, output, view, projection)
+ *   draw     DN_draw(vol, output, view, projection, rasterColorTexture, rasterDepthTexture)
  *   relight  DN_sync_gpu(vol, DN_READ_WRITE, 1) then DN_update_lighting(vol, numDiffuse, maxDiffuse, time)
  *   edit     the voxel edits on the CPU map (DN_set_voxel / DN_remove_voxel), then DN_sync_gpu(vol,
  *            DN_READ_WRITE, 1): changed chunks are re-staged in place and their lighting history reset
@@ -54,6 +54,7 @@ typedef struct DNrequest
 	const DNvoxelEdit* edits;        /* edit: copied at submission */
 	unsigned int numEdits;
 	void* user;                      /* returned with the completion */
+	int rasterColorTexture, rasterDepthTexture;   /* draw: as DN_draw (0: none) */
 } DNrequest;
 
 typedef struct DNcompletion

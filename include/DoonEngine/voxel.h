@@ -12,7 +12,9 @@
  *     (RGBA32F colour + depth, plus the hit voxel index and face per pixel),
  *     in device or host memory;
  *   - the raster colour / depth texture handles stay as ints; -1 means "no
- *     raster composition" exactly as in the reference;
+ *     raster composition" exactly as in the reference.  The textures are
+ *     device buffers made with DN_texture_create (addition) in place of the
+ *     GL textures of the application's raster pass;
  *   - the cube-map sky (voxel.h:135-136) is not available (no texture stack);
  *     the gradient sky is used and useCubemap is ignored with a NOTE.
  * Additions are marked "addition".
@@ -227,6 +229,30 @@ bool DN_finish(DNvolume* vol);
 DNimage* DN_image_create(uint32_t width, uint32_t height, int onDevice, int withHitInfo);
 void DN_image_destroy(DNimage* img);
 
+/* Raster textures (addition): the colour and depth textures of the reference's raster pass
+ * (main.c:310-322) that DN_draw composes with the voxel scene (voxelDraw.comp:86-136), as device
+ * buffers.  The handle (> 0) is passed as DN_draw's rasterColorTexture / rasterDepthTexture; composition
+ * happens when both name a texture (0 and negative handles name none, as GL never names a created texture
+ * 0).  Colour: RGBA32F per texel, alpha unused.  Depth: one float per texel, the window depth (0 at the near
+ * plane, 1 at the far plane or where nothing was rasterised).  Texel (i, j) is at [j * width + i], rows in
+ * the order of DNimage's pixels.  A draw samples both GL_LINEAR with GL_REPEAT at texture coordinate
+ * (x / colourWidth, y / colourHeight), as the reference's textures are set up. */
+typedef enum DNtextureFormat
+{
+	DN_TEXTURE_RGBA32F = 0,
+	DN_TEXTURE_DEPTH32F = 1
+} DNtextureFormat;
+int DN_texture_create(uint32_t width, uint32_t height, DNtextureFormat format);   /* handle, or -1 */
+/* waits for device work in flight, then frees the texture */
+void DN_texture_destroy(int texture);
+/* copies the whole texture from host memory (4 or 1 floats per texel); complete when it returns.  Draws
+ * that read the texture must have finished (DN_finish) before it is overwritten. */
+bool DN_texture_upload(int texture, const float* texels);
+/* the texture's format, or -1 for a handle that names no texture */
+int DN_texture_format(int texture);
+/* the texture's device buffer, for a CUDA rasteriser that writes it in place (NULL for a bad handle) */
+float* DN_texture_device_pointer(int texture, uint32_t* width, uint32_t* height);
+
 /* The inverse matrices DN_draw derives from view / projection
  * (voxel.c:845-853): inverse view, inverse view without translation,
  * inverse projection. */
@@ -283,6 +309,7 @@ typedef struct DNbatchItem
 	int lightingSplit;
 	int numDiffuseSamples, maxDiffuseSamples;   /* lighting: as DN_update_lighting */
 	float time;
+	int rasterColorTexture, rasterDepthTexture; /* draw: as DN_draw (0: none) */
 } DNbatchItem;
 
 DNbatch* DN_batch_create(void);

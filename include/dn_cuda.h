@@ -83,6 +83,14 @@ typedef struct dn_draw_params {
     uint32_t width, height, viewMode, truncate16;
     float sunStrength[3], skyBot[3], skyTop[3];
     float emissiveStrength;
+    /* raster composition (voxelDraw.comp:86-101, 127-136), used when compose is 1: device textures of the
+     * rasterised scene, texel (i, j) at [j * w + i] like the output's pixels; colour RGBA32F (alpha unused),
+     * depth one float per texel (window depth, 0 near .. 1 far) */
+    float invProj[4][4];        /* inverse projection, column-major */
+    const float* rasterColor;
+    const float* rasterDepth;
+    uint32_t rasterColorW, rasterColorH, rasterDepthW, rasterDepthH;
+    uint32_t compose;
 } dn_draw_params;
 
 typedef struct dn_stats {
@@ -232,6 +240,7 @@ int dn_cuda_free(void* p);
 int dn_cuda_malloc_host(void** p, size_t bytes);
 int dn_cuda_free_host(void* p);
 int dn_cuda_memcpy_d2h(void* dst, const void* src, size_t bytes);
+/* complete when it returns: later work on any of the library's streams sees the bytes */
 int dn_cuda_memcpy_h2d(void* dst, const void* src, size_t bytes);
 int dn_cuda_event_create(void** ev);
 int dn_cuda_event_destroy(void* ev);

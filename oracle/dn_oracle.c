@@ -970,6 +970,43 @@ static void mat4_mul(const float A[4][4], const float B[4][4], float C[4][4])
 
 static inline float gpow(float x, float y) { return powf(x, y); }
 
+/* Texel of floor coordinate f under GL_REPEAT on a texture n texels wide. */
+static uint32_t repeat_texel(float f, uint32_t n)
+{
+    int k = (int)f % (int)n;
+    return (uint32_t)(k < 0 ? k + (int)n : k);
+}
+
+/* GL_LINEAR sample with GL_REPEAT at texture coordinate (s, t): the OpenGL 4.3 formula (section 8.14.2)
+ * u = s*w - 1/2, i0 = wrap(floor(u)), i1 = wrap(floor(u) + 1), alpha = u - floor(u) (same along t), then
+ * (1-a)(1-b) T00 + a(1-b) T10 + (1-a)b T01 + ab T11 in that order.  The reference samples its raster
+ * textures this way (main.c:313-322 set GL_LINEAR; the wrap stays at its GL_REPEAT default;
+ * voxelDraw.comp:28, 89).  C floats per texel, the first n returned. */
+static void raster_sample(const float* tex, uint32_t w, uint32_t h, int C, int n, float s, float t, float* out)
+{
+    float u = s * (float)w - 0.5f, v = t * (float)h - 0.5f;
+    float fu = floorf(u), fv = floorf(v);
+    float a = u - fu, b = v - fv;
+    uint32_t i0 = repeat_texel(fu, w), j0 = repeat_texel(fv, h);
+    uint32_t i1 = i0 + 1u == w ? 0u : i0 + 1u, j1 = j0 + 1u == h ? 0u : j0 + 1u;
+    float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    for (int k = 0; k < n; k++)
+        out[k] = w00 * tex[((size_t)j0 * w + i0) * C + k] + w10 * tex[((size_t)j0 * w + i1) * C + k]
+               + w01 * tex[((size_t)j1 * w + i0) * C + k] + w11 * tex[((size_t)j1 * w + i1) * C + k];
+}
+
+/* background_color (voxelDraw.comp:24-30): the sky when no raster depth is tested, else the raster colour */
+static v3 background(const dno_draw_params* p, float maxDepth, float texS, float texT, v3 skyBot, v3 skyTop, v3 dir)
+{
+    if (maxDepth < 0.0f) {
+        v3 s = sky_color(skyBot, skyTop, dir);
+        return V(gpow(s.x, 2.2f), gpow(s.y, 2.2f), gpow(s.z, 2.2f));
+    }
+    float rc[3];
+    raster_sample(p->rasterColor, p->rasterColorW, p->rasterColorH, 4, 3, texS, texT, rc);
+    return V(rc[0], rc[1], rc[2]);
+}
+
 void dno_draw(dno_map* m, const dno_material* mats, const dno_draw_params* p,
               float* color, uint32_t* hitOut, uint8_t* faceOut, int nthreads)
 {
@@ -1011,7 +1048,24 @@ void dno_draw(dno_map* m, const dno_material* mats, const dno_draw_params* p,
                       M[0][2] * sx + M[1][2] * sy + M[2][2] * 0.0f + M[3][2] * 1.0f);
             v3 rayDir = vadds(vnormalize(rd), EPS);
             v3 inv = V(1.0f / rayDir.x, 1.0f / rayDir.y, 1.0f / rayDir.z);
-            float maxDepth = -1.0f;
+            /* raster depth as a distance from the camera, voxelDraw.comp:86-101 (negative: not tested) */
+            float maxDepth = -1.0f, texS = 0.0f, texT = 0.0f;
+            if (p->compose) {
+                texS = (float)x / (float)p->rasterColorW;
+                texT = (float)y / (float)p->rasterColorH;
+                float d;
+                raster_sample(p->rasterDepth, p->rasterDepthW, p->rasterDepthH, 1, 1, texS, texT, &d);
+                maxDepth = d * 2.0f - 1.0f;
+                if (maxDepth < 1.0f) {
+                    float vs[4];
+                    for (int r = 0; r < 4; r++)
+                        vs[r] = p->invProj[0][r] * sx + p->invProj[1][r] * sy + p->invProj[2][r] * maxDepth + p->invProj[3][r] * 1.0f;
+                    v3 vp = V(vs[0] / vs[3], vs[1] / vs[3], vs[2] / vs[3]);
+                    maxDepth = sqrtf(dot3(vp, vp));
+                } else {
+                    maxDepth = -1.0f;
+                }
+            }
             /* intersect_AABB, voxelShared.comp:261-273 */
             v3 tMin = vmul(vsub(V(0.0f, 0.0f, 0.0f), rayPos), inv);
             v3 tMax = vmul(vsub(mapMax, rayPos), inv);
@@ -1021,8 +1075,7 @@ void dno_draw(dno_map* m, const dno_material* mats, const dno_draw_params* p,
             float tFar = gmin(gmin(t2.x, t2.y), t2.z);
             v3 fc; float depth = -1.0f;
             if (tNear > tFar || tFar < 0.0f) {
-                v3 s = sky_color(skyBot, skyTop, rayDir);
-                fc = V(gpow(s.x, 2.2f), gpow(s.y, 2.2f), gpow(s.z, 2.2f));
+                fc = background(p, maxDepth, texS, texT, skyBot, skyTop, rayDir);
             } else {
                 if (tNear > 0.0f) rayPos = vadd(rayPos, vmuls(rayDir, tNear + EPS));
                 /* normal_AABB, voxelShared.comp:276-284 */
@@ -1041,6 +1094,12 @@ void dno_draw(dno_map* m, const dno_material* mats, const dno_draw_params* p,
                     if (in_map(m, mp)) store_u8(&m->vis[map_index(m, mp)], 1);
                     v3 dv = vsub(rayPos, c.orgRayPos);
                     depth = sqrtf(dot3(dv, dv));
+                    if (maxDepth > 0.0f && depth > maxDepth) {
+                        /* the rasterised scene is in front (voxelDraw.comp:127-131): no voxel is reported */
+                        fc = vadd(vmuls(background(p, maxDepth, texS, texT, skyBot, skyTop, rayDir), cmul), cadd);
+                        depth = maxDepth;
+                        goto store;
+                    }
                     /* voxel_color, voxelDraw.comp:32-61 */
                     const dno_material* mt = &mats[fv.material];
                     v3 sp = vmuls(fv.spec, mt->specular);
@@ -1070,12 +1129,11 @@ void dno_draw(dno_map* m, const dno_material* mats, const dno_draw_params* p,
                     else if (hitNormal.z > 0.0f) f = 4; else if (hitNormal.z < 0.0f) f = 5;
                     faceOut[j] = f;
                 } else {
-                    v3 s = sky_color(skyBot, skyTop, rayDir);
-                    v3 bg = V(gpow(s.x, 2.2f), gpow(s.y, 2.2f), gpow(s.z, 2.2f));
-                    fc = vadd(vmuls(bg, cmul), cadd);
+                    fc = vadd(vmuls(background(p, maxDepth, texS, texT, skyBot, skyTop, rayDir), cmul), cadd);
                     depth = maxDepth;
                 }
             }
+        store:
             out[0] = gpow(fc.x, 0.4545f); out[1] = gpow(fc.y, 0.4545f); out[2] = gpow(fc.z, 0.4545f);
             out[3] = depth;
         }

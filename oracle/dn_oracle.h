@@ -166,6 +166,13 @@ typedef struct dno_draw_params {
     /* pixel subset (NULL = all pixels): list of pixel indices y*width+x */
     const uint32_t* pixels;
     uint32_t npixels;
+    /* raster composition (voxelDraw.comp:86-101, 127-136) when compose is 1: colour RGBA (4 floats per
+     * texel, alpha unused) and window depth (1 float per texel), texel (i, j) at [j * w + i]; sampled
+     * GL_LINEAR with GL_REPEAT at texture coordinate (x / colorW, y / colorH) */
+    uint32_t compose;
+    const float* rasterColor;
+    const float* rasterDepth;
+    uint32_t rasterColorW, rasterColorH, rasterDepthW, rasterDepthH;
 } dno_draw_params;
 
 typedef struct dno_counters {

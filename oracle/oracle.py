@@ -34,7 +34,10 @@ class DrawParams(Structure):
     _fields_ = [("invView", (c_float * 4) * 4), ("invCenteredView", (c_float * 4) * 4), ("invProj", (c_float * 4) * 4),
                 ("width", c_uint32), ("height", c_uint32), ("viewMode", c_uint32), ("truncate16", c_uint32),
                 ("sunStrength", c_float * 3), ("skyBot", c_float * 3), ("skyTop", c_float * 3),
-                ("emissiveStrength", c_float), ("pixels", POINTER(c_uint32)), ("npixels", c_uint32)]
+                ("emissiveStrength", c_float), ("pixels", POINTER(c_uint32)), ("npixels", c_uint32),
+                ("compose", c_uint32), ("rasterColor", POINTER(c_float)), ("rasterDepth", POINTER(c_float)),
+                ("rasterColorW", c_uint32), ("rasterColorH", c_uint32), ("rasterDepthW", c_uint32),
+                ("rasterDepthH", c_uint32)]
 
 
 class Counters(Structure):
@@ -188,7 +191,9 @@ class OracleMap:
                                     req_idx.ctypes.data, n, d.ctypes.data, s.ctypes.data, v.ctypes.data, nthreads)
         return d, s, v
 
-    def draw(self, vol_s, inv_view, inv_cview, inv_proj, width, height, pixels=None, nthreads=0):
+    def draw(self, vol_s, inv_view, inv_cview, inv_proj, width, height, pixels=None, nthreads=0, raster=None):
+        """raster: None, or (colour (h, w, 4) float32, depth (h, w) float32) composed as DN_draw does with
+        raster textures"""
         p = DrawParams()
         for M, dst in ((inv_view, p.invView), (inv_cview, p.invCenteredView), (inv_proj, p.invProj)):
             for c in range(4):
@@ -201,6 +206,15 @@ class OracleMap:
         p.skyBot[:] = vol_s.skyGradientBot.tolist()
         p.skyTop[:] = vol_s.skyGradientTop.tolist()
         p.emissiveStrength = vol_s.emissiveStrength
+        if raster is not None:
+            rc = np.ascontiguousarray(raster[0], dtype=np.float32)
+            rd = np.ascontiguousarray(raster[1], dtype=np.float32)
+            assert rc.ndim == 3 and rc.shape[2] == 4 and rd.ndim == 2
+            p.compose = 1
+            p.rasterColor = rc.ctypes.data_as(POINTER(c_float))
+            p.rasterDepth = rd.ctypes.data_as(POINTER(c_float))
+            p.rasterColorH, p.rasterColorW = rc.shape[:2]
+            p.rasterDepthH, p.rasterDepthW = rd.shape
         if pixels is not None:
             pixels = np.ascontiguousarray(pixels, dtype=np.uint32)
             p.pixels = pixels.ctypes.data_as(POINTER(c_uint32))

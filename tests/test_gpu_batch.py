@@ -42,12 +42,12 @@ def frame_args(vol, W, H):
     return v, p
 
 
-def solo_frame(maps, t, phases=None, op=2, split=1):
+def solo_frame(maps, t, phases=None, op=2, split=1, rasters=None):
     for i, (vol, img, W, H) in enumerate(maps):
         ph = phases[i] if phases else "dsl"
         if "d" in ph:
             v, p = frame_args(vol, W, H)
-            vol.draw(img, v, p)
+            vol.draw(img, v, p, raster=rasters[i] if rasters else None)
         if "s" in ph:
             vol.sync(op, split)
         if "l" in ph:
@@ -56,7 +56,7 @@ def solo_frame(maps, t, phases=None, op=2, split=1):
         assert vol.finish(), dn.load().dn_cuda_last_error().decode()
 
 
-def batch_frame(batch, maps, t, phases=None, op=2, split=1):
+def batch_frame(batch, maps, t, phases=None, op=2, split=1, rasters=None):
     items = []
     for i, (vol, img, W, H) in enumerate(maps):
         ph = phases[i] if phases else "dsl"
@@ -65,7 +65,8 @@ def batch_frame(batch, maps, t, phases=None, op=2, split=1):
         v, p = frame_args(vol, W, H)
         items.append(dn.Batch.item(vol, img if "d" in ph else None, v, p,
                                    sync=(op, split) if "s" in ph else None,
-                                   light=(1, 1000, t) if "l" in ph else None))
+                                   light=(1, 1000, t) if "l" in ph else None,
+                                   raster=rasters[i] if rasters else None))
     batch.run(items)
     assert batch.finish(), dn.load().dn_cuda_last_error().decode()
 
@@ -207,3 +208,36 @@ def test_batch_then_delete_member(gpu_ready):
     finally:
         batch.close()
         close_all(bat)
+
+
+def test_batch_raster_composition(gpu_ready):
+    """Draws composed with raster textures (DN_draw's rasterColorTexture / rasterDepthTexture) give the same
+    images in a batch as alone, including graph replays that reuse the composition."""
+    solo, bat = build_set(), build_set()
+    batch = dn.Batch([m[0] for m in bat])
+    rng = np.random.default_rng(8)
+    textures = []
+    try:
+        rasters = []
+        for k, (vol, img, W, H) in enumerate(solo):
+            if k == 3:
+                rasters.append(None)       # one map draws without composition
+                continue
+            tw, th = W // (1 + k % 2) + k, H // (1 + k % 2) + 1
+            ct = dn.Texture(tw, th, dn.Texture.RGBA32F)
+            dt = dn.Texture(W, H, dn.Texture.DEPTH32F)
+            ct.upload(rng.random((th, tw, 4), dtype=np.float32))
+            dt.upload(np.where(rng.random((H, W)) < 0.2, 1.0, rng.uniform(0.95, 1.0, (H, W))).astype(np.float32))
+            textures += [ct, dt]
+            rasters.append((ct, dt))
+        for f in range(4):
+            t = 1.25 + 0.5 * f
+            solo_frame(solo, t, rasters=rasters)
+            batch_frame(batch, bat, t, rasters=rasters)
+            for i in range(len(SPECS)):
+                same_state(solo[i], bat[i], "frame %d map %d" % (f, i))
+    finally:
+        batch.close()
+        close_all(solo, bat)
+        for x in textures:
+            x.close()

@@ -184,15 +184,6 @@ def test_camera_inside_map_and_host_image(gpu_ready):
         pair.close()
 
 
-class _DrawParams(__import__("ctypes").Structure):
-    """dn_draw_params of include/dn_cuda.h"""
-    import ctypes as _c
-    _fields_ = [("origin", _c.c_float * 3), ("dirMat", (_c.c_float * 4) * 4), ("width", _c.c_uint32),
-                ("height", _c.c_uint32), ("viewMode", _c.c_uint32), ("truncate16", _c.c_uint32),
-                ("sunStrength", _c.c_float * 3), ("skyBot", _c.c_float * 3), ("skyTop", _c.c_float * 3),
-                ("emissiveStrength", _c.c_float)]
-
-
 def test_degenerate_ray_is_capped(gpu_ready):
     """A primary ray whose direction has an exactly zero x component: normalize((-1e-4, 0.6, 0.8)) + EPS
     gives x = 0 in float32, so the DDA's x side distance becomes 0 * inf = NaN after one step and the
@@ -212,7 +203,7 @@ def test_degenerate_ray_is_capped(gpu_ready):
         iv.m[3][0], iv.m[3][1], iv.m[3][2] = 2.5, 1.5, 2.5           # camera inside the map (chunk units)
         ip.m[3][0], ip.m[3][1], ip.m[3][2], ip.m[3][3] = -1e-4, 0.6, 0.8, 1.0
         M = lib.DN_mat4_mult(icv, ip)
-        p = _DrawParams()
+        p = _lib.DnDrawParams()
         p.origin[:] = [2.5, 1.5, 2.5]
         for c in range(4):
             for r in range(4):
@@ -238,5 +229,86 @@ def test_degenerate_ray_is_capped(gpu_ready):
         cap = 256 * (sx + sy + sz) + 4096
         assert st["outerSteps"] + st["innerSteps"] == W * H * cap, st     # every pixel's ray reached the cap
         img.close()
+    finally:
+        pair.close()
+
+
+def _window_depth(proj, t):
+    """GL window depth of a point at view distance t straight ahead (z_eye = -t) under projection proj
+    (column-major m[col][row]): clip z / clip w mapped from [-1, 1] to [0, 1]."""
+    m = np.array([[proj.m[c][r] for r in range(4)] for c in range(4)], np.float64)
+    cz = m[2][2] * -t + m[3][2]
+    cw = m[2][3] * -t + m[3][3]
+    return (0.5 * cz / cw + 0.5).astype(np.float32)
+
+
+def _raster_scene(rng, depth_px, proj, shape):
+    """Raster colour and window depth of 'shape' straddling the voxel depths of depth_px: per texel
+    nothing (depth 1), a surface 0.5-1.5x as far as the voxel seen there, or one at a random distance."""
+    h, w = shape
+    hh, ww = depth_px.shape
+    ys = (np.arange(h) * hh // h)[:, None]
+    xs = (np.arange(w) * ww // w)[None, :]
+    vox = depth_px[ys, xs]
+    t = np.where(vox > 0, vox * rng.uniform(0.5, 1.5, (h, w)), rng.uniform(0.5, 40.0, (h, w)))
+    depth = _window_depth(proj, t)
+    depth = np.where(rng.random((h, w)) < 0.2, np.float32(1.0), depth).astype(np.float32)
+    color = rng.random((h, w, 4), dtype=np.float32)
+    return color, depth
+
+
+@pytest.mark.parametrize("tex_scale,transparent", [((1, 1), False), ((2, 3), True)])
+def test_raster_composition(gpu_ready, tex_scale, transparent):
+    """DN_draw with raster colour / depth textures (voxelDraw.comp:86-136): raster surfaces in front of
+    voxels replace them, transparent voxels in front of a raster surface tint it, texture sizes other than
+    the image's wrap (GL_REPEAT) and filter (GL_LINEAR) as the oracle restates them."""
+    pair = Pair("tiny")
+    rng = np.random.default_rng(17)
+    try:
+        if transparent:
+            for m in range(0, 16, 3):
+                pair.vol.set_material(m, opacity=0.5, refract=1.52, specular=0.2, reflect_type=1, shininess=3)
+        for _ in range(3):
+            pair.step()
+        v, p, (iv, icv, ip) = pair.matrices()
+        plain = pair.img.numpy()[0][..., 3]
+        th, tw = pair.H // tex_scale[0] + 1, pair.W // tex_scale[1] + 3
+        color, depth = _raster_scene(rng, plain, p, (th, tw))
+        depth2 = _raster_scene(rng, plain, p, (pair.H, pair.W))[1] if tex_scale != (1, 1) else depth
+        ct = dn.Texture(tw, th, dn.Texture.RGBA32F)
+        dt = dn.Texture(depth2.shape[1], depth2.shape[0], dn.Texture.DEPTH32F)
+        ct.upload(color)
+        dt.upload(depth2)
+        pair.vol.draw(pair.img, v, p, raster=(ct, dt))
+        gpu = pair.img.numpy()
+        ora = pair.om.draw(pair.vol.s, iv, icv, ip, pair.W, pair.H, raster=(color, depth2))
+        compare_draw(gpu, ora, "raster composition")
+        compare_tiles(pair.vol, pair.om, "raster composition")
+        hit_plain = plain > 0
+        occluded = hit_plain & (gpu[1] == 0xFFFFFFFF)
+        shown = hit_plain & (gpu[1] != 0xFFFFFFFF)
+        assert occluded.sum() > 0 and shown.sum() > 0, (int(occluded.sum()), int(shown.sum()))
+        # a bad handle is refused with an error and draws nothing
+        before = gpu[0].copy()
+        pair.vol.draw(pair.img, v, p, raster=(dt, ct))
+        assert np.array_equal(pair.img.numpy()[0].view(np.uint32), before.view(np.uint32))
+        # the C ABI refuses raster buffers that are not device memory, before any launch
+        import ctypes
+        from doonengine_gb300 import _lib
+        lib = dn.load()
+        host = np.zeros(64, np.float32)
+        ct_ptr = lib.DN_texture_device_pointer(ct.handle, None, None)
+        assert ct_ptr
+        for compose, ptr in ((1, host.ctypes.data), (2, ct_ptr)):
+            dp = _lib.DnDrawParams()
+            dp.width, dp.height, dp.compose = 4, 4, compose
+            dp.rasterColor = dp.rasterDepth = ptr
+            dp.rasterColorW = dp.rasterColorH = dp.rasterDepthW = dp.rasterDepthH = 4
+            rc = lib.dn_cuda_draw(pair.vol.s.gpu, ctypes.byref(dp), ctypes.cast(pair.vol.s.materials, ctypes.c_void_p),
+                                  ctypes.cast(pair.img.ptr.contents.color, ctypes.c_void_p), None, None)
+            assert rc == 1, (compose, rc)
+        assert pair.vol.finish()
+        ct.close()
+        dt.close()
     finally:
         pair.close()

@@ -205,6 +205,12 @@ def test_submit_rejects_bad_requests(gpu_ready):
         bad.output = None
         with pytest.raises(RuntimeError):
             server.submit(bad)
+        # raster handles that name no texture
+        img = dn.Image(8, 8)
+        bad = dn.Server.draw_request(0, img, *vols[0].view_proj(1.0))
+        bad.rasterColorTexture, bad.rasterDepthTexture = 4000, 4001
+        with pytest.raises(RuntimeError):
+            server.submit(bad)
         server.start()
         assert server.drain(10.0)
     finally:
