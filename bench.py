@@ -619,6 +619,135 @@ def run_streaming(args):
         print(json.dumps(result), flush=True)
 
 
+# ------------------------------------------------------------ shapes workload
+
+def shape_script(rng, map_size, n):
+    """n seeded shape calls over the map: every kind, half extents 4-48 voxels, any orientation, a third of
+    them removals (two thirds of those with flipped normals)"""
+    X, Y, Z = (8 * s for s in map_size)
+    ops = []
+    for _ in range(n):
+        kind = int(rng.integers(0, 8))
+        c = tuple(float(x) for x in np.round(rng.uniform((0, 0, 0), (X, Y, Z)) * 4) / 4)
+        v = tuple(float(x) for x in np.round(rng.uniform(4.0, 48.0, 3) * 4) / 4)
+        a = float(np.round(rng.uniform(4.0, 48.0) * 4) / 4)
+        b = float(np.round(rng.uniform(3.0, 40.0) * 4) / 4)
+        if kind == 3:
+            b = min(b, a - 1.0)
+        removal = rng.random() < 1.0 / 3.0
+        mat = 255 if removal else int(rng.integers(0, 16))
+        ops.append(dict(kind=kind, c=c, v=v, a=a, b=b, orient=tuple(float(x) for x in rng.integers(0, 360, 3)),
+                        voxel=(mat, (0.0, 1.0, 0.0), tuple(int(x) for x in rng.integers(0, 256, 3))),
+                        flip=bool(removal and rng.random() < 2.0 / 3.0)))
+    return ops
+
+
+def run_shapes(args):
+    """The shape functions as an edit source: each step places a script of 16 large shapes into a
+    64x32x64-chunk map through DN_shape_* (device evaluation of every voxel of the covered chunks, host
+    edits in the reference's order).  value: voxels evaluated per second of device time; e2e: the same
+    per second of wall time through the public call (transform, evaluation, copy back, edits)."""
+    import ctypes
+    rank, world, local, pg = dist_setup()
+    import doonengine_gb300 as dn
+    lib = dn.load()
+    if lib.dn_cuda_init(local) != 0:
+        raise RuntimeError("dn_cuda_init(%d): %s" % (local, lib.dn_cuda_last_error().decode()))
+    dn.init()
+    map_size = (64, 32, 64)
+    per_step = 16
+    rng = np.random.default_rng(41 + 1000 * rank)
+    vol = dn.Volume(map_size, 4096, cpu_only=True)
+    total = args.warmup + args.steps
+    script = [shape_script(rng, map_size, per_step) for _ in range(total)]
+
+    def step(ops):
+        for o in ops:
+            vol.shape(o["kind"], o["voxel"], o["c"], o["v"], o["a"], o["b"], o["orient"], o["flip"])
+
+    for f in range(args.warmup):
+        step(script[f])
+    vox = ctypes.c_uint64()
+    dms = ctypes.c_double()
+    lib.dn_cuda_shape_stats(vox, dms, 1)
+    launches0 = lib.dn_cuda_launch_count()
+    clocks = ClockSampler(local)
+    barrier(pg)
+    lib.dn_cuda_device_sync()
+    clocks.start()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        step(script[args.warmup + k])
+    lib.dn_cuda_device_sync()
+    barrier(pg)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches = lib.dn_cuda_launch_count() - launches0
+    lib.dn_cuda_shape_stats(vox, dms, 0)
+    voxels = allreduce_sum(pg, vox.value)
+    dev_s = allreduce_max(pg, dms.value) / 1e3
+    wall = allreduce_max(pg, wall)
+    solid = int((vol.export_voxels()[0] >> 24 != 255).sum())
+    result = {
+        "metric": "shape voxels evaluated/s", "value": voxels / dev_s, "unit": "voxels/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded shape scripts)",
+        "config": {"workload": "shapes: %d DN_shape_* calls per step (all 8 kinds, half extents 4-48 voxels, "
+                               "random orientation, 1/3 removals) into a %dx%dx%d-chunk CPU map"
+                               % ((per_step,) + map_size),
+                   "map_chunks": list(map_size), "shapes_per_step": per_step,
+                   "l2": "not flushed (each shape's evaluation reads only its parameters)",
+                   "parallelism": "replicas: one map per GPU, no collective"},
+        "voxels_evaluated_per_step": voxels / args.steps, "solid_voxels_after": solid,
+        "e2e": {"value": voxels / wall, "unit": "voxels/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": None, "path": "DN_shape_* (host transform + device evaluation + host edits)",
+                "wall_ms_per_step": wall * 1e3 / args.steps},
+        "gpu_launches": int(allreduce_sum(pg, launches)), "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = shapes_cpu_baseline(map_size, script[args.warmup], args.cpu_seconds)
+    vol.close()
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+
+
+def shapes_cpu_baseline(map_size, ops, seconds):
+    """the CPU oracle's restatement of the shape functions (evaluation + edits, one thread) on the first
+    timed step's shapes, as many as fit in about the given seconds"""
+    import doonengine_gb300 as dn
+    from oracle import oracle as O
+    lib = dn.load()
+    from doonengine_gb300 import _lib as L
+    d = O.DenseShapes(map_size)
+    done = 0
+    voxels = 0
+    t0 = time.perf_counter()
+    for o in ops:
+        q = lib.DN_quaternion_from_euler(L.DNvec3(*o["orient"]))
+        rot = lib.DN_quaternion_to_mat4(q)
+        at = L.DNvec3(*o["c"])
+        if o["kind"] == 6:
+            up = lib.DN_mat4_mult_vec4(rot, L.DNvec4(0.0, 1.0, 0.0, 1.0))
+            at = lib.DN_vec3_add(at, lib.DN_vec3_scale(L.DNvec3(up.x, up.y, up.z), o["b"]))
+        t = lib.DN_mat4_mult(lib.DN_mat4_translate(at), rot)
+        it = lib.DN_mat4_inv(t)
+        tm = np.array([[t.m[c][r] for r in range(4)] for c in range(4)], np.float32)
+        im = np.array([[it.m[c][r] for r in range(4)] for c in range(4)], np.float32)
+        so = O.DenseShapes.op(o["kind"], int(o["flip"]), o["voxel"][0], o["voxel"][2], o["voxel"][1], o["c"], o["v"],
+                              o["a"], o["b"], tm, im)
+        ev = d.apply(so)
+        if ev is not None:
+            voxels += int(np.prod(ev[1] - ev[0] + 1)) * 512
+        done += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    el = time.perf_counter() - t0
+    return {"value": voxels / el, "unit": "voxels/s", "cores": 1, "kind": "port",
+            "sample": "%d of the first timed step's %d shapes through the CPU oracle (evaluation + edits, %.1f s)"
+                      % (done, len(ops), el)}
+
+
 # ------------------------------------------------------------ serving workload
 
 def run_serving(args):
@@ -841,7 +970,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-pixels", type=int, default=0, help="pixels per reference step (0 = the full image)")
     ap.add_argument("--ref-requests", type=int, default=2048, help="lighting request groups per reference step")
-    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "serving", "streaming"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "serving", "streaming", "shapes"],
                     help="plain: one map per step (the headline); batched: many maps per step")
     ap.add_argument("--maps", type=int, default=64, help="maps of the batched workload")
     ap.add_argument("--no-autotune", action="store_true")
@@ -861,6 +990,8 @@ def main():
         run_batched(args)
     elif args.workload == "streaming":
         run_streaming(args)
+    elif args.workload == "shapes":
+        run_shapes(args)
     elif args.workload == "serving":
         if args.maps == 64:
             args.maps = 256

@@ -40,6 +40,14 @@ class DNvoxel(Structure):
     _fields_ = [("material", c_uint8), ("normal", DNvec3), ("albedo", DNcolor)]
 
 
+class DNvec4(Structure):
+    _fields_ = [("x", c_float), ("y", c_float), ("z", c_float), ("w", c_float)]
+
+
+class DNquaternion(Structure):
+    _fields_ = [("x", c_float), ("y", c_float), ("z", c_float), ("w", c_float)]
+
+
 class DNcompressedVoxel(Structure):
     _fields_ = [("normal", c_uint32), ("albedo", c_uint32)]
 
@@ -208,6 +216,27 @@ _SIGS = [
     ("DN_set_allocator", None, [c_void_p, c_void_p, c_void_p]),
     ("DN_mat4_inv", DNmat4, [DNmat4]),
     ("DN_mat4_mult", DNmat4, [DNmat4, DNmat4]),
+    ("DN_mat4_translate", DNmat4, [DNvec3]),
+    ("DN_mat4_mult_vec4", DNvec4, [DNmat4, DNvec4]),
+    ("DN_vec3_add", DNvec3, [DNvec3, DNvec3]),
+    ("DN_vec3_scale", DNvec3, [DNvec3, c_float]),
+    ("DN_quaternion_identity", DNquaternion, []),
+    ("DN_quaternion_from_euler", DNquaternion, [DNvec3]),
+    ("DN_quaternion_to_mat4", DNmat4, [DNquaternion]),
+    ("DN_shape_sphere", None, [VOLP, DNvoxel, c_bool, DNvec3, c_float, DNquaternion, c_void_p, c_void_p]),
+    ("DN_shape_box", None, [VOLP, DNvoxel, c_bool, DNvec3, DNvec3, DNquaternion, c_void_p, c_void_p]),
+    ("DN_shape_rounded_box", None, [VOLP, DNvoxel, c_bool, DNvec3, DNvec3, c_float, DNquaternion, c_void_p, c_void_p]),
+    ("DN_shape_torus", None, [VOLP, DNvoxel, c_bool, DNvec3, c_float, c_float, DNquaternion, c_void_p, c_void_p]),
+    ("DN_shape_ellipsoid", None, [VOLP, DNvoxel, c_bool, DNvec3, DNvec3, DNquaternion, c_void_p, c_void_p]),
+    ("DN_shape_cylinder", None, [VOLP, DNvoxel, c_bool, DNvec3, c_float, c_float, DNquaternion, c_void_p, c_void_p]),
+    ("DN_shape_cone", None, [VOLP, DNvoxel, c_bool, DNvec3, c_float, c_float, DNquaternion, c_void_p, c_void_p]),
+    ("DN_shape_pyramid", None, [VOLP, DNvoxel, c_bool, DNvec3, DNvec3, DNquaternion, c_void_p, c_void_p]),
+    ("DN_export_voxels", None, [VOLP, c_void_p, c_void_p, c_void_p]),
+    ("dn_shape_apply", None, [VOLP, DNvoxel, c_bool, c_bool, c_void_p, c_void_p, DNvec3, DNvec3, DNmat4, c_void_p,
+                              c_void_p, c_void_p, c_void_p]),
+    ("dn_cuda_shape_eval", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("dn_cuda_shape_free", None, [c_void_p]),
+    ("dn_cuda_shape_stats", None, [POINTER(c_uint64), POINTER(c_double), c_int]),
     ("DN_vec3_normalize", DNvec3, [DNvec3]),
     ("DN_batch_create", c_void_p, []),
     ("DN_batch_destroy", None, [c_void_p]),

@@ -1014,5 +1014,6 @@ extern "C" int dn_cuda_flush_l2(void* stream, size_t bytes)
 extern "C" const char* dn_cuda_kernel_names(void)
 {
     return "k_draw;k_light;k_light_stream;k_light_packet;k_commit;k_sync_stage;k_compact;k_clamp_requests;k_flush;"
-           "k_draw_batch;k_compact_batch;k_batch_reset;k_batch_prep;k_light_stream_batch;k_light_packet_batch;k_commit_batch;k_batch_gather";
+           "k_draw_batch;k_compact_batch;k_batch_reset;k_batch_prep;k_light_stream_batch;k_light_packet_batch;k_commit_batch;k_batch_gather;"
+           "k_shape_count;k_shape_write";
 }

@@ -130,48 +130,94 @@ DNmat4 DN_mat4_lookat(DNvec3 pos, DNvec3 target, DNvec3 up)
 
 DNmat4 DN_mat4_inv(DNmat4 in)
 {
-	/* Laplace expansion by 2x2 minors of columns (0,1) and (2,3):
-	 * det = sum of products of complementary minors; inverse = adjugate / det */
-	float a[4][4];
-	memcpy(a, in.m, sizeof(a));   /* a[col][row] */
-	/* element (row r, col c) = a[c][r] */
-#define E(r, c) a[c][r]
-	float s0 = E(0,0) * E(1,1) - E(1,0) * E(0,1);
-	float s1 = E(0,0) * E(1,2) - E(1,0) * E(0,2);
-	float s2 = E(0,0) * E(1,3) - E(1,0) * E(0,3);
-	float s3 = E(0,1) * E(1,2) - E(1,1) * E(0,2);
-	float s4 = E(0,1) * E(1,3) - E(1,1) * E(0,3);
-	float s5 = E(0,2) * E(1,3) - E(1,2) * E(0,3);
-	float c5 = E(2,2) * E(3,3) - E(3,2) * E(2,3);
-	float c4 = E(2,1) * E(3,3) - E(3,1) * E(2,3);
-	float c3 = E(2,1) * E(3,2) - E(3,1) * E(2,2);
-	float c2 = E(2,0) * E(3,3) - E(3,0) * E(2,3);
-	float c1 = E(2,0) * E(3,2) - E(3,0) * E(2,2);
-	float c0 = E(2,0) * E(3,1) - E(3,0) * E(2,1);
-	float det = s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0;
+	/* Adjugate / determinant.  The cofactors come from six 2x2 minors of two columns at a time, and the
+	 * operations run in the order of the reference's math header (quickmath.h mat4_inv), so the inverse is
+	 * bit-identical to the reference's, signed zeros included.  A singular matrix returns all zeros. */
+	const float a = in.m[0][0], b = in.m[0][1], c = in.m[0][2], d = in.m[0][3];
+	const float e = in.m[1][0], f = in.m[1][1], g = in.m[1][2], h = in.m[1][3];
+	const float i = in.m[2][0], j = in.m[2][1], k = in.m[2][2], l = in.m[2][3];
+	const float m = in.m[3][0], n = in.m[3][1], o = in.m[3][2], p = in.m[3][3];
 	DNmat4 r;
-	memset(&r, 0, sizeof(r));
-	if (det == 0.0f) return r;
-	float id = 1.0f / det;
-	float b[4][4];   /* b[row][col] of the inverse */
-	b[0][0] = ( E(1,1) * c5 - E(1,2) * c4 + E(1,3) * c3) * id;
-	b[0][1] = (-E(0,1) * c5 + E(0,2) * c4 - E(0,3) * c3) * id;
-	b[0][2] = ( E(3,1) * s5 - E(3,2) * s4 + E(3,3) * s3) * id;
-	b[0][3] = (-E(2,1) * s5 + E(2,2) * s4 - E(2,3) * s3) * id;
-	b[1][0] = (-E(1,0) * c5 + E(1,2) * c2 - E(1,3) * c1) * id;
-	b[1][1] = ( E(0,0) * c5 - E(0,2) * c2 + E(0,3) * c1) * id;
-	b[1][2] = (-E(3,0) * s5 + E(3,2) * s2 - E(3,3) * s1) * id;
-	b[1][3] = ( E(2,0) * s5 - E(2,2) * s2 + E(2,3) * s1) * id;
-	b[2][0] = ( E(1,0) * c4 - E(1,1) * c2 + E(1,3) * c0) * id;
-	b[2][1] = (-E(0,0) * c4 + E(0,1) * c2 - E(0,3) * c0) * id;
-	b[2][2] = ( E(3,0) * s4 - E(3,1) * s2 + E(3,3) * s0) * id;
-	b[2][3] = (-E(2,0) * s4 + E(2,1) * s2 - E(2,3) * s0) * id;
-	b[3][0] = (-E(1,0) * c3 + E(1,1) * c1 - E(1,2) * c0) * id;
-	b[3][1] = ( E(0,0) * c3 - E(0,1) * c1 + E(0,2) * c0) * id;
-	b[3][2] = (-E(3,0) * s3 + E(3,1) * s1 - E(3,2) * s0) * id;
-	b[3][3] = ( E(2,0) * s3 - E(2,1) * s1 + E(2,2) * s0) * id;
-#undef E
-	for (int row = 0; row < 4; row++)
-		for (int col = 0; col < 4; col++) r.m[col][row] = b[row][col];
+	float t0, t1, t2, t3, t4, t5;
+
+	/* minors of columns 2 and 3 */
+	t0 = k * p - o * l; t1 = j * p - n * l; t2 = j * o - n * k;
+	t3 = i * p - m * l; t4 = i * o - m * k; t5 = i * n - m * j;
+	r.m[0][0] =   f * t0 - g * t1 + h * t2;
+	r.m[1][0] = -(e * t0 - g * t3 + h * t4);
+	r.m[2][0] =   e * t1 - f * t3 + h * t5;
+	r.m[3][0] = -(e * t2 - f * t4 + g * t5);
+	r.m[0][1] = -(b * t0 - c * t1 + d * t2);
+	r.m[1][1] =   a * t0 - c * t3 + d * t4;
+	r.m[2][1] = -(a * t1 - b * t3 + d * t5);
+	r.m[3][1] =   a * t2 - b * t4 + c * t5;
+
+	/* minors of columns 1 and 3 */
+	t0 = g * p - o * h; t1 = f * p - n * h; t2 = f * o - n * g;
+	t3 = e * p - m * h; t4 = e * o - m * g; t5 = e * n - m * f;
+	r.m[0][2] =   b * t0 - c * t1 + d * t2;
+	r.m[1][2] = -(a * t0 - c * t3 + d * t4);
+	r.m[2][2] =   a * t1 - b * t3 + d * t5;
+	r.m[3][2] = -(a * t2 - b * t4 + c * t5);
+
+	/* minors of columns 1 and 2 */
+	t0 = g * l - k * h; t1 = f * l - j * h; t2 = f * k - j * g;
+	t3 = e * l - i * h; t4 = e * k - i * g; t5 = e * j - i * f;
+	r.m[0][3] = -(b * t0 - c * t1 + d * t2);
+	r.m[1][3] =   a * t0 - c * t3 + d * t4;
+	r.m[2][3] = -(a * t1 - b * t3 + d * t5);
+	r.m[3][3] =   a * t2 - b * t4 + c * t5;
+
+	const float det = a * r.m[0][0] + b * r.m[1][0] + c * r.m[2][0] + d * r.m[3][0];
+	if (det == 0.0f) {
+		memset(&r, 0, sizeof(r));
+		return r;
+	}
+	const float s = 1.0f / det;
+	for (int col = 0; col < 4; col++)
+		for (int row = 0; row < 4; row++) r.m[col][row] = r.m[col][row] * s;
+	return r;
+}
+
+DNmat4 DN_mat4_translate(DNvec3 t)
+{
+	DNmat4 r = DN_mat4_identity();
+	r.m[3][0] = t.x; r.m[3][1] = t.y; r.m[3][2] = t.z;
+	return r;
+}
+
+DNquaternion DN_quaternion_identity(void)
+{
+	DNquaternion q = {{0.0f, 0.0f, 0.0f, 1.0f}};
+	return q;
+}
+
+DNquaternion DN_quaternion_from_euler(DNvec3 a)
+{
+	/* half angles; q = qx * qy * qz expanded (the reference's shape examples build orientations this
+	 * way, main.c:107-108), each product evaluated as (x-term * y-term) * z-term */
+	const float hx = DN_deg_to_rad(a.x * 0.5f), hy = DN_deg_to_rad(a.y * 0.5f), hz = DN_deg_to_rad(a.z * 0.5f);
+	const float sx = sinf(hx), cx = cosf(hx), sy = sinf(hy), cy = cosf(hy), sz = sinf(hz), cz = cosf(hz);
+	DNquaternion q;
+	q.x = sx * cy * cz - cx * sy * sz;
+	q.y = cx * sy * cz + sx * cy * sz;
+	q.z = cx * cy * sz - sx * sy * cz;
+	q.w = cx * cy * cz + sx * sy * sz;
+	return q;
+}
+
+DNmat4 DN_quaternion_to_mat4(DNquaternion q)
+{
+	/* rotation matrix of a unit quaternion from the doubled products (x2 = 2x etc.), stored so that
+	 * m[0][1] = 2(xy - wz): the transpose of the matrix that rotates column vectors by q, which is the
+	 * layout the reference's shape transforms are built from (voxelShapes.c:323-324) */
+	const float x2 = q.x + q.x, y2 = q.y + q.y, z2 = q.z + q.z;
+	const float xx = q.x * x2, xy = q.x * y2, xz = q.x * z2;
+	const float yy = q.y * y2, yz = q.y * z2, zz = q.z * z2;
+	const float wx = q.w * x2, wy = q.w * y2, wz = q.w * z2;
+	DNmat4 r = DN_mat4_identity();
+	r.m[0][0] = 1.0f - (yy + zz); r.m[0][1] = xy - wz;          r.m[0][2] = xz + wy;
+	r.m[1][0] = xy + wz;          r.m[1][1] = 1.0f - (xx + zz); r.m[1][2] = yz - wx;
+	r.m[2][0] = xz - wy;          r.m[2][1] = yz + wx;          r.m[2][2] = 1.0f - (xx + yy);
 	return r;
 }

@@ -1207,6 +1207,27 @@ size_t DN_abi_layout(uint64_t* out, size_t n)
 	return k;
 }
 
+void DN_export_voxels(const DNvolume* vol, uint32_t* normalWords, uint32_t* albedoWords, uint8_t* tileFlags)
+{
+	const uint32_t X = vol->mapSize.x * DN_CHUNK_SIZE, Y = vol->mapSize.y * DN_CHUNK_SIZE;
+	for (uint32_t tz = 0; tz < vol->mapSize.z; tz++)
+	for (uint32_t ty = 0; ty < vol->mapSize.y; ty++)
+	for (uint32_t tx = 0; tx < vol->mapSize.x; tx++) {
+		const size_t t = tx + (size_t)vol->mapSize.x * (ty + (size_t)vol->mapSize.y * tz);
+		const DNchunkHandle h = vol->map[t];
+		if (tileFlags) tileFlags[t] = (uint8_t)h.flag;
+		const DNchunk* c = h.flag ? &vol->chunks[h.chunkIndex] : NULL;
+		for (uint32_t z = 0; z < DN_CHUNK_SIZE; z++)
+		for (uint32_t y = 0; y < DN_CHUNK_SIZE; y++)
+		for (uint32_t x = 0; x < DN_CHUNK_SIZE; x++) {
+			const size_t v = (tx * 8 + x) + (size_t)X * ((ty * 8 + y) + (size_t)Y * (tz * 8 + z));
+			const DNcompressedVoxel w = c ? c->voxels[x][y][z] : (DNcompressedVoxel){0xFFFFFFFFu, 0u};
+			normalWords[v] = w.normal;
+			albedoWords[v] = GET_MATERIAL_ID(w.normal) == DN_MATERIAL_EMPTY ? 0u : w.albedo;
+		}
+	}
+}
+
 /* addition: the chunk packing DN_sync_gpu applies to every changed chunk (voxel.c:1397-1461), exported
  * for tests and tools: mask[16], partial[3], 2 words per surface voxel; returns the voxel count */
 uint32_t dn_pack_chunk(const DNvolume* vol, const DNchunk* chunk, uint32_t mask[16], uint32_t partial[3], uint32_t* words)

@@ -282,6 +282,39 @@ class Volume:
     def shapes(self, seed, n, min_size, max_size, n_materials=14, y_lo=0.0, y_hi=0.5):
         self.lib.dn_scene_shapes(self.ptr, seed, n, min_size, max_size, n_materials, y_lo, y_hi)
 
+    # shapes (include/DoonEngine/voxelShapes.h); voxel = (material, normal, albedo), orient = Euler degrees
+    _SHAPES = {"sphere": 0, "box": 1, "rounded_box": 2, "torus": 3, "ellipsoid": 4, "cylinder": 5, "cone": 6,
+               "pyramid": 7}
+
+    def shape(self, kind, voxel, c, v=(0.0, 0.0, 0.0), a=0.0, b=0.0, orient=(0.0, 0.0, 0.0), flip=False, func=None,
+              user=None):
+        """DN_shape_<kind>: sphere (c, a=r), box (c, v=len), rounded_box (c, v=len, a=r), torus (c, a=ra, b=rb),
+        ellipsoid (c, v=radii), cylinder (c, a=r, b=h), cone (base c, a=r, b=h), pyramid (base c, v=len);
+        func: a C VoxelTransformFunc pointer (or None)"""
+        vox = L.DNvoxel()
+        vox.material = voxel[0]
+        vox.normal = L.DNvec3(*voxel[1])
+        vox.albedo = L.DNcolor(*voxel[2])
+        q = self.lib.DN_quaternion_from_euler(L.DNvec3(*orient))
+        cv, vv = L.DNvec3(*c), L.DNvec3(*v)
+        k = kind if isinstance(kind, int) else self._SHAPES[kind]
+        f = self.lib
+        args = {0: (f.DN_shape_sphere, (cv, a)), 1: (f.DN_shape_box, (cv, vv)), 2: (f.DN_shape_rounded_box, (cv, vv, a)),
+                3: (f.DN_shape_torus, (cv, a, b)), 4: (f.DN_shape_ellipsoid, (cv, vv)),
+                5: (f.DN_shape_cylinder, (cv, a, b)), 6: (f.DN_shape_cone, (cv, a, b)), 7: (f.DN_shape_pyramid, (cv, vv))}
+        fn, rest = args[k]
+        fn(self.ptr, vox, bool(flip), *rest, q, func, user)
+
+    def export_voxels(self):
+        """(normal words, albedo words, tile flags) of the CPU map, dense"""
+        sx, sy, sz = self.map_size
+        n = 512 * sx * sy * sz
+        nw = np.zeros(n, np.uint32)
+        aw = np.zeros(n, np.uint32)
+        tf = np.zeros(sx * sy * sz, np.uint8)
+        self.lib.DN_export_voxels(self.ptr, nw.ctypes.data, aw.ctypes.data, tf.ctypes.data)
+        return nw, aw, tf
+
     def camera(self, fx, fy, fz, pitch, yaw, fov=90.0):
         self.lib.dn_scene_camera(self.ptr, fx, fy, fz, pitch, yaw, fov)
 

@@ -20,6 +20,7 @@ typedef union DNvec3 { float v[3]; struct { float x, y, z; }; struct { float r, 
 typedef union DNvec4 { float v[4]; struct { float x, y, z, w; }; } DNvec4;
 typedef union DNmat3 { float m[3][3]; } DNmat3;     /* column-major m[col][row] */
 typedef union DNmat4 { float m[4][4]; } DNmat4;     /* column-major m[col][row] */
+typedef union DNquaternion { float q[4]; struct { float x, y, z, w; }; } DNquaternion;   /* w the real part */
 
 float DN_deg_to_rad(float deg);
 DNvec3 DN_vec3_add(DNvec3 a, DNvec3 b);
@@ -43,6 +44,14 @@ DNmat4 DN_mat4_perspective(float fovDeg, float aspect, float nearPlane, float fa
 DNmat4 DN_mat4_lookat(DNvec3 pos, DNvec3 target, DNvec3 up);
 /* general 4x4 inverse by cofactor expansion; a singular matrix returns all zeros */
 DNmat4 DN_mat4_inv(DNmat4 m);
+/* translation by t */
+DNmat4 DN_mat4_translate(DNvec3 t);
+DNquaternion DN_quaternion_identity(void);
+/* rotation from Euler angles in degrees {x, y, z}: the product of the three half-angle rotations about x,
+ * y and z, written out component by component */
+DNquaternion DN_quaternion_from_euler(DNvec3 anglesDeg);
+/* rotation matrix of a unit quaternion, m[0][1] = 2(xy - wz) (the layout the shape functions use) */
+DNmat4 DN_quaternion_to_mat4(DNquaternion q);
 
 #ifdef __cplusplus
 }

@@ -253,6 +253,11 @@ int DN_texture_format(int texture);
 /* the texture's device buffer, for a CUDA rasteriser that writes it in place (NULL for a bad handle) */
 float* DN_texture_device_pointer(int texture, uint32_t* width, uint32_t* height);
 
+/* addition: a dense copy of the CPU map (tools, tests): per voxel x + 8X*(y + 8Y*z) of the whole map the
+ * compressed normal word (0xFFFFFFFF where the tile has no chunk) and albedo word (0 for empty voxels);
+ * tileFlags (may be NULL) the DNchunkHandle flag of every tile */
+void DN_export_voxels(const DNvolume* vol, uint32_t* normalWords, uint32_t* albedoWords, uint8_t* tileFlags);
+
 /* The inverse matrices DN_draw derives from view / projection
  * (voxel.c:845-853): inverse view, inverse view without translation,
  * inverse projection. */

@@ -234,6 +234,46 @@ int dn_cuda_export_requests(struct DNgpuVolume* g, uint32_t* out, uint64_t capac
 int dn_cuda_export_lighting(struct DNgpuVolume* g, uint32_t* index, float* diff, float* spec,
                             uint64_t capacity, uint64_t* count);
 
+/* --- shapes: the per-voxel signed-distance pass of the shape functions (voxelShapes.c:150-441) over the
+ *     chunk range a shape covers, on the device.  The host applies the resulting edits to the CPU map in
+ *     the reference's order (voxelShapes.c:183-232), so the map's contents are the reference's. --- */
+enum {
+    DN_SHAPE_SPHERE = 0, DN_SHAPE_BOX = 1, DN_SHAPE_ROUNDED_BOX = 2, DN_SHAPE_TORUS = 3,
+    DN_SHAPE_ELLIPSOID = 4, DN_SHAPE_CYLINDER = 5, DN_SHAPE_CONE = 6, DN_SHAPE_PYRAMID = 7
+};
+typedef struct dn_shape_params {
+    uint32_t kind;              /* DN_SHAPE_* */
+    uint32_t removing;          /* the placed voxel is empty: inside voxels need no normal */
+    uint32_t flipNormals;       /* with removing: also report the shell (distance in [0, 1)) */
+    float invTransform[4][4];   /* voxel coordinates -> shape space, column-major */
+    float center[3];            /* sphere centre */
+    float r2, r12;              /* sphere: r*r and (r+1)*(r+1) */
+    float radius, radiusB, height;
+    float angles[2];            /* cone: (h, r) / sqrt(r*r + h*h) */
+    float radii[3];             /* ellipsoid semi-axes */
+    float length[3];            /* box / rounded box half extents; pyramid base (x, z) */
+    int32_t chunkMin[3], chunkMax[3];   /* inclusive chunk range, inside the map */
+} dn_shape_params;
+
+/* a voxel the shape touches: local = x + 8*(y + 8*z) within its chunk; inside 1 (distance < 0) or 0 (a
+ * shell voxel of a removal with flipped normals); normal as the reference computes it before flipping
+ * (zero for inside voxels of a removal) */
+typedef struct dn_shape_hit {
+    uint16_t local;
+    uint8_t inside;
+    uint8_t pad;
+    float normal[3];
+} dn_shape_hit;
+
+/* Evaluates p over every voxel of its chunk range on the current device (synchronous).  counts (host,
+ * one per chunk of the range, chunk i = x + nx*(y + ny*z) relative to chunkMin) receives each chunk's hit
+ * count; *hits (allocated here, freed with dn_cuda_shape_free) the hits of all chunks in chunk order,
+ * each chunk's in voxel order z, y, x; *total their number. */
+int dn_cuda_shape_eval(const dn_shape_params* p, uint32_t* counts, dn_shape_hit** hits, uint64_t* total);
+void dn_cuda_shape_free(dn_shape_hit* hits);
+/* voxels evaluated and device time of the evaluation kernels (both passes) since the last reset */
+void dn_cuda_shape_stats(uint64_t* voxels, double* deviceMs, int reset);
+
 /* device / pinned memory and event helpers for callers without their own CUDA runtime */
 int dn_cuda_malloc(void** p, size_t bytes);
 int dn_cuda_free(void* p);

@@ -241,6 +241,33 @@ uint32_t dno_hash32(uint32_t x);
 /* K-point golden-angle sphere, computed in double and rounded to float */
 void dno_sphere_points(uint32_t K, float out[][3]);
 
+/* Shapes (dno_shapes.c): the reference's shape functions (voxelShapes.c:23-442) on a dense map.  The
+ * caller gives each shape's transform and inverse; every kind takes its centre (base for the cone and
+ * the pyramid) in c and, by kind: sphere a = r; box v = len; rounded box v = len, a = r; torus a = ra,
+ * b = rb; ellipsoid v = radii; cylinder a = r, b = h; cone a = r, b = h; pyramid v = len. */
+enum { DNO_SHAPE_SPHERE = 0, DNO_SHAPE_BOX, DNO_SHAPE_ROUNDED_BOX, DNO_SHAPE_TORUS, DNO_SHAPE_ELLIPSOID,
+       DNO_SHAPE_CYLINDER, DNO_SHAPE_CONE, DNO_SHAPE_PYRAMID };
+typedef struct dno_shape_op {
+    int32_t kind, flip;
+    uint8_t material, albedo[3];      /* the placed voxel (255 = empty: a removal) */
+    float normal[3];                  /* its own normal, kept by removals */
+    float c[3], v[3];
+    float a, b;
+    float transform[4][4], invTransform[4][4];
+} dno_shape_op;
+typedef struct dno_shape_hit { uint16_t local; uint8_t inside, pad; float normal[3]; } dno_shape_hit;
+/* the shape's bounding box after its transform (the sphere's is not transformed) */
+void dno_shape_bounds(const dno_shape_op* op, float mn[3], float mx[3]);
+/* the covered chunk range inside the map; 0 when empty */
+int dno_shape_range(const dno_shape_op* op, const uint32_t mapSize[3], int32_t cmin[3], int32_t cmax[3]);
+/* per-chunk hit counts and the hits (up to capacity) in chunk then voxel order; returns the total */
+uint64_t dno_shape_eval(const dno_shape_op* op, const int32_t cmin[3], const int32_t cmax[3], uint32_t* counts,
+                        dno_shape_hit* hits, uint64_t capacity);
+/* applies the hits to a dense map: normal / albedo words per voxel (x + 8X*(y + 8Y*z)), voxel count per tile */
+void dno_shape_apply(const dno_shape_op* op, const uint32_t mapSize[3], const int32_t cmin[3], const int32_t cmax[3],
+                     const uint32_t* counts, const dno_shape_hit* hits, uint32_t* normalWords, uint32_t* albedoWords,
+                     int32_t* tileCount);
+
 #ifdef __cplusplus
 }
 #endif

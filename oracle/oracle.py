@@ -11,7 +11,7 @@ import ctypes
 import os
 import platform
 import subprocess
-from ctypes import POINTER, Structure, c_float, c_int, c_uint8, c_uint32, c_uint64, c_void_p
+from ctypes import POINTER, Structure, c_float, c_int, c_int32, c_uint8, c_uint16, c_uint32, c_uint64, c_void_p
 
 import numpy as np
 
@@ -45,6 +45,17 @@ class Counters(Structure):
                 ("innerSteps", c_uint64), ("hits", c_uint64), ("litVoxels", c_uint64)]
 
 
+class ShapeOp(Structure):
+    """dno_shape_op of dn_oracle.h"""
+    _fields_ = [("kind", c_int32), ("flip", c_int32), ("material", c_uint8), ("albedo", c_uint8 * 3),
+                ("normal", c_float * 3), ("c", c_float * 3), ("v", c_float * 3), ("a", c_float), ("b", c_float),
+                ("transform", (c_float * 4) * 4), ("invTransform", (c_float * 4) * 4)]
+
+
+# dno_shape_hit of dn_oracle.h (the layout of the product's dn_shape_hit)
+SHAPE_HIT = np.dtype([("local", "<u2"), ("inside", "u1"), ("pad", "u1"), ("normal", "<f4", 3)])
+
+
 _lib = None
 
 
@@ -65,7 +76,8 @@ def load():
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(os.path.join(HERE, "dn_oracle.c")):
+    srcs = [os.path.join(HERE, f) for f in ("dn_oracle.c", "dno_shapes.c", "dn_oracle.h")]
+    if not os.path.exists(LIB) or any(os.path.getmtime(LIB) < os.path.getmtime(p) for p in srcs):
         build()
     lib = ctypes.CDLL(LIB)
     sigs = [
@@ -94,6 +106,11 @@ def load():
         ("dno_sin", c_float, [c_float]),
         ("dno_hash32", c_uint32, [c_uint32]),
         ("dno_sphere_points", None, [c_uint32, c_void_p]),
+        ("dno_shape_bounds", None, [POINTER(ShapeOp), c_void_p, c_void_p]),
+        ("dno_shape_range", c_int, [POINTER(ShapeOp), c_void_p, c_void_p, c_void_p]),
+        ("dno_shape_eval", c_uint64, [POINTER(ShapeOp), c_void_p, c_void_p, c_void_p, c_void_p, c_uint64]),
+        ("dno_shape_apply", None, [POINTER(ShapeOp), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                   c_void_p, c_void_p]),
     ]
     for n, r, a in sigs:
         f = getattr(lib, n)
@@ -285,3 +302,63 @@ class OracleMap:
     def import_samples(self, samples):
         samples = np.ascontiguousarray(samples, np.uint32)
         self.lib.dno_import_samples(self.ptr, samples.ctypes.data)
+
+
+class DenseShapes:
+    """A dense CPU map (normal / albedo words per voxel, voxel count per tile) edited by the oracle's
+    restatement of the reference's shape functions."""
+
+    def __init__(self, map_size):
+        self.lib = load()
+        self.size = np.array(map_size, np.uint32)
+        n = int(8 * self.size[0] * 8 * self.size[1] * 8 * self.size[2])
+        self.normal = np.full(n, 0xFFFFFFFF, np.uint32)
+        self.albedo = np.zeros(n, np.uint32)
+        self.count = np.zeros(int(self.size.prod()), np.int32)
+
+    @staticmethod
+    def op(kind, flip, material, albedo, normal, c, v, a, b, transform, inv):
+        o = ShapeOp()
+        o.kind, o.flip, o.material = kind, flip, material
+        o.albedo[:], o.normal[:], o.c[:], o.v[:] = list(albedo), list(normal), list(c), list(v)
+        o.a, o.b = a, b
+        t = np.asarray(transform, np.float32).reshape(4, 4)
+        it = np.asarray(inv, np.float32).reshape(4, 4)
+        for col in range(4):
+            o.transform[col][:] = t[col].tolist()
+            o.invTransform[col][:] = it[col].tolist()
+        return o
+
+    def bounds(self, o):
+        mn = np.zeros(3, np.float32)
+        mx = np.zeros(3, np.float32)
+        self.lib.dno_shape_bounds(ctypes.byref(o), mn.ctypes.data, mx.ctypes.data)
+        return mn, mx
+
+    def evaluate(self, o):
+        """(cmin, cmax, counts, hits) of the shape on this map, or None when it covers no chunk"""
+        cmin = np.zeros(3, np.int32)
+        cmax = np.zeros(3, np.int32)
+        if not self.lib.dno_shape_range(ctypes.byref(o), self.size.ctypes.data, cmin.ctypes.data, cmax.ctypes.data):
+            return None
+        nch = int(np.prod(cmax - cmin + 1))
+        counts = np.zeros(nch, np.uint32)
+        total = self.lib.dno_shape_eval(ctypes.byref(o), cmin.ctypes.data, cmax.ctypes.data, counts.ctypes.data, None, 0)
+        hits = np.zeros(max(1, total), SHAPE_HIT)
+        self.lib.dno_shape_eval(ctypes.byref(o), cmin.ctypes.data, cmax.ctypes.data, counts.ctypes.data,
+                                hits.ctypes.data, total)
+        return cmin, cmax, counts, hits[:total]
+
+    def apply(self, o):
+        ev = self.evaluate(o)
+        if ev is None:
+            return None
+        cmin, cmax, counts, hits = ev
+        hits = np.ascontiguousarray(hits) if len(hits) else np.zeros(1, SHAPE_HIT)
+        self.lib.dno_shape_apply(ctypes.byref(o), self.size.ctypes.data, cmin.ctypes.data, cmax.ctypes.data,
+                                 counts.ctypes.data, hits.ctypes.data, self.normal.ctypes.data, self.albedo.ctypes.data,
+                                 self.count.ctypes.data)
+        return ev
+
+    def tile_flags(self):
+        return (self.count != 0).astype(np.uint8)

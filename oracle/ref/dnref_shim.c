@@ -16,6 +16,7 @@
 #include <string.h>
 #include <math.h>
 #include "voxel.c"
+#include "voxelShapes.c"
 
 #define EXPORT __attribute__((visibility("default")))
 
@@ -166,4 +167,90 @@ EXPORT uint32_t ref_compress_chunk(DNvolume* vol, const DNchunk* chunk, char* me
 EXPORT void ref_decompress_chunk(DNvolume* vol, const char* mem, DNchunk* out)
 {
     _DN_decompress_chunk((char*)mem, vol, out);
+}
+
+/* ---- shapes, voxelShapes.c:239-442 ---- */
+
+/* one shape call: kind 0 sphere (c, a = r), 1 box (c, v = len), 2 rounded box (c, v, a = r), 3 torus
+ * (c, a = ra, b = rb), 4 ellipsoid (c, v = radii), 5 cylinder (c, a = r, b = h), 6 cone (base c, a = r,
+ * b = h), 7 pyramid (base c, v = len); orientation from Euler angles in degrees */
+typedef struct ref_shape_op {
+    int32_t kind, flip, transform;   /* transform: 1 passes ref_shape_transform as the transform function */
+    uint8_t material, albedo[3];
+    float normal[3], c[3], v[3], a, b, euler[3];
+} ref_shape_op;
+
+/* the transform function of the shape tests: colour from the position in shape space, material from the
+ * side the normal faces, the normal kept */
+static DNvoxel ref_shape_transform(DNvec3 pos, DNvec3 normal, DNvoxel vox, DNvec3 mn, DNvec3 mx, DNmat4 inv, void* user)
+{
+    (void)user;
+    DNvec4 lp = DN_mat4_mult_vec4(inv, (DNvec4){{pos.x, pos.y, pos.z, 1.0f}});
+    vox.normal = normal;
+    vox.albedo.r = (uint8_t)((int)floorf(lp.x * 8.0f) & 255);
+    vox.albedo.g = (uint8_t)((int)floorf(lp.y * 8.0f) & 255);
+    vox.albedo.b = (uint8_t)((int)floorf((pos.z - mn.z) * 4.0f + mx.x) & 255);
+    vox.material = normal.y > 0.0f ? 3 : 4;
+    return vox;
+}
+
+EXPORT void ref_shape_run(DNvolume* vol, const ref_shape_op* op)
+{
+    DNvoxel vox;
+    vox.material = op->material;
+    vox.normal = (DNvec3){{op->normal[0], op->normal[1], op->normal[2]}};
+    vox.albedo = (DNcolor){op->albedo[0], op->albedo[1], op->albedo[2]};
+    DNquaternion q = DN_quaternion_from_euler((DNvec3){{op->euler[0], op->euler[1], op->euler[2]}});
+    DNvec3 c = {{op->c[0], op->c[1], op->c[2]}}, v = {{op->v[0], op->v[1], op->v[2]}};
+    VoxelTransformFunc f = op->transform ? ref_shape_transform : NULL;
+    switch (op->kind) {
+    case 0: DN_shape_sphere(vol, vox, op->flip, c, op->a, q, f, NULL); break;
+    case 1: DN_shape_box(vol, vox, op->flip, c, v, q, f, NULL); break;
+    case 2: DN_shape_rounded_box(vol, vox, op->flip, c, v, op->a, q, f, NULL); break;
+    case 3: DN_shape_torus(vol, vox, op->flip, c, op->a, op->b, q, f, NULL); break;
+    case 4: DN_shape_ellipsoid(vol, vox, op->flip, c, v, q, f, NULL); break;
+    case 5: DN_shape_cylinder(vol, vox, op->flip, c, op->a, op->b, q, f, NULL); break;
+    case 6: DN_shape_cone(vol, vox, op->flip, c, op->a, op->b, q, f, NULL); break;
+    case 7: DN_shape_pyramid(vol, vox, op->flip, c, v, q, f, NULL); break;
+    }
+}
+
+/* the quaternion, translate * rotation and its inverse of a shape call (the cone's translation is its
+ * apex), as DN_shape_* builds them */
+EXPORT void ref_shape_matrices(const ref_shape_op* op, float q[4], float transform[16], float inv[16])
+{
+    DNquaternion qq = DN_quaternion_from_euler((DNvec3){{op->euler[0], op->euler[1], op->euler[2]}});
+    DNmat4 rot = DN_quaternion_to_mat4(qq);
+    DNvec3 at = {{op->c[0], op->c[1], op->c[2]}};
+    if (op->kind == 6) {
+        DNvec4 up = DN_mat4_mult_vec4(rot, (DNvec4){{0.0f, 1.0f, 0.0f, 1.0f}});
+        at = DN_vec3_add(at, DN_vec3_scale((DNvec3){{up.x, up.y, up.z}}, op->b));
+    }
+    DNmat4 t = DN_mat4_mult(DN_mat4_translate(at), rot);
+    DNmat4 it = DN_mat4_inv(t);
+    memcpy(q, &qq, 16);
+    memcpy(transform, t.m, 64);
+    memcpy(inv, it.m, 64);
+}
+
+/* dense copy of the CPU map: normal word per voxel (0xFFFFFFFF where the tile has no chunk), albedo word
+ * (0 for empty voxels), flag per tile */
+EXPORT void ref_export_voxels(const DNvolume* vol, uint32_t* normalWords, uint32_t* albedoWords, uint8_t* tileFlags)
+{
+    const uint32_t X = vol->mapSize.x * 8, Y = vol->mapSize.y * 8;
+    for (uint32_t tz = 0; tz < vol->mapSize.z; tz++)
+    for (uint32_t ty = 0; ty < vol->mapSize.y; ty++)
+    for (uint32_t tx = 0; tx < vol->mapSize.x; tx++) {
+        const size_t t = tx + (size_t)vol->mapSize.x * (ty + (size_t)vol->mapSize.y * tz);
+        tileFlags[t] = vol->map[t].flag;
+        const DNchunk* c = vol->map[t].flag ? &vol->chunks[vol->map[t].chunkIndex] : NULL;
+        for (uint32_t z = 0; z < 8; z++)
+        for (uint32_t y = 0; y < 8; y++)
+        for (uint32_t x = 0; x < 8; x++) {
+            const size_t i = (tx * 8 + x) + (size_t)X * ((ty * 8 + y) + (size_t)Y * (tz * 8 + z));
+            const DNcompressedVoxel w = c ? c->voxels[x][y][z] : (DNcompressedVoxel){UINT32_MAX, 0};
+            normalWords[i] = w.normal;
+            albedoWords[i] = (w.normal >> 24) == DN_MATERIAL_EMPTY ? 0u : w.albedo;
+        }
+    }
 }

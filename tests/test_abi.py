@@ -14,7 +14,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared_functions():
     names = set()
     for hdr in ("include/dn_cuda.h", "include/DoonEngine/voxel.h", "include/DoonEngine/dn_math.h",
-                "include/DoonEngine/globals.h"):
+                "include/DoonEngine/globals.h", "include/DoonEngine/serve.h", "include/DoonEngine/voxelShapes.h"):
         txt = open(os.path.join(ROOT, hdr)).read()
         txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
         txt = re.sub(r"//[^\n]*", "", txt)
