@@ -19,7 +19,6 @@
 #include "dn_internal.cuh"
 #include <stdlib.h>
 #include <string.h>
-#include <vector>
 
 namespace {
 
@@ -197,6 +196,117 @@ extern "C" void dn_cuda_shape_stats(uint64_t* voxels, double* deviceMs, int rese
     if (reset) { g_shapeVoxels = 0; g_shapeMs = 0.0; }
 }
 
+namespace {
+
+// Per-thread buffers of the evaluation, grown as needed and kept between calls (a shape call then costs
+// two launches and three copies, no allocation): device counts / offsets / hits, pinned host offsets and
+// hits, a stream and four timing events.  A shape call made from inside a transform function while the
+// thread's buffers are still lent out (between dn_cuda_shape_eval and dn_cuda_shape_free) uses buffers
+// of its own for that call.  The buffers are not freed at thread exit.
+struct ShapeScratch {
+    bool busy;
+    int device;
+    cudaStream_t stream;
+    cudaEvent_t ev[4];
+    uint32_t* dcounts; size_t nCounts;
+    uint64_t* doffsets; size_t nOffsets;
+    dn_shape_hit* dhits; size_t nHits;
+    uint64_t* hoffsets; size_t nHOffsets;
+    dn_shape_hit* hhits; size_t nHHits;
+};
+thread_local ShapeScratch t_scratch = {};
+
+template <class T> int grow_device(T*& p, size_t& cap, size_t need)
+{
+    if (need <= cap && p) return DN_CUDA_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    const size_t n = need < 1024 ? 1024 : need + need / 2;
+    CK(cudaMalloc((void**)&p, n * sizeof(T)));
+    cap = n;
+    return DN_CUDA_OK;
+}
+
+template <class T> int grow_pinned(T*& p, size_t& cap, size_t need)
+{
+    if (need <= cap && p) return DN_CUDA_OK;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    const size_t n = need < 1024 ? 1024 : need + need / 2;
+    CK(cudaMallocHost((void**)&p, n * sizeof(T)));
+    cap = n;
+    return DN_CUDA_OK;
+}
+
+int scratch_ready(ShapeScratch& sc)
+{
+    if (sc.device == g_device && sc.stream) return DN_CUDA_OK;
+    sc = ShapeScratch{};     // buffers of another device are left to it
+    CK(cudaStreamCreateWithFlags(&sc.stream, cudaStreamNonBlocking));
+    for (auto& e : sc.ev) CK(cudaEventCreate(&e));
+    sc.device = g_device;
+    return DN_CUDA_OK;
+}
+
+// the two passes on sc; hits land in sc.hhits (pinned)
+int shape_eval_on(ShapeScratch& sc, const ShapeArgs& proto, int64_t nchunks, uint32_t* counts, uint64_t* total)
+{
+    ShapeArgs a = proto;
+    int rc = grow_device(sc.dcounts, sc.nCounts, (size_t)nchunks);
+    if (!rc) rc = grow_device(sc.doffsets, sc.nOffsets, (size_t)nchunks);
+    if (!rc) rc = grow_pinned(sc.hoffsets, sc.nHOffsets, (size_t)nchunks);
+    if (rc) return rc;
+    a.counts = sc.dcounts;
+    COUNT_LAUNCH();
+    CK(cudaEventRecord(sc.ev[0], sc.stream));
+    k_shape_count<<<(unsigned)nchunks, 512, 0, sc.stream>>>(a);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(sc.ev[1], sc.stream));
+    CK(cudaMemcpyAsync(counts, sc.dcounts, (size_t)nchunks * 4, cudaMemcpyDeviceToHost, sc.stream));
+    CK(cudaStreamSynchronize(sc.stream));
+    float msCount = 0.0f, msWrite = 0.0f;
+    cudaEventElapsedTime(&msCount, sc.ev[0], sc.ev[1]);
+    uint64_t sum = 0;
+    for (int64_t i = 0; i < nchunks; i++) { sc.hoffsets[i] = sum; sum += counts[i]; }
+    if (sum) {
+        rc = grow_device(sc.dhits, sc.nHits, (size_t)sum);
+        if (!rc) rc = grow_pinned(sc.hhits, sc.nHHits, (size_t)sum);
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(sc.doffsets, sc.hoffsets, (size_t)nchunks * 8, cudaMemcpyHostToDevice, sc.stream));
+        a.offsets = sc.doffsets;
+        a.hits = sc.dhits;
+        a.capacity = sum;
+        COUNT_LAUNCH();
+        CK(cudaEventRecord(sc.ev[2], sc.stream));
+        k_shape_write<<<(unsigned)nchunks, 512, 0, sc.stream>>>(a);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(sc.ev[3], sc.stream));
+        CK(cudaMemcpyAsync(sc.hhits, sc.dhits, (size_t)sum * sizeof(dn_shape_hit), cudaMemcpyDeviceToHost, sc.stream));
+        CK(cudaStreamSynchronize(sc.stream));
+        cudaEventElapsedTime(&msWrite, sc.ev[2], sc.ev[3]);
+    } else if (!sc.hhits) {
+        rc = grow_pinned(sc.hhits, sc.nHHits, 1);
+        if (rc) return rc;
+    }
+    g_shapeMs += (double)msCount + (double)msWrite;
+    g_shapeVoxels += (unsigned long long)nchunks * 512ull;
+    *total = sum;
+    return DN_CUDA_OK;
+}
+
+void scratch_release(ShapeScratch& sc)
+{
+    for (auto& e : sc.ev) if (e) cudaEventDestroy(e);
+    if (sc.stream) cudaStreamDestroy(sc.stream);
+    cudaFree(sc.dcounts); cudaFree(sc.doffsets); cudaFree(sc.dhits);
+    cudaFreeHost(sc.hoffsets);
+    sc = ShapeScratch{};
+}
+
+}  // namespace
+
 extern "C" int dn_cuda_shape_eval(const dn_shape_params* p, uint32_t* counts, dn_shape_hit** hits, uint64_t* total)
 {
     if (!p || !counts || !hits || !total) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
@@ -217,63 +327,35 @@ extern "C" int dn_cuda_shape_eval(const dn_shape_params* p, uint32_t* counts, dn
     a.p = *p;
     a.nx = (uint32_t)n[0];
     a.ny = (uint32_t)n[1];
-    uint32_t* dcounts = nullptr;
-    uint64_t* doffsets = nullptr;
-    dn_shape_hit* dhits = nullptr;
-    int rc = dalloc(&dcounts, (size_t)nchunks);
+    ShapeScratch& sc = t_scratch;
+    if (!sc.busy) {
+        int rc = scratch_ready(sc);
+        if (!rc) rc = shape_eval_on(sc, a, nchunks, counts, total);
+        if (rc) return rc;
+        sc.busy = true;
+        *hits = sc.hhits;
+        return DN_CUDA_OK;
+    }
+    // nested call (from a transform function): buffers of its own, the hits copied to malloc'd memory
+    ShapeScratch tmp = {};
+    int rc = scratch_ready(tmp);
+    if (!rc) rc = shape_eval_on(tmp, a, nchunks, counts, total);
+    dn_shape_hit* out = nullptr;
+    if (!rc) {
+        out = (dn_shape_hit*)malloc((size_t)(*total ? *total : 1) * sizeof(dn_shape_hit));
+        if (!out) rc = dn_set_err(DN_CUDA_ERR_NOMEM, "no host memory for %llu shape hits", (unsigned long long)*total);
+        else memcpy(out, tmp.hhits, (size_t)*total * sizeof(dn_shape_hit));
+    }
+    cudaFreeHost(tmp.hhits);
+    scratch_release(tmp);
     if (rc) return rc;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    for (auto& x : ev) cudaEventCreate(&x);
-    a.counts = dcounts;
-    COUNT_LAUNCH();
-    cudaEventRecord(ev[0]);
-    k_shape_count<<<(unsigned)nchunks, 512>>>(a);
-    cudaEventRecord(ev[1]);
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpy(counts, dcounts, (size_t)nchunks * 4, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) {
-        dfree(dcounts);
-        for (auto& x : ev) cudaEventDestroy(x);
-        return dn_set_err(DN_CUDA_ERR_LAUNCH, "shape count pass: %s", cudaGetErrorString(e));
-    }
-    float msCount = 0.0f, msWrite = 0.0f;
-    cudaEventElapsedTime(&msCount, ev[0], ev[1]);
-    std::vector<uint64_t> off((size_t)nchunks);
-    uint64_t sum = 0;
-    for (int64_t i = 0; i < nchunks; i++) { off[(size_t)i] = sum; sum += counts[i]; }
-    dn_shape_hit* host = (dn_shape_hit*)malloc((size_t)(sum ? sum : 1) * sizeof(dn_shape_hit));
-    if (!host) { dfree(dcounts); return dn_set_err(DN_CUDA_ERR_NOMEM, "no host memory for %llu shape hits", (unsigned long long)sum); }
-    if (sum) {
-        rc = dalloc(&doffsets, (size_t)nchunks);
-        if (!rc) rc = dalloc(&dhits, (size_t)sum);
-        if (rc) { dfree(dcounts); dfree(doffsets); free(host); return rc; }
-        e = cudaMemcpy(doffsets, off.data(), (size_t)nchunks * 8, cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) {
-            a.offsets = doffsets;
-            a.hits = dhits;
-            a.capacity = sum;
-            COUNT_LAUNCH();
-            cudaEventRecord(ev[2]);
-            k_shape_write<<<(unsigned)nchunks, 512>>>(a);
-            cudaEventRecord(ev[3]);
-            e = cudaGetLastError();
-        }
-        if (e == cudaSuccess) e = cudaMemcpy(host, dhits, (size_t)sum * sizeof(dn_shape_hit), cudaMemcpyDeviceToHost);
-        if (e == cudaSuccess) cudaEventElapsedTime(&msWrite, ev[2], ev[3]);
-    }
-    for (auto& x : ev) cudaEventDestroy(x);
-    g_shapeMs += (double)msCount + (double)msWrite;
-    g_shapeVoxels += (unsigned long long)nchunks * 512ull;
-    dfree(dcounts);
-    dfree(doffsets);
-    dfree(dhits);
-    if (e != cudaSuccess) {
-        free(host);
-        return dn_set_err(DN_CUDA_ERR_LAUNCH, "shape write pass: %s", cudaGetErrorString(e));
-    }
-    *hits = host;
-    *total = sum;
+    *hits = out;
     return DN_CUDA_OK;
 }
 
-extern "C" void dn_cuda_shape_free(dn_shape_hit* hits) { free(hits); }
+extern "C" void dn_cuda_shape_free(dn_shape_hit* hits)
+{
+    ShapeScratch& sc = t_scratch;
+    if (sc.busy && hits == sc.hhits) sc.busy = false;
+    else free(hits);
+}

@@ -72,8 +72,18 @@ static bool chunk_range(const DNvolume* vol, DNvec3 min, DNvec3 max, bool removi
 	return true;
 }
 
+/* the voxel word at (tile t, cp) as DN_get_compressed_voxel reads it: empty where the tile has no chunk */
+static inline DNcompressedVoxel word_at(const DNvolume* vol, size_t t, DNivec3 cp)
+{
+	const DNchunkHandle h = vol->map[t];
+	if (!h.flag) return (DNcompressedVoxel){0xFFFFFFFFu, 0u};
+	return vol->chunks[h.chunkIndex].voxels[cp.x][cp.y][cp.z];
+}
+
 /* Applies evaluated hits to the CPU map (exported for tests).  counts: per chunk of the range
- * [cmin, cmax] in x-fastest order; hits: concatenated in that chunk order. */
+ * [cmin, cmax] in x-fastest order; hits: concatenated in that chunk order.  Without a transform function
+ * the rules are applied on the voxel words directly (DN_compress_voxel + DN_set_compressed_voxel, the
+ * steps DN_get_voxel / DN_set_voxel take); with one, through DN_get_voxel / DN_set_voxel. */
 void dn_shape_apply(DNvolume* vol, DNvoxel voxel, bool flipNormals, bool sphere, VoxelTransformFunc func,
                     void* userData, DNvec3 shapeMin, DNvec3 shapeMax, DNmat4 invTransform, const int32_t cmin[3],
                     const int32_t cmax[3], const uint32_t* counts, const dn_shape_hit* hits)
@@ -89,6 +99,30 @@ void dn_shape_apply(DNvolume* vol, DNvoxel voxel, bool flipNormals, bool sphere,
 		/* the tile as it was before this chunk's edits (voxelShapes.c:186) */
 		const DNchunkHandle tile = vol->map[DN_FLATTEN_INDEX(mapPos, vol->mapSize)];
 		const uint32_t n = counts[chunk++];
+		const size_t t = DN_FLATTEN_INDEX(mapPos, vol->mapSize);
+		if (!func) {
+			/* the placed voxel's word with its own normal (removals store it as is) */
+			const DNcompressedVoxel placed = DN_compress_voxel(voxel);
+			for (uint32_t i = 0; i < n; i++) {
+				const dn_shape_hit* e = &hits[at++];
+				const DNivec3 cp = {e->local & 7, (e->local >> 3) & 7, e->local >> 6};
+				const DNcompressedVoxel cur = word_at(vol, t, cp);
+				const bool exists = (cur.normal >> 24) != DN_MATERIAL_EMPTY;
+				DNvoxel v;
+				if (e->inside) {
+					if (tile.flag != 0 && exists && !removing) continue;
+					if (removing) { DN_set_compressed_voxel(vol, mapPos, cp, placed); continue; }
+					v = voxel;
+					v.normal = (DNvec3){{e->normal[0], e->normal[1], e->normal[2]}};
+				} else {
+					if (tile.flag == 0 || !exists) continue;
+					v = DN_decompress_voxel(cur);
+					v.normal = DN_vec3_scale((DNvec3){{e->normal[0], e->normal[1], e->normal[2]}}, -1.0f);
+				}
+				DN_set_compressed_voxel(vol, mapPos, cp, DN_compress_voxel(v));
+			}
+			continue;
+		}
 		for (uint32_t i = 0; i < n; i++) {
 			const dn_shape_hit* e = &hits[at++];
 			const DNivec3 cp = {e->local & 7, (e->local >> 3) & 7, e->local >> 6};

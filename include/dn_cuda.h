@@ -267,8 +267,9 @@ typedef struct dn_shape_hit {
 
 /* Evaluates p over every voxel of its chunk range on the current device (synchronous).  counts (host,
  * one per chunk of the range, chunk i = x + nx*(y + ny*z) relative to chunkMin) receives each chunk's hit
- * count; *hits (allocated here, freed with dn_cuda_shape_free) the hits of all chunks in chunk order,
- * each chunk's in voxel order z, y, x; *total their number. */
+ * count; *hits the hits of all chunks in chunk order, each chunk's in voxel order z, y, x; *total their
+ * number.  *hits stays valid until dn_cuda_shape_free(*hits), to be called once per successful call
+ * (the calling thread's buffers, reused by its next call). */
 int dn_cuda_shape_eval(const dn_shape_params* p, uint32_t* counts, dn_shape_hit** hits, uint64_t* total);
 void dn_cuda_shape_free(dn_shape_hit* hits);
 /* voxels evaluated and device time of the evaluation kernels (both passes) since the last reset */
