@@ -12,9 +12,11 @@
  *   pass 2 (k_shape_write): each edited voxel's record at its chunk's offset plus its rank among the
  *                           chunk's edited voxels in voxel order z, y, x (warp ballots + a block scan).
  * The host side (voxelShapes.c of this library) applies the list to the CPU map with the reference's
- * rules.  Every float operation is the reference's, in its order and type (a few of its steps run in
- * double through fmin / fmax), with no contraction, so the distances and normals are bit-identical to
- * the reference's x86 build.
+ * rules.  Every float operation is the reference's, in its order, with no contraction, so the distances
+ * and normals are bit-identical to the reference's x86 build.  Where the reference passes floats through
+ * double fmin / fmax / fabs or multiplies two of them in double, the single-precision operation gives the
+ * same float (a min / max returns one of its operands; the product of two floats is exact in double and
+ * is rounded once either way); only the cylinder's two double sums stay in double.
  */
 #include "dn_internal.cuh"
 #include <stdlib.h>
@@ -48,7 +50,7 @@ __device__ float shape_sdf(const dn_shape_params& p, V3 q)
     case DN_SHAPE_ROUNDED_BOX: {
         const float ax = fabsf(q.x) - p.length[0], ay = fabsf(q.y) - p.length[1], az = fabsf(q.z) - p.length[2];
         const float q1 = len3(gt_max(ax, 0.0f), gt_max(ay, 0.0f), gt_max(az, 0.0f));
-        const float q2 = (float)fmin(fmax(fmax((double)ax, (double)ay), (double)az), 0.0);
+        const float q2 = fminf(fmaxf(fmaxf(ax, ay), az), 0.0f);
         const float d = q1 + q2;
         return p.kind == DN_SHAPE_BOX ? d : d - p.radius;
     }
@@ -58,18 +60,18 @@ __device__ float shape_sdf(const dn_shape_params& p, V3 q)
     }
     case DN_SHAPE_ELLIPSOID: {
         const float l = len3(q.x / p.radii[0], q.y / p.radii[1], q.z / p.radii[2]);
-        const double m = fmin(fmin((double)p.radii[0], (double)p.radii[1]), (double)p.radii[2]);
-        return (float)((double)(l - 1.0f) * m);
+        return (l - 1.0f) * fminf(fminf(p.radii[0], p.radii[1]), p.radii[2]);
     }
     case DN_SHAPE_CYLINDER: {
+        // the two sums the reference forms in double (a float result rounded once more could differ)
         const float dx = len2(q.x, q.z) - p.radius, dy = (float)(fabs((double)q.y) - (double)p.height);
-        const double a = fmin(fmax((double)dx, (double)dy), 0.0);
-        return (float)(a + (double)len2(gt_max(dx, 0.0f), gt_max(dy, 0.0f)));
+        const float a = fminf(fmaxf(dx, dy), 0.0f);
+        return (float)((double)a + (double)len2(gt_max(dx, 0.0f), gt_max(dy, 0.0f)));
     }
     case DN_SHAPE_CONE: {
         const float l = len2(q.x, q.z);
         const float dt = p.angles[0] * l + p.angles[1] * q.y;
-        return (float)fmax((double)dt, (double)(-p.height - q.y));
+        return fmaxf(dt, -p.height - q.y);
     }
     case DN_SHAPE_PYRAMID: {
         const float h = p.height;
@@ -106,7 +108,7 @@ __device__ uint32_t shape_classify(const dn_shape_params& p, int gx, int gy, int
         if (d2 < p.r2) cls = 1;
         else if (p.removing && p.flipNormals && d2 < p.r12) cls = 2;
         if (cls == 0 || (cls == 1 && p.removing)) return cls;
-        const float mx = (float)fmax(fmax((double)fabsf(fx), (double)fabsf(fy)), (double)fabsf(fz));
+        const float mx = fmaxf(fmaxf(fabsf(fx), fabsf(fy)), fabsf(fz));
         const float k = 1.0f / mx;
         n[0] = fx * k; n[1] = fy * k; n[2] = fz * k;
         return cls;
@@ -122,7 +124,7 @@ __device__ uint32_t shape_classify(const dn_shape_params& p, int gx, int gy, int
     const float x = shape_sdf(p, xform(p.invTransform, px + h, py + 0.0f, pz + 0.0f, 1.0f + 0.0f)) - dist;
     const float y = shape_sdf(p, xform(p.invTransform, px + 0.0f, py + h, pz + 0.0f, 1.0f + 0.0f)) - dist;
     const float z = shape_sdf(p, xform(p.invTransform, px + 0.0f, py + 0.0f, pz + h, 1.0f + 0.0f)) - dist;
-    const float mx = (float)fmax(fmax((double)fabsf(x), (double)fabsf(y)), (double)fabsf(z));
+    const float mx = fmaxf(fmaxf(fabsf(x), fabsf(y)), fabsf(z));
     const float k = 1.0f / mx;
     n[0] = x * k; n[1] = y * k; n[2] = z * k;
     return cls;
