@@ -311,18 +311,22 @@ def cpu_baseline_sample(vol, view, proj, W, H, seconds):
     om.reset_counters()
     t0 = time.perf_counter()
     om.draw(vol.s, iv, icv, ip, W, H, pixels=pix, nthreads=ncores)
-    n, done, budget = 64, 0, seconds
-    while done < len(order) and time.perf_counter() - t0 < budget:
-        chunk = order[done:done + n]
+    # the frame's request groups in a seeded order, passed over again (the same work: nothing is
+    # committed) until the time budget is spent
+    n, done, at, budget = 64, 0, 0, seconds
+    while len(order) and time.perf_counter() - t0 < budget:
+        chunk = order[at:at + n]
         om.light_requests(vol.s, params, chunk, nthreads=ncores)
         done += len(chunk)
+        at = (at + len(chunk)) % len(order)
         n = min(n * 2, 1 << 14)
     el = time.perf_counter() - t0
     c = om.counters()
     om.close()
     return {"value": c["rays"] / el, "unit": "rays/s", "cores": ncores, "kind": "port",
-            "sample": "%d pixels of the 1920x1080 draw + %d of %d lighting request groups of the last timed frame "
-                      "(%d rays, %.1f s)" % (len(pix), done, len(order), c["rays"], el)}
+            "sample": "%d pixels of the %dx%d draw + %d lighting request groups (%.2f passes over the last timed "
+                      "frame's %d) (%d rays, %.1f s)" % (len(pix), W, H, done, done / max(1, len(order)), len(order),
+                                                        c["rays"], el)}
 
 
 # ------------------------------------------------------------ batched workload

@@ -38,7 +38,15 @@ struct PacketVoxel {
 };
 enum : uint32_t { PV_VALID = 1u, PV_FIRST = 2u, PV_SPEC = 4u, PV_DIFF = 8u };
 
-constexpr uint32_t PK_POOL_FAN = 64;          // rays per fan kind in one pool: voxels per pool = 64 / K
+// rays per fan kind in one pool (voxels per pool = PK_POOL_FAN / K): the pool's specular contributions,
+// shadow contributions and counts live in shared memory, 38 B per pooled ray.  96 (3 voxels at K = 32)
+// measured best on the large map: 64 at 6 blocks per SM 3.20 G rays/s, 96 3.34, 128 at 5 blocks 3.27,
+// 192 / 224 at 4 blocks 3.06 / 3.08; larger pools shorten the tail of a pool's longest rays, fewer
+// resident blocks cost more than that saves.
+#ifndef DN_PK_POOL_FAN
+#define DN_PK_POOL_FAN 96
+#endif
+constexpr uint32_t PK_POOL_FAN = DN_PK_POOL_FAN;
 
 struct PacketWarp {
     PacketVoxel v[32];
@@ -123,7 +131,7 @@ __device__ __forceinline__ int pass_voxel(uint32_t mask, uint32_t base, uint32_t
     return __ffs(mm) - 1;
 }
 
-// The request groups of one launch.  Per group: (1) pools of 64/K voxels (at least one): every ray of their
+// The request groups of one launch.  Per group: (1) pools of PK_POOL_FAN/K voxels (at least one): every ray of their
 // specular fans, first-sample shadow rays and shadow fans is traced by whichever lane is free -- a lane
 // takes the pool's next ray as soon as its own ended, and the shading of ended segments runs once `batch`
 // lanes have one, so no lane waits for the slowest ray of a fan; each ray's contributions go to shared
@@ -343,10 +351,10 @@ __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLi
             }
             __syncwarp();
             // the pool's sums in the reference's order: lane 2j sums voxel j's specular rays (ray, then
-            // segment order), lane 2j+1 its shadow rays
-            {
-                const uint32_t j = lane >> 1;
-                if (j < np) {
+            // segment order), lane 2j+1 its shadow rays; pools of more than 16 voxels (small K) take a
+            // second round
+            for (uint32_t j = lane >> 1; j < np; j += 16u) {
+                {
                     uint32_t mm = poolMask;
                     for (uint32_t t = 0; t < j; t++) mm &= mm - 1u;
                     const int v = __ffs(mm) - 1;

@@ -312,3 +312,15 @@ def test_raster_composition(gpu_ready, tex_scale, transparent):
         dt.close()
     finally:
         pair.close()
+
+
+@pytest.mark.parametrize("K", [1, 2, 3, 5])
+def test_small_fan_counts(gpu_ready, K):
+    """Few direct / specular rays per voxel: the packet kernel's pools then hold more than 16 voxels
+    (96 / K), so its per-pool sums take more than one round of lanes."""
+    pair = Pair("tiny", K=K)
+    try:
+        for _ in range(3):
+            pair.step()
+    finally:
+        pair.close()
