@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(128, DN_STREAM_MIN_BLOCKS) k_light_stream_batc
 __global__ void __launch_bounds__(128, DN_PACKET_MIN_BLOCKS) k_light_packet_batch(const __grid_constant__ BatchLightArgs a)
 {
     __shared__ PacketWarp warps[4];
-    packet_loop<true>(nullptr, &a, nullptr, warps[threadIdx.x >> 5]);
+    packet_loop<true>(nullptr, &a, warps[threadIdx.x >> 5]);
 }
 
 __global__ void k_commit_batch(const BatchLightMap* l, const uint32_t* reqStart, uint32_t nl)

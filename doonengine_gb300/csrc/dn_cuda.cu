@@ -138,7 +138,7 @@ extern "C" void dn_cuda_map_destroy(DNgpuVolume* g)
     if (g->stream) cudaStreamSynchronize(g->stream);
     free_tiles(g);
     dfree(g->rec); dfree(g->nsamples); dfree(g->vox); dfree(g->diff); dfree(g->spec);
-    dfree(g->reqs); dfree(g->lightOut); dfree(g->st); dfree(g->dstage);
+    dfree(g->reqs); dfree(g->lightOut); dfree(g->st); dfree(g->dtab); dfree(g->dstage);
     dfree(g->dimg); dfree(g->dhit); dfree(g->dface);
     if (g->hstage) cudaFreeHost(g->hstage);
     if (g->hst) cudaFreeHost(g->hst);
@@ -191,6 +191,7 @@ extern "C" int dn_cuda_map_create(uint32_t sx, uint32_t sy, uint32_t sz, uint32_
     if (!rc) rc = dalloc(&g->diff, voxelCap);
     if (!rc) rc = dalloc(&g->spec, voxelCap);
     if (!rc) rc = dalloc(&g->st, 1);
+    if (!rc) rc = dalloc(&g->dtab, 1);
     if (!rc) rc = reserve_requests(g, 1024);
     if (!rc) {
         e = cudaMallocHost((void**)&g->hst, sizeof(DevState));
@@ -264,6 +265,7 @@ static int persistent_arrays(DNgpuVolume* g, PersistentArray* out)
     out[k++] = {(void**)&g->spec, (size_t)g->voxCap * 16};
     out[k++] = {(void**)&g->reqs, (size_t)g->reqCap * 4};
     out[k++] = {(void**)&g->st, sizeof(DevState)};
+    out[k++] = {(void**)&g->dtab, sizeof(LightTables)};
     return k;
 }
 
@@ -461,14 +463,21 @@ __global__ void __launch_bounds__(128, DN_STREAM_MIN_BLOCKS) k_light_stream(cons
 }
 
 // The lighting launch with specular and shadow fans traced as warp packets (dn_light_packet.cuh).
+// the launch's materials and shadow directions into the volume's device tables, which k_light_packet
+// reads through L1 (a kernel, not a copy from host memory, so that the launch sequence can be captured)
+__global__ void k_light_tables(const __grid_constant__ MaterialTable t, const __grid_constant__ dn_light_params p,
+                               LightTables* out)
+{
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) out->mats[i] = t.m[i];
+    for (int k = threadIdx.x; k < 65; k += blockDim.x) shadow_dir(p, k, out->sdir[k], out->sinv[k]);
+}
+
 __global__ void __launch_bounds__(128, DN_PACKET_MIN_BLOCKS) k_light_packet(const __grid_constant__ StreamArgs a)
 {
-    __shared__ StreamShared sh;
+    // shared memory holds only the four warps' pools (26 KB per block): 6 blocks fit the 164 KB carveout,
+    // leaving about 92 KB of L1 for the map's masks and voxels; the tables are read from a.gtab
     __shared__ PacketWarp warps[4];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) sh.mats[i] = a.mats[i];
-    for (int k = threadIdx.x; k < 65; k += blockDim.x) shadow_dir(a.p, k, sh.sdir[k], sh.sinv[k]);
-    __syncthreads();
-    packet_loop<false>(&a, nullptr, &sh, warps[threadIdx.x >> 5]);
+    packet_loop<false>(&a, nullptr, warps[threadIdx.x >> 5]);
 }
 
 // launches the lighting kernel g_lightKernel selects (1 ray streams, 2 warp packets; packets need
@@ -480,6 +489,11 @@ static int launch_light(DNgpuVolume* g, StreamArgs& a)
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_packet, 128, 0));
         if (perSM < 1) perSM = 1;
         a.batch = g_packetBatch;
+        static thread_local MaterialTable table;
+        memcpy(table.m, a.mats, sizeof(table.m));
+        a.gtab = g->dtab;
+        COUNT_LAUNCH();
+        k_light_tables<<<1, 256, 0, g->stream>>>(table, a.p, g->dtab);
         COUNT_LAUNCH();
         k_light_packet<<<g->numSMs * perSM, 128, 0, g->stream>>>(a);
     } else {
@@ -1013,7 +1027,7 @@ extern "C" int dn_cuda_flush_l2(void* stream, size_t bytes)
 
 extern "C" const char* dn_cuda_kernel_names(void)
 {
-    return "k_draw;k_light;k_light_stream;k_light_packet;k_commit;k_sync_stage;k_compact;k_clamp_requests;k_flush;"
+    return "k_draw;k_light;k_light_stream;k_light_packet;k_light_tables;k_commit;k_sync_stage;k_compact;k_clamp_requests;k_flush;"
            "k_draw_batch;k_compact_batch;k_batch_reset;k_batch_prep;k_light_stream_batch;k_light_packet_batch;k_commit_batch;k_batch_gather;"
            "k_shape_count;k_shape_write";
 }

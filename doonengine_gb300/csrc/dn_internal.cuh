@@ -34,6 +34,7 @@ struct DevState {
 };
 
 struct DNgpuBatch;
+namespace dn { struct LightTables; }   // dn_light_stream.cuh
 
 struct DNgpuVolume {
     int device;
@@ -50,6 +51,7 @@ struct DNgpuVolume {
     uint2* vox; float4* diff; float4* spec; uint64_t voxCap;
     uint32_t* reqs; float4* lightOut; uint64_t reqCap;
     DevState* st;
+    dn::LightTables* dtab;              // materials and shadow directions of the last lighting launch (k_light_packet)
     // pinned staging for sync uploads and small readbacks
     unsigned char* hstage; size_t hstageCap;
     unsigned char* dstage; size_t dstageCap;

@@ -139,8 +139,7 @@ __device__ __forceinline__ int pass_voxel(uint32_t mask, uint32_t base, uint32_t
 // diffuse paths, one lane per voxel; (3) the running average and the write-out.  One stepping loop
 // serves both traced phases.
 template <bool MANY>
-__device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLightArgs* many, const StreamShared* sh,
-                                            PacketWarp& W)
+__device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLightArgs* many, PacketWarp& W)
 {
     const uint32_t lane = lane_id_s();
     uint32_t nreq = 0;
@@ -169,9 +168,9 @@ __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLi
         }
         const DevMap& m = MANY ? e->m : one->m;
         const dn_light_params& p = MANY ? e->p : one->p;
-        const Material* mats = MANY ? e->mats : sh->mats;
-        const float (*sdir)[3] = MANY ? e->sdir : sh->sdir;
-        const float (*sinv)[3] = MANY ? e->sinv : sh->sinv;
+        const Material* mats = MANY ? e->mats : one->gtab->mats;
+        const float (*sdir)[3] = MANY ? e->sdir : one->gtab->sdir;
+        const float (*sinv)[3] = MANY ? e->sinv : one->gtab->sinv;
         float4* out = MANY ? e->out : one->out;
         const bool rngSin = p.rngMode == 1u;
         const f3 sun = mk(p.sunStrength[0], p.sunStrength[1], p.sunStrength[2]);

@@ -42,6 +42,16 @@ struct StreamArgs {
     uint32_t batch;
     dn_light_params p;
     Material mats[256];
+    const struct LightTables* gtab;   // device copy of mats and the shadow directions (k_light_packet)
+};
+
+struct MaterialTable { Material m[256]; };
+
+// per-launch tables k_light_packet reads through L1: the materials and the shadow directions
+struct LightTables {
+    Material mats[256];
+    float sdir[65][3];   // shadow directions k < K, [64]: the first-sample direction sunDir + EPS
+    float sinv[65][3];
 };
 
 // traversal state of one ray segment (flattened two-level DDA, refraction off).  Both levels step with
@@ -209,6 +219,7 @@ struct StreamShared {
     float sdir[65][3];   // shadow directions k < K, [64]: the first-sample direction sunDir + EPS
     float sinv[65][3];
 };
+
 
 // diffuse bounce direction (voxelLighting.comp:160-168)
 __device__ __forceinline__ f3 diffuse_dir(const Job& j, const dn_light_params& p, const Material* mats, bool rngSin)
