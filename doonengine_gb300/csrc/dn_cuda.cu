@@ -474,8 +474,9 @@ __global__ void k_light_tables(const __grid_constant__ MaterialTable t, const __
 
 __global__ void __launch_bounds__(128, DN_PACKET_MIN_BLOCKS) k_light_packet(const __grid_constant__ StreamArgs a)
 {
-    // shared memory holds only the four warps' pools (26 KB per block): 6 blocks fit the 164 KB carveout,
-    // leaving about 92 KB of L1 for the map's masks and voxels; the tables are read from a.gtab
+    // shared memory holds only the four warps' pools (31 KB per block with 128-ray pools): 6 blocks fit
+    // the 196 KB carveout, leaving about 60 KB of L1 for the map's masks and voxels; the tables are read
+    // from a.gtab
     __shared__ PacketWarp warps[4];
     packet_loop<false>(&a, nullptr, warps[threadIdx.x >> 5]);
 }

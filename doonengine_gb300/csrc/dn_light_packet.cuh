@@ -39,12 +39,12 @@ struct PacketVoxel {
 enum : uint32_t { PV_VALID = 1u, PV_FIRST = 2u, PV_SPEC = 4u, PV_DIFF = 8u };
 
 // rays per fan kind in one pool (voxels per pool = PK_POOL_FAN / K): the pool's specular contributions,
-// shadow contributions and counts live in shared memory, 38 B per pooled ray.  96 (3 voxels at K = 32)
-// measured best on the large map: 64 at 6 blocks per SM 3.20 G rays/s, 96 3.34, 128 at 5 blocks 3.27,
-// 192 / 224 at 4 blocks 3.06 / 3.08; larger pools shorten the tail of a pool's longest rays, fewer
-// resident blocks cost more than that saves.
+// shadow contributions and counts live in shared memory, 38 B per pooled ray.  Larger pools shorten the
+// tail that a pool's longest rays leave; the shared memory they take comes out of L1 (the SM's 256 KB
+// split).  Measured on the large map at 6 blocks per SM with the tables in global memory: 64 rays
+// 3.38 G rays/s, 96 3.55, 128 3.64-3.66 (31 KB per block, 60 KB of L1), 160 3.60, 192 (5 blocks) 3.40.
 #ifndef DN_PK_POOL_FAN
-#define DN_PK_POOL_FAN 96
+#define DN_PK_POOL_FAN 128
 #endif
 constexpr uint32_t PK_POOL_FAN = DN_PK_POOL_FAN;
 
