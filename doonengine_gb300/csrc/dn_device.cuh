@@ -253,7 +253,7 @@ __device__ __forceinline__ uint32_t step_cap(uint32_t sx, uint32_t sy, uint32_t 
 }
 
 // step_chunk, voxelShared.comp:328-418
-static __device__ __noinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapPos, uint32_t slot, uint32_t tile,
+static __device__ __forceinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapPos, uint32_t slot, uint32_t tile,
                                         f3& rayDir, f3& inv, f3& rayPos, bool ignoreFirst, float maxDepth,
                                         f3& hitNormal, Voxel& vox, f3& colorAdd, float& colorMult,
                                         bool& refracted, HitInfo& hi)
@@ -331,7 +331,7 @@ static __device__ __noinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapPos,
 }
 
 // step_map, voxelShared.comp:421-475
-static __device__ __noinline__ bool step_map(RayCtx& c, TState& ts, f3& rayDir, f3 inv, f3& rayPos, bool ignoreFirst,
+static __device__ __forceinline__ bool step_map(RayCtx& c, TState& ts, f3& rayDir, f3 inv, f3& rayPos, bool ignoreFirst,
                                       float maxDepth, f3& hitNormal, Voxel& vox, f3& colorAdd, float& colorMult,
                                       HitInfo& hi)
 {
