@@ -324,3 +324,30 @@ def test_small_fan_counts(gpu_ready, K):
             pair.step()
     finally:
         pair.close()
+
+
+@pytest.mark.parametrize("spec,diff", [(0, 5), (1, 1), (3, 2), (4, 0)])
+def test_bounce_limits(gpu_ready, spec, diff):
+    """specBounceLimit 0..4 (above 2 the lighting runs the per-lane-stream kernel) and diffuseBounceLimit
+    0..5, with specular, reflecting materials so that specular rays bounce"""
+    pair = Pair("tiny")
+    try:
+        pair.vol.s.specBounceLimit = spec
+        pair.vol.s.diffuseBounceLimit = diff
+        for m in range(0, 16, 2):
+            pair.vol.set_material(m, specular=0.6, reflect_type=1 + m % 2, shininess=2 + m % 3)
+        for _ in range(3):
+            pair.step()
+    finally:
+        pair.close()
+
+
+@pytest.mark.parametrize("nd,md", [(2, 1000), (3, 2)])
+def test_several_diffuse_samples(gpu_ready, nd, md):
+    """numDiffuseSamples > 1 per voxel and a small maxDiffuseSamples (the running average's weight caps)"""
+    pair = Pair("tiny")
+    try:
+        for _ in range(4):
+            pair.step(num_diffuse=nd, max_diffuse=md)
+    finally:
+        pair.close()
