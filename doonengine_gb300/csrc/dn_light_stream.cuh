@@ -55,12 +55,16 @@ struct LightTables {
 };
 
 // traversal state of one ray segment (flattened two-level DDA, refraction off).  Both levels step with
-// the same delta and step signs, so one set of DDA registers (cpos, cside, clast) holds the level being
-// walked; entering a chunk saves the chunk-level registers (opos, oside, olast) and leaving restores them.
+// the same delta and step signs, so one set of DDA registers (cpos, cside, clastMin) holds the level being
+// walked; entering a chunk saves the chunk-level registers (opos, oside, olastMin) and leaving restores
+// them.  The reference keeps the side distances before the last step as a vector (lastSideDist) but only
+// ever uses its minimum (voxelShared.comp:338, 445), so that minimum is kept instead, formed in the same
+// order (min3).
 struct Seg {
     f3 pos, dir, inv;
     i3 cpos, opos, step;
-    f3 cside, clast, oside, olast, cp;
+    f3 cside, oside, cp;
+    float clastMin, olastMin;
     const ChunkRec* rec;
     uint32_t base;
     uint32_t flags;      // bit0 inner level, bit1 ignore (current level), bit2 saved outer ignore, bit3 requested,
@@ -79,7 +83,7 @@ __device__ __forceinline__ void seg_begin(Seg& s, f3 pos, f3 dir, f3 inv)
     s.ts.lastVoxID = 255u; s.ts.lastVoxRefract = 1.0f;   // D13: fresh per ray job (spec / diffuse bounces keep it)
     f3 delta;
     init_dda(dir, inv, pos, s.cpos, delta, s.step, s.cside);
-    s.clast = mk(0.0f, 0.0f, 0.0f);
+    s.clastMin = 0.0f;   // min3 of the zero vector
     s.flags = 2u;        // ignore the first voxel
 }
 
@@ -114,20 +118,20 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
             c.outer++;
             c.entered++;
             if (m.ttouch[idx] == 0) m.ttouch[idx] = 1;
-            const float tt = min3(s.clast) - EPS;
+            const float tt = s.clastMin - EPS;
             const f3 up = add(s.pos, muls(s.dir, tt));
             f3 cp = mk((up.x - (float)s.cpos.x) * 8.0f, (up.y - (float)s.cpos.y) * 8.0f, (up.z - (float)s.cpos.z) * 8.0f);
             const float lo = EPS, hi_ = 8.0f - EPS;
             cp.x = gmin(gmax(cp.x, lo), hi_); cp.y = gmin(gmax(cp.y, lo), hi_); cp.z = gmin(gmax(cp.z, lo), hi_);
             s.cp = cp;
-            s.opos = s.cpos; s.oside = s.cside; s.olast = s.clast;
+            s.opos = s.cpos; s.oside = s.cside; s.olastMin = s.clastMin;
             const f3 fl = vfloor(cp);
             s.cpos.x = f2i(fl.x); s.cpos.y = f2i(fl.y); s.cpos.z = f2i(fl.z);
             const f3 sg = mk((float)step.x, (float)step.y, (float)step.z);
             s.cside.x = (sg.x * ((float)s.cpos.x - cp.x) + sg.x * 0.5f + 0.5f) * delta.x;
             s.cside.y = (sg.y * ((float)s.cpos.y - cp.y) + sg.y * 0.5f + 0.5f) * delta.y;
             s.cside.z = (sg.z * ((float)s.cpos.z - cp.z) + sg.z * 0.5f + 0.5f) * delta.z;
-            s.clast = mk(0.0f, 0.0f, 0.0f);
+            s.clastMin = 0.0f;
             s.rec = &m.rec[__ldg(&m.tword[idx]) & SLOT_MASK];
             s.base = __ldg(&s.rec->voxBase);
             s.flags = (s.flags & ~4u) | 1u | ((s.flags & 2u) << 1);   // inner level; the chunk inherits ignoreFirst
@@ -135,7 +139,7 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
         }
         if (!inb) {
             // the chunk was crossed without a hit: back to the chunk level, which then iterates
-            s.cpos = s.opos; s.cside = s.oside; s.clast = s.olast;
+            s.cpos = s.opos; s.cside = s.oside; s.clastMin = s.olastMin;
             s.flags = (s.flags & ~3u) | ((s.flags >> 1) & 2u);
         } else {
             c.inner++;
@@ -145,7 +149,7 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
             const uint32_t material = vw.x >> 24;
             const Material& mat = mats[material];
             if (mat.opacity == 1.0f) {
-                const float t = min3(s.clast) + EPS;
+                const float t = s.clastMin + EPS;
                 const f3 cp = add(s.cp, muls(s.dir, t));
                 s.pos = add(mk((float)s.opos.x, (float)s.opos.y, (float)s.opos.z), muls(cp, INV_CHUNK));
                 hitIdx = vi;
@@ -175,10 +179,11 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
         }
     }
     // iterate_DDA on the current level (voxelShared.comp:309-317)
-    s.clast = s.cside;
-    const bool mx = s.cside.x <= gmin(s.cside.y, s.cside.z);
-    const bool my = s.cside.y <= gmin(s.cside.z, s.cside.x);
-    const bool mz = s.cside.z <= gmin(s.cside.x, s.cside.y);
+    const float gyz = gmin(s.cside.y, s.cside.z), gzx = gmin(s.cside.z, s.cside.x), gxy = gmin(s.cside.x, s.cside.y);
+    s.clastMin = gmin(gxy, s.cside.z);   // min3(lastSideDist) of the next step
+    const bool mx = s.cside.x <= gyz;
+    const bool my = s.cside.y <= gzx;
+    const bool mz = s.cside.z <= gxy;
     s.cside.x = s.cside.x + (mx ? 1.0f : 0.0f) * delta.x;
     s.cside.y = s.cside.y + (my ? 1.0f : 0.0f) * delta.y;
     s.cside.z = s.cside.z + (mz ? 1.0f : 0.0f) * delta.z;
