@@ -108,9 +108,11 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
     const uint32_t idx = (uint32_t)s.cpos.x + bx * ((uint32_t)s.cpos.y + by * (uint32_t)s.cpos.z);
     uint32_t w = 0;
     if (inb) w = __ldg(inner ? &s.rec->mask[idx >> 5] : &m.tbits[idx >> 4]);
-    // chunk level: 2-bit state (0 absent, 1 unloaded, 2 loaded); voxel level: occupancy bit
-    const uint32_t cst = (w >> ((idx & 15u) * 2u)) & 3u;
-    const bool occ = inb && (inner ? ((((w >> (idx & 31)) & 1u) != 0u) && !(s.flags & 2u)) : (cst == 2u));
+    // chunk level: 2-bit state (0 absent, 1 unloaded, 2 loaded); voxel level: occupancy bit -- one shift
+    // brings either to the low bits (cst is only read at the chunk level)
+    const uint32_t bits = w >> (inner ? (idx & 31u) : ((idx & 15u) << 1));
+    const uint32_t cst = bits & 3u;
+    const bool occ = inb && (inner ? (((bits & 1u) != 0u) && !(s.flags & 2u)) : (cst == 2u));
     if (!inb || occ) {
         if (!inner) {
             if (!inb) return 2u;
