@@ -978,7 +978,7 @@ def main():
                     help="plain: one map per step (the headline); batched: many maps per step")
     ap.add_argument("--maps", type=int, default=64, help="maps of the batched workload")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--rates", default="100,200,300,400,500,600,700,850,1000,1500,2000,5000,10000,20000",
+    ap.add_argument("--rates", default="100,200,300,400,500,600,700,850,1000,1100,1200,1300,1400,1500,2000,5000,10000,20000",
                     help="serving: offered req/s, swept upwards until the server saturates")
     ap.add_argument("--seconds", type=float, default=4.0, help="serving: seconds of arrivals per rate")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device budget")
