@@ -3,12 +3,14 @@
  *
  * Every lit voxel casts two fans of K rays from one point: K specular rays around its reflection
  * direction (voxelLighting.comp:83-146, each up to specBounceLimit segments) and K shadow rays around the
- * sun direction (D8).  A warp takes one request group (32 voxels of one chunk) and traces each voxel's
- * fan across its lanes -- lane k traces ray k, 32/K voxels per pass when K <= 32, ceil(K/32) rounds when
- * K > 32 -- so the lanes of a warp walk nearly the same cells in the same order: the shadow rays of a
- * voxel are almost parallel, and the specular rays share their origin and lobe.  The per-voxel sums are
- * then formed by a serial walk over the lanes in ray order (shuffles / shared memory), so every sum is
- * accumulated in exactly the reference's order.  The diffuse paths (numDiffuse per voxel, up to
+ * sun direction (D8).  A warp takes one request group (32 voxels of one chunk) and traces the fans of
+ * PK_POOL_FAN / K of its voxels at a time as one pool: the pool's rays are numbered (specular fans first,
+ * then the shadow rays), and a lane whose ray has ended takes the pool's next ray, so consecutive rays of
+ * a fan run side by side and the lanes of a warp walk nearly the same cells (a fan's shadow rays are
+ * almost parallel, its specular rays share their origin and lobe).  Ended segments are shaded once
+ * `batch` lanes have one.  Each ray's contributions go to shared memory; when the pool is empty, each
+ * voxel's sums are formed by one lane walking its rays (and their segments) in ray order, so every sum
+ * is accumulated in exactly the reference's order.  The diffuse paths (numDiffuse per voxel, up to
  * diffuseBounceLimit segments each) run one lane per voxel, and each lane finishes its voxel as the
  * reference's lighting main does (running average, clamps, voxelLighting.comp:238-288).
  *
