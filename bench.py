@@ -136,11 +136,11 @@ def allreduce_sum(pg, x):
     return float(t.item())
 
 
-def workload_desc(cfg, vol=None, nonempty=None):
+def workload_desc(cfg, vol=None, nonempty=None, name="large"):
     sx, sy, sz = cfg["map"]
-    d = {"workload": "large: %dx%dx%d chunks (%dx%dx%d voxels), heightfield + %d boxes/spheres, %dx%d draw, "
+    d = {"workload": "%s: %dx%dx%d chunks (%dx%dx%d voxels), heightfield + %d boxes/spheres, %dx%d draw, "
                      "K=%d direct/specular rays, 1 diffuse path per voxel per frame"
-                     % (sx, sy, sz, sx * 8, sy * 8, sz * 8, cfg["shapes"], cfg["res"][0], cfg["res"][1], cfg["K"]),
+                     % (name, sx, sy, sz, sx * 8, sy * 8, sz * 8, cfg["shapes"], cfg["res"][0], cfg["res"][1], cfg["K"]),
          "map_chunks": [sx, sy, sz], "resolution": list(cfg["res"]), "K": cfg["K"], "diffuse_spp": 1,
          "seed": cfg["seed"], "frame": "draw -> sync -> lighting",
          "l2": "flushed between timed steps (256 MiB write, outside the timed events)"}
@@ -247,7 +247,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
         "ms_per_step": dev_ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded heightfield + boxes/spheres; the reference publishes no scenes)",
-        "config": dict(workload_desc(cfg, vol, nonempty), parallelism="replicas: one map per GPU, no collective"),
+        "config": dict(workload_desc(cfg, vol, nonempty, args.config), parallelism="replicas: one map per GPU, no collective"),
         "lit_voxels_per_s": lit_total / (dev_ms_max / 1e3),
         "primary_rays_per_s": prim_total / (dev_ms_max / 1e3),
         "rays_per_step": rays_total / K,
@@ -952,7 +952,7 @@ def run_reference(args):
               "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
               "data": "synthetic (seeded heightfield + boxes/spheres)", "impl": "reference",
-              "config": workload_desc(cfg, vol, nonempty),
+              "config": workload_desc(cfg, vol, nonempty, args.config),
               "cpu_baseline": {"value": value, "unit": "rays/s", "cores": ncores, "kind": "port", "sample": sample},
               "e2e": {"value": value, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
               "note": "the reference path runs only as GLSL through OpenGL, which is unavailable on this box; "
