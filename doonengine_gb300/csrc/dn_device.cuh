@@ -8,7 +8,7 @@
  * --fmad=false and IEEE division / square root, so a ray takes exactly the
  * same steps as on the host and hit voxels match bit for bit.
  *
- * Deterministic semantics (shared with the host checker, numbered as there):
+ * Deterministic semantics (shared with the CPU oracle, numbered as there):
  *   D1 lighting reads last frame's committed lighting, new values are
  *      committed by a second kernel; D2 sample count snapshotted per launch;
  *   D3 FP32 lighting; D4 visible / requested / touched are per-tile bytes

@@ -4,7 +4,7 @@
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference's
  * GLSL compute shaders (assets/shaders/voxelShared.comp, voxelLighting.comp,
  * voxelDraw.comp) and of the host-side packing / sync logic in
- * src/DoonEngine/voxel.c.  It is the checker that the CUDA path is compared
+ * src/DoonEngine/voxel.c.  It is the oracle that the CUDA path is compared
  * against and the timed CPU baseline; the product library never links,
  * loads or calls it.
  *
