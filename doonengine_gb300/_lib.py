@@ -4,7 +4,7 @@ library's own ``DN_abi_layout``."""
 import ctypes
 import os
 from ctypes import (POINTER, Structure, c_bool, c_char_p, c_double, c_float, c_int, c_size_t, c_uint8, c_uint32,
-                    c_uint64, c_void_p, c_int32)
+                    c_uint64, c_void_p, c_int32, c_int64)
 
 from . import build as _build
 
@@ -181,6 +181,10 @@ _SIGS = [
     ("DN_set_map_size", c_bool, [VOLP, DNuvec3]),
     ("DN_set_max_chunks", c_bool, [VOLP, c_size_t]),
     ("DN_set_max_voxels_gpu", c_bool, [VOLP, c_size_t]),
+    ("DN_set_residency", c_bool, [VOLP, c_int]),
+    ("DN_get_residency", c_int, [VOLP]),
+    ("DN_residency_nodes", c_size_t, [VOLP, POINTER(c_size_t), POINTER(c_uint32), POINTER(c_uint64),
+                                      POINTER(c_int64), c_size_t]),
     ("DN_set_max_lighting_requests", c_bool, [VOLP, c_size_t]),
     ("DN_in_map_bounds", c_bool, [VOLP, DNivec3]),
     ("DN_in_chunk_bounds", c_bool, [DNivec3]),
@@ -285,6 +289,7 @@ _SIGS = [
     ("dn_cuda_reset_stats", c_int, [c_void_p]),
     ("dn_cuda_stream", c_void_p, [c_void_p]),
     ("dn_cuda_export_tiles", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("dn_cuda_read_tile_flags", c_int, [c_void_p, c_void_p, c_void_p]),
     ("dn_cuda_export_requests", c_int, [c_void_p, c_void_p, c_uint64, POINTER(c_uint64)]),
     ("dn_cuda_export_lighting", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint64, POINTER(c_uint64)]),
     ("dn_cuda_malloc", c_int, [POINTER(c_void_p), c_size_t]),

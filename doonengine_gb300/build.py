@@ -27,7 +27,7 @@ C_FLAGS = ["-O2", "-fPIC", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", 
            "-Wno-unused-function", "-I" + INCLUDE]
 
 CU_SOURCES = ["dn_cuda.cu", "dn_batch.cu", "dn_shapes.cu"]
-C_SOURCES = ["voxel.c", "dn_math.c", "dn_scenes.c", "voxvol.c", "dn_serve.c", "voxelShapes.c"]
+C_SOURCES = ["voxel.c", "dn_math.c", "dn_scenes.c", "voxvol.c", "dn_serve.c", "voxelShapes.c", "dn_residency.c"]
 HEADERS = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))) + [
     os.path.join(INCLUDE, "dn_cuda.h"), os.path.join(INCLUDE, "DoonEngine", "voxel.h"),
     os.path.join(INCLUDE, "DoonEngine", "globals.h"), os.path.join(INCLUDE, "DoonEngine", "dn_math.h"),

@@ -28,7 +28,7 @@ def build_volume(name, cpu_only=False, **over):
     cfg = dict(CONFIGS[name])
     cfg.update(over)
     sx, sy, sz = cfg["map"]
-    vol = Volume((sx, sy, sz), min_chunks=max(64, sx * sy * sz // 4), cpu_only=cpu_only)
+    vol = Volume((sx, sy, sz), min_chunks=cfg.get("min_chunks", max(64, sx * sy * sz // 4)), cpu_only=cpu_only)
     seed = cfg["seed"]
     vol.palette(seed, 16, 2, 0.1, 0.9, 0.5)
     vol.terrain(seed, cfg["mean"], cfg["amp"], 16, 2)

@@ -894,6 +894,17 @@ extern "C" int dn_cuda_reset_stats(DNgpuVolume* g)
 
 extern "C" void* dn_cuda_stream(DNgpuVolume* g) { return g ? (void*)g->stream : nullptr; }
 
+extern "C" int dn_cuda_read_tile_flags(DNgpuVolume* g, uint8_t* requested, uint8_t* touched)
+{
+    if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
+    if (g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    CK(cudaSetDevice(g->device));
+    CK(cudaMemcpyAsync(requested, g->treq, g->ntiles, cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaMemcpyAsync(touched, g->ttouch, g->ntiles, cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    return DN_CUDA_OK;
+}
+
 extern "C" int dn_cuda_export_tiles(DNgpuVolume* g, uint8_t* state, uint8_t* vis, uint32_t* lastUsed, uint32_t* samples)
 {
     if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");

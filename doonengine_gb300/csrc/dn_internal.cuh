@@ -363,6 +363,8 @@ __device__ __forceinline__ void compact_tiles(const CompactArgs& a, uint64_t bas
         const bool req = a.treq[t] != 0;
         uint32_t vis = a.tvis[t];
         uint32_t gflag = (st == 1u && req) ? 3u : st;
+        // an earlier tile of this sync took the chunk's node (DN_RESIDENCY_LRU): it reaches its turn unloaded
+        if (pend & DN_PEND_EVICTED) { gflag = 1u; vis = 0; slot = DN_SLOT_NONE; }
         const bool updated = (pend & DN_PEND_UPDATED) != 0;
         uint32_t lu = a.tlast[t];
         if (a.ttouch[t]) { lu = 0; a.ttouch[t] = 0; }
@@ -379,9 +381,13 @@ __device__ __forceinline__ void compact_tiles(const CompactArgs& a, uint64_t bas
             if (exists && gflag == 0u) { gflag = 1u; changed = true; }
             else if (!exists && gflag != 0u) { gflag = 0u; changed = true; }
             if (gflag == 2u && updated) { gflag = 3u; changed = true; }
-            if (gflag == 3u && exists && newSlot != DN_SLOT_NONE) { gflag = 2u; lu = 0; changed = true; }
+            // a load; with DN_RESIDENCY_LRU it can find no node and leave the chunk unloaded
+            const bool hold = (pend & DN_PEND_HOLD) != 0;
+            if (gflag == 3u && exists && (hold || newSlot != DN_SLOT_NONE)) { gflag = hold ? 1u : 2u; lu = 0; changed = true; }
+            // a later tile of this sync took the chunk's node
+            if (pend & DN_PEND_EVICT) { gflag = 1u; changed = true; }
             if (changed) vis = 0;
-            slot = exists ? newSlot : DN_SLOT_NONE;
+            slot = (exists && !(pend & (DN_PEND_EVICT | DN_PEND_EVICTED))) ? newSlot : DN_SLOT_NONE;
             a.treq[t] = (gflag == 3u) ? 1 : 0;
             finalSt = gflag == 3u ? 1u : gflag;
             a.tword[t] = (finalSt << 30) | (slot & dn::SLOT_MASK);

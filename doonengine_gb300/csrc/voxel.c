@@ -25,6 +25,7 @@
 #include "DoonEngine/voxel.h"
 #include "DoonEngine/serve.h"
 #include "dn_cuda.h"
+#include "dn_residency.h"
 #include <math.h>
 #include <string.h>
 #include <stdarg.h>
@@ -108,6 +109,16 @@ typedef struct DNvolumePriv
 	float sphereK; float spherePts[64][3]; uint32_t sphereValid;
 	struct DNbatch* batch;     /* the batch this volume belongs to, if any */
 	uint64_t batchStamp;       /* the batch run that last listed this volume */
+	/* residency (DN_set_residency) */
+	DNresidency residency;
+	uint64_t createChunks;     /* min(tiles, minChunks) of DN_create_volume (voxel.c:181) */
+	uint64_t syncs;            /* syncs so far */
+	dn_nodes nodes;            /* DN_RESIDENCY_LRU: the reference's voxel buffer nodes */
+	uint8_t* lruState;         /* per tile: 0 absent, 1 unloaded, 2 loaded -- the device's, mirrored */
+	uint32_t* lruLast;         /* per tile: lastUsed, mirrored */
+	uint8_t* lruReq;           /* per tile: requested / touched bytes read back at a sync */
+	uint8_t* lruTouch;
+	uint32_t* lruOp;           /* per tile: 1 + index of its op in the sync being prepared, 0 for none */
 } DNvolumePriv;
 
 static inline DNvolumePriv* priv(DNvolume* v) { return (DNvolumePriv*)v; }
@@ -149,8 +160,32 @@ static void clear_chunk(DNvolume* vol, size_t index)
 
 static size_t num_tiles(DNuvec3 s) { return (size_t)s.x * s.y * s.z; }
 
+static void lru_free(DNvolumePriv* p)
+{
+	dn_nodes_free(&p->nodes);
+	DN_FREE(p->lruState); DN_FREE(p->lruLast); DN_FREE(p->lruReq); DN_FREE(p->lruTouch); DN_FREE(p->lruOp);
+	p->lruState = NULL; p->lruLast = NULL; p->lruReq = NULL; p->lruTouch = NULL; p->lruOp = NULL;
+}
+
+/* the per-tile mirrors of DN_RESIDENCY_LRU, zeroed: every tile absent, lastUsed 0 */
+static bool lru_alloc_tiles(DNvolumePriv* p, size_t tiles)
+{
+	size_t n = tiles ? tiles : 1;
+	DN_FREE(p->lruState); DN_FREE(p->lruLast); DN_FREE(p->lruReq); DN_FREE(p->lruTouch); DN_FREE(p->lruOp);
+	p->lruState = (uint8_t*)DN_MALLOC(n);
+	p->lruLast = (uint32_t*)DN_MALLOC(n * sizeof(uint32_t));
+	p->lruReq = (uint8_t*)DN_MALLOC(n);
+	p->lruTouch = (uint8_t*)DN_MALLOC(n);
+	p->lruOp = (uint32_t*)DN_MALLOC(n * sizeof(uint32_t));
+	if (!p->lruState || !p->lruLast || !p->lruReq || !p->lruTouch || !p->lruOp) return false;
+	memset(p->lruState, 0, n); memset(p->lruLast, 0, n * sizeof(uint32_t));
+	memset(p->lruReq, 0, n); memset(p->lruTouch, 0, n); memset(p->lruOp, 0, n * sizeof(uint32_t));
+	return true;
+}
+
 static void free_priv_arrays(DNvolumePriv* p)
 {
+	lru_free(p);
 	DN_FREE(p->dirty); DN_FREE(p->dirtyList.v); DN_FREE(p->tileSlot);
 	DN_FREE(p->freeSlots.v); DN_FREE(p->slotBase); DN_FREE(p->slotClass); DN_FREE(p->slotGroups);
 	for (int c = 0; c < NUM_CLASSES; c++) DN_FREE(p->freeRanges[c].v);
@@ -208,6 +243,7 @@ static DNvolume* create_volume(DNuvec3 mapSize, unsigned int minChunks, int with
 
 	/* sized from x*y*z (the reference sizes its GPU buffers from x*y*x, voxel.c:173, 184) */
 	size_t numChunks = tiles < minChunks ? tiles : (size_t)minChunks;
+	p->createChunks = numChunks;
 	if (numChunks == 0) numChunks = 1;
 
 	vol->map = (DNchunkHandle*)DN_MALLOC(sizeof(DNchunkHandle) * tiles);
@@ -400,9 +436,9 @@ static bool ensure_slots(DNvolumePriv* p, uint32_t need)
 	return true;
 }
 
-bool DN_set_max_voxels_gpu(DNvolume* vol, size_t num)
+/* grows the device pool keeping its contents */
+static bool pool_reserve(DNvolume* vol, size_t num)
 {
-	/* voxel.c:1031-1082: grows the device pool keeping its contents */
 	if (num <= vol->voxelCap) return true;
 	if (!need_device(vol, "DN_set_max_voxels_gpu")) return false;
 	int rc = dn_cuda_reserve(vol->gpu, 0, num, 0);
@@ -412,6 +448,68 @@ bool DN_set_max_voxels_gpu(DNvolume* vol, size_t num)
 	}
 	vol->voxelCap = num;
 	return true;
+}
+
+bool DN_set_max_voxels_gpu(DNvolume* vol, size_t num)
+{
+	/* voxel.c:1031-1082.  The device pool only grows; with DN_RESIDENCY_LRU the node buffer grows too */
+	DNvolumePriv* p = priv(vol);
+	if (!pool_reserve(vol, num)) return false;
+	if (p->residency == DN_RESIDENCY_LRU && !dn_nodes_grow(&p->nodes, num)) {
+		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to reallocate memory for GPU voxel layout");
+		return false;
+	}
+	return true;
+}
+
+bool DN_set_residency(DNvolume* vol, DNresidency mode)
+{
+	if (!vol) return false;
+	DNvolumePriv* p = priv(vol);
+	if (mode == p->residency) return true;
+	if (mode != DN_RESIDENCY_KEEP && mode != DN_RESIDENCY_LRU) {
+		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "DN_set_residency: unknown mode %d", (int)mode);
+		return false;
+	}
+	if (p->syncs) {
+		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "DN_set_residency: set it before the volume's first DN_sync_gpu");
+		return false;
+	}
+	if (p->batch) {
+		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "DN_set_residency: the volume belongs to a batch");
+		return false;
+	}
+	if (mode == DN_RESIDENCY_LRU) {
+		if (!dn_nodes_init(&p->nodes, p->createChunks) || !lru_alloc_tiles(p, num_tiles(vol->mapSize))) {
+			lru_free(p);
+			dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to allocate memory for GPU voxel layout");
+			return false;
+		}
+	} else {
+		lru_free(p);
+	}
+	p->residency = mode;
+	return true;
+}
+
+DNresidency DN_get_residency(const DNvolume* vol)
+{
+	return vol ? ((const DNvolumePriv*)vol)->residency : DN_RESIDENCY_KEEP;
+}
+
+size_t DN_residency_nodes(const DNvolume* vol, size_t* voxelCap, uint32_t* sizes, uint64_t* starts, int64_t* tiles,
+                          size_t capacity)
+{
+	const DNvolumePriv* p = (const DNvolumePriv*)vol;
+	if (voxelCap) *voxelCap = 0;
+	if (!p || p->residency != DN_RESIDENCY_LRU) return 0;
+	if (voxelCap) *voxelCap = (size_t)p->nodes.voxelCap;
+	for (size_t i = 0; i < p->nodes.n && i < capacity; i++) {
+		if (sizes) sizes[i] = p->nodes.v[i].size;
+		if (starts) starts[i] = p->nodes.v[i].start;
+		if (tiles) tiles[i] = p->nodes.v[i].tile;
+	}
+	return p->nodes.n;
 }
 
 bool DN_set_max_lighting_requests(DNvolume* vol, size_t num)
@@ -482,6 +580,16 @@ bool DN_set_map_size(DNvolume* vol, DNuvec3 size)
 	for (size_t i = 0; i < tiles; i++) p->tileSlot[i] = DN_SLOT_NONE;
 	p->dirtyList.n = 0;
 	release_all_slots(p);
+	if (p->residency == DN_RESIDENCY_LRU) {
+		/* every tile restarts absent: the nodes are freed with the map (the reference keeps their old
+		 * chunk positions, voxel.c:957-1010) */
+		for (size_t i = 0; i < p->nodes.n; i++) p->nodes.v[i].tile = -1;
+		if (!lru_alloc_tiles(p, tiles)) {
+			dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to reallocate the residency state");
+			lru_free(p);
+			p->residency = DN_RESIDENCY_KEEP;
+		}
+	}
 	for (size_t t = 0; t < tiles; t++) if (vol->map[t].flag) mark_dirty(vol, t);
 	return true;
 }
@@ -722,7 +830,7 @@ static bool alloc_slot(DNvolumePriv* p, uint32_t nvox, uint32_t* slotOut)
 			while (p->poolNext + size > nc) nc *= 2;
 			dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_NOTE, "automatically resizing voxel buffer to accomodate %llu GPU voxels (%llu bytes)",
 			       (unsigned long long)nc, (unsigned long long)(nc * 40));
-			if (!DN_set_max_voxels_gpu(&p->pub, nc)) { u32_push(&p->freeSlots, slot); return false; }
+			if (!pool_reserve(&p->pub, nc)) { u32_push(&p->freeSlots, slot); return false; }
 		}
 		base = p->poolNext;
 		p->poolNext += size;
@@ -756,6 +864,124 @@ static bool grow_scratch(void** buf, size_t* cap, size_t need, size_t elem)
 }
 
 /* ---------------------------------------------------------------- sync */
+
+/* the op of tile t in the sync being prepared, appended (with 'flags') when the tile has none; -1 when
+ * the scratch cannot grow */
+static long lru_op(DNvolumePriv* p, uint32_t t, uint32_t* nops, uint32_t flags)
+{
+	if (p->lruOp[t]) return (long)p->lruOp[t] - 1;
+	if (!grow_scratch((void**)&p->ops, &p->opsCap, (size_t)*nops + 1, sizeof(dn_tile_op))) return -1;
+	dn_tile_op* o = &p->ops[*nops];
+	o->tile = t; o->flags = flags; o->slot = DN_SLOT_NONE; o->recordIndex = 0;
+	p->lruOp[t] = ++*nops;
+	return (long)*nops - 1;
+}
+
+/* DN_RESIDENCY_LRU: the per-tile loop of DN_sync_gpu (voxel.c:738-762) on the host's node model, in the
+ * reference's tile order -- lastUsed, the state machine of _DN_stream_to_gpu (1491-1536) and the node
+ * choice of _DN_stream_voxels (1554-1630) -- then the node sort and the buffer growth (764-781).  The
+ * decisions reach the device as tile-op bits.  A chunk that loads without a record slot (it was
+ * evicted) is packed and staged again, as the reference uploads it again. */
+static bool lru_pass(DNvolume* vol, DNmemOp op, uint32_t* nops, uint32_t* nrecs, uint64_t* nvw)
+{
+	DNvolumePriv* p = priv(vol);
+	const size_t tiles = num_tiles(vol->mapSize);
+	if (dn_cuda_read_tile_flags(vol->gpu, p->lruReq, p->lruTouch) != DN_CUDA_OK) {
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "failed to read the tile flags: %s", dn_cuda_last_error());
+		return false;
+	}
+	/* the rays' lastUsed = 0 (voxelShared.comp:143-144) happened before the sync's increments */
+	for (size_t t = 0; t < tiles; t++) if (p->lruTouch[t]) p->lruLast[t] = 0;
+	for (uint32_t k = 0; k < *nops; k++) p->lruOp[p->ops[k].tile] = k + 1;
+	bool grow = false, ok = true;
+	for (uint32_t t = 0; t < (uint32_t)tiles && ok; t++) {
+		if (p->lruLast[t] != UINT32_MAX) p->lruLast[t]++;
+		if (op == DN_READ) continue;
+		uint32_t g = p->lruState[t];
+		if (g == 1 && p->lruReq[t]) g = 3;
+		const bool exists = vol->map[t].flag != 0;
+		const bool updated = p->lruOp[t] && (p->ops[p->lruOp[t] - 1].flags & DN_PEND_UPDATED);
+		if (exists && g == 0) g = 1;
+		else if (!exists && g != 0) { if (g == 2) dn_nodes_unload(&p->nodes, t); g = 0; }
+		if (g == 2 && updated) { dn_nodes_unload(&p->nodes, t); g = 3; }
+		if (g == 3 && exists) {
+			DNchunk* c = &vol->chunks[vol->map[t].chunkIndex];
+			p->lruLast[t] = 0;
+			int64_t victim = -1;
+			int r = dn_nodes_stream(&p->nodes, t, c->numVoxelsGpu, p->lruLast, &victim);
+			if (r < 0) {
+				dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to reallocate memory for GPU voxel layout");
+				ok = false;
+				r = 0;
+			}
+			if (r > 0 && victim >= 0) {
+				/* the node's chunk is unloaded; if it comes later in the loop it meets its turn unloaded */
+				const uint32_t v = (uint32_t)victim;
+				long vi = lru_op(p, v, nops, 0);
+				if (vi < 0) { dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to allocate sync scratch"); ok = false; }
+				else p->ops[vi].flags |= (v < t) ? DN_PEND_EVICT : DN_PEND_EVICTED;
+				p->lruState[v] = 1;
+				if (p->tileSlot[v] != DN_SLOT_NONE) { u32_push(&p->deferredSlots, p->tileSlot[v]); p->tileSlot[v] = DN_SLOT_NONE; }
+			}
+			bool staged = true;
+			if (r > 0 && p->tileSlot[t] == DN_SLOT_NONE) {
+				/* loads without a record (it was evicted): pack and stage it again */
+				staged = false;
+				long oi = lru_op(p, t, nops, DN_PEND_VALID | DN_PEND_EXISTS);
+				uint32_t slot;
+				if (oi < 0 || !grow_scratch((void**)&p->recs, &p->recsCap, (size_t)*nrecs + 1, sizeof(dn_chunk_record)) ||
+				    !grow_scratch((void**)&p->vwords, &p->vwordsCap, (size_t)*nvw + 1024, sizeof(uint32_t))) {
+					dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to allocate sync scratch");
+					ok = false;
+				} else {
+					dn_chunk_record* rec = &p->recs[*nrecs];
+					uint32_t n = pack_chunk(vol, c, rec, &p->vwords[*nvw]);
+					if (!alloc_slot(p, n, &slot)) {
+						dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "failed to stage a chunk on the device");
+					} else {
+						rec->pos[0] = c->pos.x; rec->pos[1] = c->pos.y; rec->pos[2] = c->pos.z;
+						rec->voxBase = p->slotBase[slot];
+						c->numVoxelsGpu = n;
+						dn_tile_op* o = &p->ops[oi];
+						o->flags |= DN_PEND_VALID | DN_PEND_EXISTS | DN_PEND_STAGED;
+						o->slot = slot;
+						o->recordIndex = *nrecs;
+						p->tileSlot[t] = slot;
+						(*nrecs)++;
+						*nvw += 2ull * n;
+						staged = true;
+					}
+				}
+				if (!staged) dn_nodes_unload(&p->nodes, t);   /* it cannot load after all: the node is free again */
+			}
+			if (r > 0 && staged) {
+				g = 2;
+			} else {
+				/* no node: unloaded again, and the buffer doubles after the loop */
+				g = 1;
+				if (r == 0 && ok) grow = true;
+				long oi = lru_op(p, t, nops, 0);
+				if (oi < 0) { dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to allocate sync scratch"); ok = false; }
+				else p->ops[oi].flags |= DN_PEND_HOLD;
+			}
+		}
+		p->lruState[t] = (uint8_t)g;
+	}
+	for (uint32_t k = 0; k < *nops; k++) p->lruOp[p->ops[k].tile] = 0;
+	if (!ok) return false;
+	dn_nodes_sort(&p->nodes, 10);
+	if (grow) {
+		uint64_t nc = p->nodes.voxelCap * 2, lim = (uint64_t)vol->chunkCap * DN_CHUNK_LENGTH;
+		if (nc > lim) nc = lim;
+		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_NOTE, "automatically resizing voxel buffer to accomodate %llu GPU voxels (%llu bytes)",
+		       (unsigned long long)nc, (unsigned long long)(nc * 16));
+		if (!dn_nodes_grow(&p->nodes, nc)) {
+			dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to reallocate memory for GPU voxel layout");
+			return false;
+		}
+	}
+	return true;
+}
 
 /* Host half of DN_sync_gpu (voxel.c:719-786): advances frameNum, packs every dirty chunk into the
  * volume's op / record / voxel-word scratch and fills sp.  Returns false when the scratch cannot grow. */
@@ -821,6 +1047,8 @@ static bool sync_prepare(DNvolume* vol, DNmemOp op, int lightingSplit, dn_sync_p
 			}
 		}
 	}
+	p->syncs++;
+	if (p->residency == DN_RESIDENCY_LRU && !lru_pass(vol, op, &nops, &nrecs, &nvw)) return false;
 	if (p->groupsStaged > vol->lightingRequestCap) DN_set_max_lighting_requests(vol, (size_t)p->groupsStaged * 2);
 
 	spOut->op = (uint32_t)op;
@@ -1278,6 +1506,7 @@ bool DN_batch_add(DNbatch* b, DNvolume* vol)
 {
 	if (!b || !vol || !need_device(vol, "DN_batch_add")) return false;
 	if (priv(vol)->batch) { dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "DN_batch_add: the volume already belongs to a batch"); return false; }
+	if (priv(vol)->residency != DN_RESIDENCY_KEEP) { dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "DN_batch_add: batches hold DN_RESIDENCY_KEEP volumes only"); return false; }
 	if (!grow_scratch((void**)&b->members, &b->membersCap, b->nmembers + 1, sizeof(DNvolume*))) {
 		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to grow a batch");
 		return false;

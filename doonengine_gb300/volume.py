@@ -1,7 +1,7 @@
 """Python mirror of the DN_* API: a thin object wrapper over libdoonengine.so for tests, benchmarks and
 tools.  Every call goes through the C ABI; nothing here computes lighting or traverses rays."""
 import ctypes
-from ctypes import POINTER, byref, c_float, c_uint8, c_uint32, c_uint64, c_void_p
+from ctypes import POINTER, byref, c_float, c_int64, c_size_t, c_uint8, c_uint32, c_uint64, c_void_p
 
 import numpy as np
 
@@ -261,6 +261,24 @@ class Volume:
         if not ok:
             raise RuntimeError("DN_export_tiles failed: %s" % self.lib.dn_cuda_last_error().decode())
         return st, vis, lu, ns
+
+    def set_residency(self, mode):
+        """DN_set_residency: "keep" (default) or "lru" (the reference's fixed voxel buffer with least-recently-used
+        unloading); before the volume's first sync"""
+        m = {"keep": 0, "lru": 1}[mode]
+        if not self.lib.DN_set_residency(self.ptr, m):
+            raise RuntimeError("DN_set_residency(%s) failed" % mode)
+
+    def residency_nodes(self):
+        """DN_RESIDENCY_LRU: (buffer size in voxels, node sizes, first voxels, owning tiles or -1)"""
+        cap = c_size_t(0)
+        n = self.lib.DN_residency_nodes(self.ptr, ctypes.byref(cap), None, None, None, 0)
+        sizes = np.zeros(max(n, 1), np.uint32)
+        starts = np.zeros(max(n, 1), np.uint64)
+        tiles = np.zeros(max(n, 1), np.int64)
+        self.lib.DN_residency_nodes(self.ptr, ctypes.byref(cap), sizes.ctypes.data_as(POINTER(c_uint32)),
+                                    starts.ctypes.data_as(POINTER(c_uint64)), tiles.ctypes.data_as(POINTER(c_int64)), n)
+        return int(cap.value), sizes[:n], starts[:n], tiles[:n]
 
     def export_requests(self):
         n = self.lib.DN_export_requests(self.ptr, None, 0)

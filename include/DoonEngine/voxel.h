@@ -200,6 +200,25 @@ bool DN_set_max_chunks(DNvolume* vol, size_t num);
 bool DN_set_max_voxels_gpu(DNvolume* vol, size_t num);
 bool DN_set_max_lighting_requests(DNvolume* vol, size_t num);
 
+/* Device residency of chunks.
+ *   DN_RESIDENCY_KEEP (default): a chunk loads at the sync after a ray requests it and stays loaded until
+ *     it is edited or removed; the device pool grows as needed.
+ *   DN_RESIDENCY_LRU: the reference's fixed GPU voxel buffer (voxel.c:1538-1695): power-of-two nodes of
+ *     16..512 voxels in a buffer of 512 * min(tiles, minChunks) / 2 voxels.  A requested chunk takes the
+ *     smallest free node that fits, else the node of the loaded chunk unused for the most syncs (more
+ *     than one), which is unloaded and must be requested again; with neither, it stays unloaded and the
+ *     buffer doubles (up to 512 voxels per chunk slot) at the end of the sync.  Each sync reads the
+ *     rays' request and use flags back from the device first, so it waits for the map's earlier work.
+ * Set before the volume's first DN_sync_gpu, outside a batch; false otherwise. */
+typedef enum DNresidency { DN_RESIDENCY_KEEP = 0, DN_RESIDENCY_LRU = 1 } DNresidency;
+bool DN_set_residency(DNvolume* vol, DNresidency mode);
+DNresidency DN_get_residency(const DNvolume* vol);
+/* DN_RESIDENCY_LRU: the node buffer's size in voxels (*voxelCap) and its nodes in buffer order -- size,
+ * first voxel, owning tile or -1 -- for up to 'capacity' nodes (NULL arrays: count only).  Returns the
+ * node count (0 with DN_RESIDENCY_KEEP). */
+size_t DN_residency_nodes(const DNvolume* vol, size_t* voxelCap, uint32_t* sizes, uint64_t* starts, int64_t* tiles,
+                          size_t capacity);
+
 /* MAP UTILITY (voxel.h:269-344) */
 bool DN_in_map_bounds(DNvolume* vol, DNivec3 pos);
 bool DN_in_chunk_bounds(DNivec3 pos);

@@ -53,6 +53,11 @@ typedef struct dn_chunk_record {
 #define DN_PEND_EXISTS  0x2u   /* the chunk exists on the CPU (DNchunkHandle.flag != 0) */
 #define DN_PEND_UPDATED 0x4u   /* DNchunk.updated was set */
 #define DN_PEND_STAGED  0x8u   /* a freshly packed record was staged into 'slot' */
+/* DN_RESIDENCY_LRU decisions of the host's node model (voxel.c:1554-1630); the tile's record slot is
+ * dropped with an eviction */
+#define DN_PEND_EVICT   0x10u  /* a later tile of this sync took the chunk's node: unloaded after its requests */
+#define DN_PEND_EVICTED 0x20u  /* an earlier tile of this sync took the chunk's node: unloaded before its turn */
+#define DN_PEND_HOLD    0x40u  /* the requested chunk found no node: unloaded again, lastUsed 0 */
 typedef struct dn_tile_op {
     uint32_t tile;
     uint32_t flags;
@@ -229,6 +234,9 @@ int dn_cuda_stats_kind(struct DNgpuVolume* g, int kind, dn_stats* out);
 int dn_cuda_reset_stats(struct DNgpuVolume* g);
 void* dn_cuda_stream(struct DNgpuVolume* g);
 int dn_cuda_export_tiles(struct DNgpuVolume* g, uint8_t* state, uint8_t* vis, uint32_t* lastUsed, uint32_t* samples);
+/* the per-tile requested and touched bytes the rays set since the last sync (waits for the map's stream);
+ * the host's residency model reads them before it decides a sync */
+int dn_cuda_read_tile_flags(struct DNgpuVolume* g, uint8_t* requested, uint8_t* touched);
 int dn_cuda_export_requests(struct DNgpuVolume* g, uint32_t* out, uint64_t capacity, uint64_t* count);
 /* lighting of every loaded chunk; rows ordered by tile then rank */
 int dn_cuda_export_lighting(struct DNgpuVolume* g, uint32_t* index, float* diff, float* spec,

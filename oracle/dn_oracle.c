@@ -239,6 +239,9 @@ typedef struct orec {
     float (*spec)[3];
 } orec;
 
+/* a node of the reference's GPU voxel buffer (DNvoxelNode, voxel.h:74-79); tile -1 = unused */
+typedef struct onode { uint32_t size; uint64_t start; int64_t tile; } onode;
+
 struct dno_map {
     uint32_t sx, sy, sz;
     uint64_t ntiles;
@@ -251,6 +254,11 @@ struct dno_map {
     uint32_t* req;
     uint32_t nreq, reqCap;
     dno_counters ctr;
+    /* LRU residency (the reference's node buffer) */
+    int lru;
+    onode* nodes;
+    size_t nnodes, nodesCap;
+    uint64_t voxelCap, chunkCap;
 };
 
 static void rec_free(orec* r)
@@ -279,6 +287,7 @@ void dno_destroy(dno_map* m)
     if (!m) return;
     if (m->rec) for (uint64_t t = 0; t < m->ntiles; t++) rec_free(&m->rec[t]);
     free(m->state); free(m->vis); free(m->touch); free(m->lastUsed); free(m->rec); free(m->req);
+    free(m->nodes);
     free(m);
 }
 
@@ -308,6 +317,136 @@ static void push_req(dno_map* m, uint32_t w)
     m->req[m->nreq++] = w;
 }
 
+/* ---------------------------------------------- LRU residency (node buffer) */
+
+static void nodes_reserve(dno_map* m, size_t n)
+{
+    if (n <= m->nodesCap) return;
+    size_t c = m->nodesCap ? m->nodesCap : 64;
+    while (c < n) c *= 2;
+    m->nodes = (onode*)realloc(m->nodes, c * sizeof(onode));
+    m->nodesCap = c;
+}
+
+/* DN_set_max_voxels_gpu's node part (voxel.c:1064-1079): (num - voxelCap) / 512 whole nodes appended */
+static void nodes_grow(dno_map* m, uint64_t num)
+{
+    if (num <= m->voxelCap) return;
+    int numNewNodes = (int)((num - m->voxelCap) / 512);
+    nodes_reserve(m, m->nnodes + (size_t)numNewNodes);
+    for (int i = 0; i < numNewNodes; i++) {
+        onode* nd = &m->nodes[m->nnodes + (size_t)i];
+        nd->tile = -1;
+        nd->size = 512;
+        nd->start = m->voxelCap + (uint64_t)i * 512;
+    }
+    m->nnodes += (size_t)numNewNodes;
+    m->voxelCap = num;
+}
+
+void dno_set_lru(dno_map* m, uint64_t numChunks)
+{
+    /* DN_create_volume's buffer (voxel.c:181, 190, 235-249): 512 * numChunks / 2 voxels of 512-voxel nodes */
+    m->lru = 1;
+    m->voxelCap = 512 * numChunks / 2;
+    m->nnodes = (size_t)(m->voxelCap / 512);
+    nodes_reserve(m, m->nnodes ? m->nnodes : 1);
+    for (size_t i = 0; i < m->nnodes; i++) {
+        m->nodes[i].tile = -1;
+        m->nodes[i].size = 512;
+        m->nodes[i].start = (uint64_t)i * 512;
+    }
+    m->chunkCap = numChunks;
+}
+
+void dno_set_chunk_cap(dno_map* m, uint64_t chunkCap) { m->chunkCap = chunkCap; }
+
+size_t dno_lru_nodes(const dno_map* m, uint64_t* voxelCap, uint32_t* sizes, uint64_t* starts, int64_t* tiles, size_t cap)
+{
+    if (voxelCap) *voxelCap = m->lru ? m->voxelCap : 0;
+    if (!m->lru) return 0;
+    for (size_t i = 0; i < m->nnodes && i < cap; i++) {
+        if (sizes) sizes[i] = m->nodes[i].size;
+        if (starts) starts[i] = m->nodes[i].start;
+        if (tiles) tiles[i] = m->nodes[i].tile;
+    }
+    return m->nnodes;
+}
+
+/* _DN_unload_voxels (voxel.c:1538-1546) */
+static void lru_unload(dno_map* m, int64_t tile)
+{
+    for (size_t i = 0; i < m->nnodes; i++)
+        if (m->nodes[i].tile == tile) { m->nodes[i].tile = -1; break; }
+}
+
+/* _DN_stream_voxels (voxel.c:1554-1640) without the upload: 1 with a node (*victim = the tile whose node was
+ * taken, or -1), 0 without (the buffer must grow).  The reference compares the unsigned node size with its
+ * int best size, which starts at -1: as unsigned that is the largest value. */
+static int lru_stream(dno_map* m, int64_t tile, uint32_t numVoxels, int64_t* victim)
+{
+    *victim = -1;
+    int nodeSize = 16;
+    while (nodeSize < (int)numVoxels) nodeSize *= 2;
+    uint32_t maxTime = 0;
+    int maxTimeNodeSize = -1;
+    long maxTimeIndex = -1;
+    for (size_t i = 0; i < m->nnodes; i++) {
+        if (m->nodes[i].size < (uint32_t)nodeSize) continue;
+        uint32_t time = m->nodes[i].tile >= 0 ? m->lastUsed[m->nodes[i].tile] : UINT32_MAX;
+        if (time > maxTime || (time == UINT32_MAX && m->nodes[i].size < (uint32_t)maxTimeNodeSize)) {
+            maxTime = time;
+            maxTimeNodeSize = (int)m->nodes[i].size;
+            maxTimeIndex = (long)i;
+        }
+        if (maxTimeNodeSize == nodeSize && maxTime == UINT32_MAX) break;
+    }
+    if (maxTimeIndex < 0 || maxTime <= 1) return 0;
+    *victim = m->nodes[maxTimeIndex].tile;
+    if (maxTimeNodeSize > nodeSize) {
+        int numAdded = 0;
+        while (maxTimeNodeSize > nodeSize) { maxTimeNodeSize /= 2; numAdded++; }
+        nodes_reserve(m, m->nnodes + (size_t)numAdded);
+        uint64_t orgStart = m->nodes[maxTimeIndex].start;
+        memmove(&m->nodes[maxTimeIndex + numAdded], &m->nodes[maxTimeIndex], sizeof(onode) * (m->nnodes - (size_t)maxTimeIndex));
+        uint32_t mult = 1;
+        for (long i = maxTimeIndex; i <= maxTimeIndex + numAdded; i++) {
+            m->nodes[i].size = (uint32_t)nodeSize * mult;
+            m->nodes[i].start = orgStart + (i == maxTimeIndex ? 0 : (uint64_t)nodeSize * mult);
+            m->nodes[i].tile = -1;
+            if (i > maxTimeIndex) mult *= 2;
+        }
+        m->nnodes += (size_t)numAdded;
+    }
+    m->nodes[maxTimeIndex].tile = tile;
+    return 1;
+}
+
+/* _DN_sort_gpu_voxel_buffer (voxel.c:1642-1695); with no node the loop does not run (the reference's
+ * size_t count minus one would wrap) */
+static void lru_sort(dno_map* m, int maxCopies)
+{
+    int numCopies = 0;
+    for (size_t i = 0; m->nnodes > 0 && i < m->nnodes - 1; i++) {
+        onode cur = m->nodes[i], next = m->nodes[i + 1];
+        if (cur.tile >= 0) continue;
+        if (next.tile >= 0 || next.size < cur.size) {
+            numCopies++;
+            next.start -= cur.size;
+            cur.start += next.size;
+            m->nodes[i] = next;
+            m->nodes[i + 1] = cur;
+        }
+        if (next.tile < 0 && cur.size == next.size && cur.size < 512) {
+            numCopies++;
+            m->nodes[i].size *= 2;
+            if (i < m->nnodes - 2) memmove(&m->nodes[i + 1], &m->nodes[i + 2], sizeof(onode) * (m->nnodes - i - 2));
+            m->nnodes--;
+        }
+        if (numCopies > maxCopies) break;
+    }
+}
+
 void dno_sync(dno_map* m, const dno_handle* cpuMap, const dno_chunk* chunks,
               const dno_material* mats, int op, int split)
 {
@@ -316,12 +455,16 @@ void dno_sync(dno_map* m, const dno_handle* cpuMap, const dno_chunk* chunks,
     m->frameNum++;
     if (m->frameNum >= (uint32_t)split) m->frameNum = 0;
     m->nreq = 0;
+    int resizeVoxels = 0;
+    /* lastUsed: rays set it to 0 during the frame (D4: when entering a loaded chunk), so every tile's value
+     * is 0 before the loop reaches it; the loop adds 1 */
+    for (uint64_t t = 0; t < m->ntiles; t++) {
+        if (m->touch[t]) m->lastUsed[t] = 0;
+        m->touch[t] = 0;
+    }
     for (uint64_t t = 0; t < m->ntiles; t++) {
         int gflag = m->state[t];
         int vis = m->vis[t];
-        /* lastUsed: rays set it to 0 (D4: when entering a loaded chunk); sync adds 1 */
-        if (m->touch[t]) m->lastUsed[t] = 0;
-        m->touch[t] = 0;
         if (m->lastUsed[t] != 0xFFFFFFFFu) m->lastUsed[t]++;
         int exists = cpuMap[t].flag != 0;
         int updated = exists ? chunks[cpuMap[t].chunkIndex].updated != 0 : 0;
@@ -335,13 +478,41 @@ void dno_sync(dno_map* m, const dno_handle* cpuMap, const dno_chunk* chunks,
             /* every assignment of the reference's flags word clears the visible bit */
             int changed = 0;
             if (exists && gflag == 0) { gflag = 1; changed = 1; }
-            else if (!exists && gflag != 0) { if (gflag == 2) rec_free(&m->rec[t]); gflag = 0; changed = 1; }
-            if (gflag == 2 && updated) { rec_free(&m->rec[t]); gflag = 3; changed = 1; }
-            if (gflag == 3 && exists) { rec_load(&m->rec[t], &chunks[cpuMap[t].chunkIndex], mats); gflag = 2; m->lastUsed[t] = 0; changed = 1; }
+            else if (!exists && gflag != 0) {
+                if (gflag == 2) { rec_free(&m->rec[t]); if (m->lru) lru_unload(m, (int64_t)t); }
+                gflag = 0; changed = 1;
+            }
+            if (gflag == 2 && updated) { rec_free(&m->rec[t]); if (m->lru) lru_unload(m, (int64_t)t); gflag = 3; changed = 1; }
+            if (gflag == 3 && exists) {
+                rec_load(&m->rec[t], &chunks[cpuMap[t].chunkIndex], mats);
+                gflag = 2; m->lastUsed[t] = 0; changed = 1;
+                if (m->lru) {
+                    int64_t victim;
+                    if (!lru_stream(m, (int64_t)t, m->rec[t].nvox, &victim)) {
+                        /* no node: the chunk stays unloaded and the buffer grows after the loop */
+                        rec_free(&m->rec[t]);
+                        gflag = 1;
+                        resizeVoxels = 1;
+                    } else if (victim >= 0) {
+                        /* the node's chunk is unloaded (its flags word set to 1, which clears the visible
+                         * bit); its voxels are gone and a later load packs it again */
+                        m->state[victim] = 1;
+                        m->vis[victim] = 0;
+                        rec_free(&m->rec[victim]);
+                    }
+                }
+            }
             if (changed) vis = 0;
         }
         m->state[t] = (uint8_t)gflag;
         m->vis[t] = (uint8_t)vis;
+    }
+    if (m->lru) {
+        lru_sort(m, 10);
+        if (resizeVoxels) {
+            uint64_t newCap = m->voxelCap * 2 < m->chunkCap * 512 ? m->voxelCap * 2 : m->chunkCap * 512;
+            nodes_grow(m, newCap);
+        }
     }
 }
 

@@ -193,6 +193,14 @@ typedef struct dno_counters {
 void dno_sync(dno_map* m, const dno_handle* cpuMap, const dno_chunk* chunks,
               const dno_material* materials, int op, int lightingSplit);
 
+/* LRU residency: the reference's GPU voxel buffer of power-of-two nodes (voxel.c:1538-1695), as the
+ * product's DN_RESIDENCY_LRU.  dno_set_lru starts it with DN_create_volume's buffer for numChunks chunk
+ * slots (before the first sync); dno_set_chunk_cap gives the CPU chunk capacity that bounds the buffer's
+ * growth (call it before each sync); dno_lru_nodes exports the nodes in buffer order. */
+void dno_set_lru(dno_map* m, uint64_t numChunks);
+void dno_set_chunk_cap(dno_map* m, uint64_t chunkCap);
+size_t dno_lru_nodes(const dno_map* m, uint64_t* voxelCap, uint32_t* sizes, uint64_t* starts, int64_t* tiles, size_t cap);
+
 /* Lighting update over the current request list (voxelLighting.comp:207-288). */
 void dno_light(dno_map* m, const dno_material* materials, const dno_light_params* p, int nthreads);
 

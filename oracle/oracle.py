@@ -11,7 +11,7 @@ import ctypes
 import os
 import platform
 import subprocess
-from ctypes import POINTER, Structure, c_float, c_int, c_int32, c_uint8, c_uint16, c_uint32, c_uint64, c_void_p
+from ctypes import POINTER, Structure, c_float, c_int, c_int32, c_uint8, c_uint16, c_uint32, c_uint64, c_void_p, c_size_t
 
 import numpy as np
 
@@ -94,6 +94,9 @@ def load():
         ("dno_get_counters", None, [c_void_p, POINTER(Counters)]),
         ("dno_reset_counters", None, [c_void_p]),
         ("dno_export_tiles", None, [c_void_p, c_void_p, c_void_p, c_void_p]),
+        ("dno_set_lru", None, [c_void_p, c_uint64]),
+        ("dno_set_chunk_cap", None, [c_void_p, c_uint64]),
+        ("dno_lru_nodes", c_size_t, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t]),
         ("dno_export_lighting", c_uint64, [c_void_p, c_void_p, c_void_p, c_void_p]),
         ("dno_export_samples", None, [c_void_p, c_void_p]),
         ("dno_import_lighting", None, [c_void_p, c_uint64, c_void_p, c_void_p, c_void_p]),
@@ -143,6 +146,7 @@ class OracleMap:
             raise MemoryError("dno_create")
         self.frame = 0
         self.last_time = 123.456   # reference default, voxel.c:278
+        self.lru = False
 
     def close(self):
         if self.ptr:
@@ -160,8 +164,25 @@ class OracleMap:
         x, y, z = self.map_size
         return x * y * z
 
+    def set_lru(self, num_chunks):
+        """the reference's node buffer with least-recently-used unloading, for num_chunks = min(tiles, minChunks)"""
+        self.lib.dno_set_lru(self.ptr, num_chunks)
+        self.lru = True
+
+    def lru_nodes(self):
+        """(buffer size in voxels, node sizes, first voxels, owning tiles or -1)"""
+        cap = c_uint64(0)
+        n = self.lib.dno_lru_nodes(self.ptr, ctypes.byref(cap), None, None, None, 0)
+        sizes = np.zeros(max(n, 1), np.uint32)
+        starts = np.zeros(max(n, 1), np.uint64)
+        tiles = np.zeros(max(n, 1), np.int64)
+        self.lib.dno_lru_nodes(self.ptr, ctypes.byref(cap), sizes.ctypes.data, starts.ctypes.data, tiles.ctypes.data, n)
+        return int(cap.value), sizes[:n], starts[:n], tiles[:n]
+
     def sync(self, vol_s, op=2, split=1):
         """vol_s: a product DNvolume struct (ctypes); reads map / chunks / materials before the product's sync."""
+        if self.lru:
+            self.lib.dno_set_chunk_cap(self.ptr, vol_s.chunkCap)
         self.lib.dno_sync(self.ptr, ctypes.cast(vol_s.map, c_void_p), ctypes.cast(vol_s.chunks, c_void_p),
                           ctypes.cast(vol_s.materials, c_void_p), op, split)
         self.frame = self.lib.dno_frame_num(self.ptr)
