@@ -75,6 +75,12 @@
  *       a zero or NaN direction component makes a side distance NaN
  *       (0 * inf) after one step, after which the reference's loop
  *       (voxelShared.comp:339, 435) would never end.
+ *   D18 LRU residency (dno_set_lru): the reference's node buffer decides
+ *       loads, unloads and growth in its tile order (voxel.c:1491-1695); a
+ *       chunk unloaded later in the same sync keeps its requests, which
+ *       light nothing (the reference would light the slots' new data); a
+ *       reload packs the chunk again; with no node the sort does not run.
+ *       Unpinned: the reference's allocator touches OpenGL on every path.
  */
 #ifndef DN_ORACLE_H
 #define DN_ORACLE_H
