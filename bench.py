@@ -161,6 +161,8 @@ def run_ours(args):
     dn.init()
     vol, cfg = configs.build_volume(args.config, seed=configs.CONFIGS[args.config]["seed"] + 1000 * rank)
     vol.s.mapId = rank
+    if args.residency == "lru":
+        vol.set_residency("lru")
     nonempty = vol.nonempty_chunks() / vol.num_tiles
     W, H = cfg["res"]
     img = dn.Image(W, H, on_device=True)
@@ -247,7 +249,10 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
         "ms_per_step": dev_ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded heightfield + boxes/spheres; the reference publishes no scenes)",
-        "config": dict(workload_desc(cfg, vol, nonempty, args.config), parallelism="replicas: one map per GPU, no collective"),
+        "config": dict(workload_desc(cfg, vol, nonempty, args.config), parallelism="replicas: one map per GPU, no collective",
+                       **({"residency": "DN_RESIDENCY_LRU (the reference's voxel-buffer nodes; each sync reads the "
+                                        "rays' flags back and walks the tiles on the host)"}
+                          if args.residency == "lru" else {})),
         "lit_voxels_per_s": lit_total / (dev_ms_max / 1e3),
         "primary_rays_per_s": prim_total / (dev_ms_max / 1e3),
         "rays_per_step": rays_total / K,
@@ -978,6 +983,8 @@ def main():
                     help="plain: one map per step (the headline); batched: many maps per step")
     ap.add_argument("--maps", type=int, default=64, help="maps of the batched workload")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--residency", default="keep", choices=["keep", "lru"],
+                    help="plain workload: chunk residency (DN_set_residency); lru = the reference's voxel-buffer nodes")
     ap.add_argument("--rates", default="100,200,300,400,500,600,700,850,1000,1100,1200,1300,1400,1500,2000,5000,10000,20000",
                     help="serving: offered req/s, swept upwards until the server saturates")
     ap.add_argument("--seconds", type=float, default=4.0, help="serving: seconds of arrivals per rate")
