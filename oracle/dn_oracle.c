@@ -447,6 +447,13 @@ static void lru_sort(dno_map* m, int maxCopies)
     }
 }
 
+/* the node model's steps on their own, for a differential test against the product's model */
+int dno_lru_stream(dno_map* m, int64_t tile, uint32_t nvox, int64_t* victim) { return lru_stream(m, tile, nvox, victim); }
+void dno_lru_unload(dno_map* m, int64_t tile) { lru_unload(m, tile); }
+void dno_lru_sort(dno_map* m, int maxCopies) { lru_sort(m, maxCopies); }
+void dno_lru_grow(dno_map* m, uint64_t num) { nodes_grow(m, num); }
+void dno_set_last_used(dno_map* m, const uint32_t* lastUsed) { memcpy(m->lastUsed, lastUsed, m->ntiles * sizeof(uint32_t)); }
+
 void dno_sync(dno_map* m, const dno_handle* cpuMap, const dno_chunk* chunks,
               const dno_material* mats, int op, int split)
 {

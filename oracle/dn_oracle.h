@@ -206,6 +206,14 @@ void dno_sync(dno_map* m, const dno_handle* cpuMap, const dno_chunk* chunks,
 void dno_set_lru(dno_map* m, uint64_t numChunks);
 void dno_set_chunk_cap(dno_map* m, uint64_t chunkCap);
 size_t dno_lru_nodes(const dno_map* m, uint64_t* voxelCap, uint32_t* sizes, uint64_t* starts, int64_t* tiles, size_t cap);
+/* the node model's steps on their own (a differential test drives them with random sequences):
+ * _DN_stream_voxels' choice (1 with a node, *victim the previous owner or -1; 0 without), _DN_unload_voxels,
+ * the sort pass, whole-node growth; lastUsed replaced for every tile */
+int dno_lru_stream(dno_map* m, int64_t tile, uint32_t nvox, int64_t* victim);
+void dno_lru_unload(dno_map* m, int64_t tile);
+void dno_lru_sort(dno_map* m, int maxCopies);
+void dno_lru_grow(dno_map* m, uint64_t num);
+void dno_set_last_used(dno_map* m, const uint32_t* lastUsed);
 
 /* Lighting update over the current request list (voxelLighting.comp:207-288). */
 void dno_light(dno_map* m, const dno_material* materials, const dno_light_params* p, int nthreads);

@@ -97,6 +97,11 @@ def load():
         ("dno_set_lru", None, [c_void_p, c_uint64]),
         ("dno_set_chunk_cap", None, [c_void_p, c_uint64]),
         ("dno_lru_nodes", c_size_t, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t]),
+        ("dno_lru_stream", c_int, [c_void_p, ctypes.c_int64, c_uint32, c_void_p]),
+        ("dno_lru_unload", None, [c_void_p, ctypes.c_int64]),
+        ("dno_lru_sort", None, [c_void_p, c_int]),
+        ("dno_lru_grow", None, [c_void_p, c_uint64]),
+        ("dno_set_last_used", None, [c_void_p, c_void_p]),
         ("dno_export_lighting", c_uint64, [c_void_p, c_void_p, c_void_p, c_void_p]),
         ("dno_export_samples", None, [c_void_p, c_void_p]),
         ("dno_import_lighting", None, [c_void_p, c_uint64, c_void_p, c_void_p, c_void_p]),

@@ -91,3 +91,84 @@ def test_oracle_lru_unloads_and_reloads():
     finally:
         om.close()
         vol.close()
+
+
+class _Node(ctypes.Structure):
+    _fields_ = [("size", ctypes.c_uint32), ("start", ctypes.c_uint64), ("tile", ctypes.c_int64)]
+
+
+class _Nodes(ctypes.Structure):
+    _fields_ = [("v", ctypes.POINTER(_Node)), ("n", ctypes.c_size_t), ("cap", ctypes.c_size_t),
+                ("voxelCap", ctypes.c_uint64)]
+
+
+def test_node_models_agree_on_random_sequences():
+    """the product's node model (csrc/dn_residency.c, inside libdoonengine.so) and the oracle's restatement,
+    driven by the same random sequences of streams, unloads, sort passes and growth"""
+    import doonengine_gb300 as dn
+    lib = dn.load()
+    lib.dn_nodes_init.argtypes = [ctypes.POINTER(_Nodes), ctypes.c_uint64]
+    lib.dn_nodes_stream.argtypes = [ctypes.POINTER(_Nodes), ctypes.c_int64, ctypes.c_uint32,
+                                    ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int64)]
+    lib.dn_nodes_unload.argtypes = [ctypes.POINTER(_Nodes), ctypes.c_int64]
+    lib.dn_nodes_sort.argtypes = [ctypes.POINTER(_Nodes), ctypes.c_int]
+    lib.dn_nodes_grow.argtypes = [ctypes.POINTER(_Nodes), ctypes.c_uint64]
+    lib.dn_nodes_free.argtypes = [ctypes.POINTER(_Nodes)]
+    ntiles = 96
+    seen = {"evict": 0, "fail": 0, "split": 0, "merge": 0}
+    for seed in range(12):
+        rng = np.random.default_rng(seed)
+        chunks = int(rng.integers(2, 24))
+        b = _Nodes()
+        assert lib.dn_nodes_init(ctypes.byref(b), chunks)
+        om = O.OracleMap((4, 4, 6))
+        om.set_lru(chunks)
+        owned = set()
+        stale_bias = rng.uniform(0.2, 0.9)
+        try:
+            for step in range(400):
+                lu = np.where(rng.random(ntiles) < stale_bias, rng.integers(2, 9, ntiles),
+                              rng.integers(0, 2, ntiles)).astype(np.uint32)
+                om.lib.dno_set_last_used(om.ptr, lu.ctypes.data)
+                op = rng.random()
+                if op < 0.6 and len(owned) < ntiles:
+                    free_tiles = [t for t in range(ntiles) if t not in owned]
+                    t = int(rng.choice(free_tiles))
+                    nvox = int(rng.choice([0, 1, 16, 17, 33, 100, 200, 256, 300, 511, 512]))
+                    gv, ov = ctypes.c_int64(-2), ctypes.c_int64(-2)
+                    gr = lib.dn_nodes_stream(ctypes.byref(b), t, nvox,
+                                             lu.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), ctypes.byref(gv))
+                    orr = om.lib.dno_lru_stream(om.ptr, t, nvox, ctypes.byref(ov))
+                    assert gr == orr and (gr == 0 or gv.value == ov.value), (seed, step, gr, orr, gv.value, ov.value)
+                    if gr:
+                        seen["evict"] += gv.value >= 0
+                        owned.add(t)
+                        owned.discard(gv.value)
+                    else:
+                        seen["fail"] += 1
+                    if not gr and rng.random() < 0.7:
+                        cap = b.voxelCap * 2 if b.voxelCap else 512
+                        lib.dn_nodes_grow(ctypes.byref(b), cap)
+                        om.lib.dno_lru_grow(om.ptr, cap)
+                elif op < 0.8 and owned:
+                    t = int(rng.choice(sorted(owned)))
+                    lib.dn_nodes_unload(ctypes.byref(b), t)
+                    om.lib.dno_lru_unload(om.ptr, t)
+                    owned.discard(t)
+                else:
+                    mc = int(rng.integers(0, 12))
+                    n0 = b.n
+                    lib.dn_nodes_sort(ctypes.byref(b), mc)
+                    seen["merge"] += b.n < n0
+                    om.lib.dno_lru_sort(om.ptr, mc)
+                cap, sizes, starts, tiles = om.lru_nodes()
+                seen["split"] += int((sizes < 512).any())
+                assert b.voxelCap == cap and b.n == len(sizes), (seed, step)
+                got = [(b.v[i].size, b.v[i].start, b.v[i].tile) for i in range(b.n)]
+                assert got == list(zip(sizes.tolist(), starts.tolist(), tiles.tolist())), (seed, step)
+                assert set(tiles[tiles >= 0].tolist()) == owned, (seed, step)
+        finally:
+            lib.dn_nodes_free(ctypes.byref(b))
+            om.close()
+    # every decision of the model occurred
+    assert all(v > 0 for v in seen.values()), seen
