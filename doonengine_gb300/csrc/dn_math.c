@@ -1,11 +1,14 @@
 /*
  * dn_math.c -- vector / matrix helpers of the DN_* API (see dn_math.h).
  *
- * Restated from the underlying maths, not from the reference's vendored
- * header: Tait-Bryan Z*Y*X rotation, the OpenGL-style perspective frustum,
- * a right-handed look-at basis, and a cofactor (adjugate / determinant)
- * inverse.  Compiled with -ffp-contract=off so results do not depend on FMA
- * contraction.  Matrices are column-major, m[col][row].
+ * Tait-Bryan Z*Y*X rotation, the OpenGL-style perspective frustum and a
+ * right-handed look-at basis are restated from the underlying maths.  The
+ * cofactor (adjugate / determinant) inverse DN_mat4_inv and the quaternion
+ * helpers follow the reference's vendored math header (QuickMath,
+ * quickmath.h mat4_inv and the quaternion functions) operation by operation,
+ * because the camera matrices and shape transforms must be bit-identical to
+ * the reference's.  Compiled with -ffp-contract=off so results do not depend
+ * on FMA contraction.  Matrices are column-major, m[col][row].
  */
 #include "DoonEngine/dn_math.h"
 #include <math.h>

@@ -64,9 +64,18 @@ def build():
     return LIB
 
 
-def build_reference(ref_root="/root/reference"):
-    """Compile the reference's own host C into oracle/_ref (x86-64 only; needs the reference tree)."""
-    if platform.machine() not in ("x86_64", "AMD64") or not os.path.isdir(ref_root):
+def reference_root(arg=None):
+    """The reference tree's root: an explicit argument, else the DN_REFERENCE_ROOT environment variable;
+    None when neither names an existing directory."""
+    root = arg or os.environ.get("DN_REFERENCE_ROOT")
+    return root if root and os.path.isdir(root) else None
+
+
+def build_reference(ref_root=None):
+    """Compile the reference's own host C into oracle/_ref (x86-64 only; needs the reference tree, named by
+    ref_root or DN_REFERENCE_ROOT).  Returns the library path, or None when it cannot be built here."""
+    ref_root = reference_root(ref_root)
+    if platform.machine() not in ("x86_64", "AMD64") or ref_root is None:
         return None
     subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "REF=" + ref_root], check=True)
     return REF_LIB

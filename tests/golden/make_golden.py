@@ -87,7 +87,9 @@ def materials_table(rng, n=256):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = O.reference_root(sys.argv[1] if len(sys.argv) > 1 else None)
+    if ref_root is None:
+        sys.exit("usage: %s REFERENCE_ROOT (or set DN_REFERENCE_ROOT)" % sys.argv[0])
     lib = load_ref(ref_root)
     rng = np.random.default_rng(20261203)
     out = {}

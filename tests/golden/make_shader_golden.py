@@ -25,6 +25,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
 from make_golden import load_ref, CHUNK_BYTES  # noqa: E402
+from oracle import oracle as O  # noqa: E402
 
 INV255 = np.float32(0.00392156862)
 INV65535 = np.float32(0.0000152590219)
@@ -157,7 +158,9 @@ def requests_for(size, mapb, chunks):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = O.reference_root(sys.argv[1] if len(sys.argv) > 1 else None)
+    if ref_root is None:
+        sys.exit("usage: %s REFERENCE_ROOT (or set DN_REFERENCE_ROOT)" % sys.argv[0])
     ref = load_ref(ref_root)
     pin = load_pin(ref_root)
     src = open(os.path.join(ref_root, "assets", "shaders", "voxelLighting.comp")).read()

@@ -108,7 +108,9 @@ def run(lib, ops):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = O.reference_root(sys.argv[1] if len(sys.argv) > 1 else None)
+    if ref_root is None:
+        sys.exit("usage: %s REFERENCE_ROOT (or set DN_REFERENCE_ROOT)" % sys.argv[0])
     path = O.build_reference(ref_root)
     if not path:
         raise SystemExit("the reference host C builds only on x86-64 with the reference tree present")
