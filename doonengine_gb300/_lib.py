@@ -281,6 +281,7 @@ _SIGS = [
     ("dn_cuda_sync", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p, c_uint32, c_void_p, c_uint64]),
     ("dn_cuda_light", c_int, [c_void_p, c_void_p, c_void_p]),
     ("dn_cuda_light_noalloc", c_int, [c_void_p, c_void_p, c_void_p]),
+    ("dn_cuda_light_noalloc_set_limit", c_uint32, [c_uint32]),
     ("dn_cuda_draw", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("dn_cuda_draw_host", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("dn_cuda_finish", c_int, [c_void_p, POINTER(c_uint64)]),
@@ -326,6 +327,7 @@ _SIGS = [
     ("dn_cuda_event_query", c_int, [c_void_p]),
     ("dn_cuda_kernel_names", c_char_p, []),
     ("dn_cuda_launch_count", c_uint64, []),
+    ("dn_cuda_alloc_count", c_uint64, []),
 ]
 
 _lib = None

@@ -18,7 +18,6 @@
  * lighting of a voxel does not depend on which lane, warp or launch computes it.
  */
 #include "dn_internal.cuh"
-#include "dn_light.cuh"
 #include "dn_light_stream.cuh"
 #include "dn_light_packet.cuh"
 #include <string.h>
@@ -217,6 +216,7 @@ extern "C" int dn_cuda_batch_create(DNgpuBatch** out)
     if (!rc) rc = dalloc(&b->bst, 1);
     if (!rc) rc = dalloc(&b->lsave, 8);
     if (!rc) {
+        COUNT_ALLOC();
         e = cudaMallocHost((void**)&b->hbst, sizeof(DevState));
         if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_NOMEM, "pinned: %s", cudaGetErrorString(e));
     }
@@ -467,6 +467,7 @@ extern "C" int dn_cuda_batch_frame(DNgpuBatch* b, const dn_batch_item* items, ui
         b->htab = nullptr;
         dfree(b->dtab);
         const size_t nc = f.t.size + f.t.size / 2;
+        COUNT_ALLOC();
         CK(cudaMallocHost((void**)&b->htab, nc));
         int rc = dalloc(&b->dtab, nc);
         if (rc) { b->tabCap = 0; return rc; }
@@ -592,6 +593,7 @@ extern "C" int dn_cuda_batch_finish(DNgpuBatch* b)
                 b->dstsCap = 0;
                 int rc;
                 if ((rc = dalloc(&b->dsts, n)) || (rc = dalloc(&b->dgather, (size_t)n * 4))) return rc;
+                COUNT_ALLOC();
                 CK(cudaMallocHost((void**)&b->hgather, (size_t)n * 16));
                 b->dstsCap = n;
             }
@@ -680,6 +682,7 @@ extern "C" int dn_cuda_batch_autotune(DNgpuBatch* b, dn_batch_tuning* chosen)
     size_t flagBytes = 0;
     for (const auto& mg : b->lastLightGens) flagBytes += 3 * mg.first->ntiles;
     unsigned char* saved = nullptr;
+    COUNT_ALLOC();
     CK(cudaMalloc((void**)&saved, flagBytes ? flagBytes : 1));
     {
         size_t o = 0;

@@ -9,10 +9,9 @@
  *   pool    vox[i] (uint2: normal word, linear albedo word), diff[i] / spec[i] (float4, FP32)
  *   frame   reqs[] ((tile << 4) | group), lightOut[] (scratch: new lighting per request lane)
  * Kernels per frame: k_draw (primary rays), k_sync_stage + k_compact (DN_sync_gpu),
- * k_light + k_commit (DN_update_lighting).
+ * k_light_packet (or k_light_stream) + k_commit (DN_update_lighting).
  */
 #include "dn_internal.cuh"
-#include "dn_light.cuh"
 #include "dn_light_stream.cuh"
 #include "dn_light_packet.cuh"
 #include <stdio.h>
@@ -62,6 +61,7 @@ extern "C" const char* dn_cuda_error_string(int code)
 int g_device = -1;
 int g_numSMs = 0;
 unsigned long long g_launches = 0;
+unsigned long long g_allocs = 0;
 static unsigned long long g_generation = 0;
 
 // a process-wide unique generation: graphs keyed on (volume, generation) never match a volume that was
@@ -69,16 +69,19 @@ static unsigned long long g_generation = 0;
 void dn_new_generation(DNgpuVolume* g) { g->gen = __atomic_add_fetch(&g_generation, 1ull, __ATOMIC_RELAXED); }
 
 extern "C" uint64_t dn_cuda_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+extern "C" uint64_t dn_cuda_alloc_count(void) { return __atomic_load_n(&g_allocs, __ATOMIC_RELAXED); }
 
-// lighting kernel selection and stream batch threshold (DN_LIGHT_KERNEL=0 lockstep, 1 per-lane ray streams,
-// 2 warp packets of ray fans; DN_STREAM_BATCH lanes, 1..32), read once at init
+// lighting kernel selection and stream batch threshold (DN_LIGHT_KERNEL=1 per-lane ray streams, 2 warp packets
+// of ray fans; DN_STREAM_BATCH lanes, 1..32), read once at init
 int g_lightKernel = 2;
 uint32_t g_streamBatch = 24;
 uint32_t g_packetBatch = 12;   // lanes with an ended segment before the packet kernel shades (measured best)
 
+static void noalloc_forget(void);
+
 extern "C" int dn_cuda_init(int device)
 {
-    if (const char* e = getenv("DN_LIGHT_KERNEL")) g_lightKernel = atoi(e);
+    if (const char* e = getenv("DN_LIGHT_KERNEL")) g_lightKernel = atoi(e) == 1 ? 1 : 2;
     if (const char* e = getenv("DN_STREAM_BATCH")) {
         int b = atoi(e);
         g_streamBatch = (uint32_t)(b < 1 ? 1 : (b > 32 ? 32 : b));
@@ -99,10 +102,11 @@ extern "C" int dn_cuda_init(int device)
     CK(cudaFree(0));
     CK(cudaDeviceGetAttribute(&g_numSMs, cudaDevAttrMultiProcessorCount, device));
     g_device = device;
+    noalloc_forget();
     return DN_CUDA_OK;
 }
 
-extern "C" void dn_cuda_shutdown(void) { g_device = -1; }
+extern "C" void dn_cuda_shutdown(void) { g_device = -1; noalloc_forget(); }
 
 
 static int alloc_tiles(DNgpuVolume* g)
@@ -194,6 +198,7 @@ extern "C" int dn_cuda_map_create(uint32_t sx, uint32_t sy, uint32_t sz, uint32_
     if (!rc) rc = dalloc(&g->dtab, 1);
     if (!rc) rc = reserve_requests(g, 1024);
     if (!rc) {
+        COUNT_ALLOC();
         e = cudaMallocHost((void**)&g->hst, sizeof(DevState));
         if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_NOMEM, "pinned: %s", cudaGetErrorString(e));
     }
@@ -295,6 +300,7 @@ extern "C" int dn_cuda_map_evict(DNgpuVolume* g)
     size_t total = 0;
     for (int i = 0; i < k; i++) total += align16(a[i].bytes);
     unsigned char* h = nullptr;
+    COUNT_ALLOC();
     CK(cudaMallocHost((void**)&h, total ? total : 1));
     size_t o = 0;
     for (int i = 0; i < k; i++) {
@@ -322,6 +328,7 @@ extern "C" int dn_cuda_map_restore(DNgpuVolume* g)
     const int k = persistent_arrays(g, a);
     int rc = DN_CUDA_OK;
     for (int i = 0; i < k && !rc; i++) {
+        COUNT_ALLOC();
         cudaError_t e = cudaMalloc(a[i].ptr, a[i].bytes ? a[i].bytes : 1);
         if (e != cudaSuccess) { *a[i].ptr = nullptr; rc = dn_set_err(DN_CUDA_ERR_NOMEM, "restore: %s", cudaGetErrorString(e)); }
     }
@@ -378,77 +385,6 @@ __global__ void __launch_bounds__(256) k_draw(const __grid_constant__ DrawArgs a
 
 // -------------------------------------------------------------- lighting
 
-struct LightArgs {
-    DevMap m;
-    const uint32_t* reqs;
-    DevState* st;
-    const uint32_t* nsamples;
-    float4* out;                // 2 float4 per request lane: diffuse, specular
-    dn_light_params p;
-    Material mats[256];
-};
-
-__global__ void __launch_bounds__(128) k_light(const __grid_constant__ LightArgs a)
-{
-    __shared__ Material smat[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) smat[i] = a.mats[i];
-    __syncthreads();
-    const uint32_t lane = threadIdx.x & 31u;
-    LightCtx L;
-    L.rc.m = &a.m; L.rc.mats = smat;
-    L.rc.sunStrength = mk(a.p.sunStrength[0], a.p.sunStrength[1], a.p.sunStrength[2]);
-    L.rc.emissive = a.p.emissiveStrength;
-    L.rc.refraction = false;   // voxelLighting.comp:209
-    L.rc.orgRayPos = mk(0.0f, 0.0f, 0.0f);
-    L.rc.c = Counters{0, 0, 0, 0, 0};
-    L.p = &a.p;
-    L.sunDir = mk(a.p.sunDir[0], a.p.sunDir[1], a.p.sunDir[2]);
-    L.ambient = mk(a.p.ambient[0], a.p.ambient[1], a.p.ambient[2]);
-    L.camPos = mk(a.p.camPos[0], a.p.camPos[1], a.p.camPos[2]);
-    L.skyBot = mk(a.p.skyBot[0], a.p.skyBot[1], a.p.skyBot[2]);
-    L.skyTop = mk(a.p.skyTop[0], a.p.skyTop[1], a.p.skyTop[2]);
-    L.rngSin = a.p.rngMode == 1u;
-    L.sample = 0;
-    uint32_t lit = 0;
-    const uint32_t nreq = *(volatile uint32_t*)&a.st->w[ST_REQ];
-    while (true) {
-        uint32_t r = 0;
-        if (lane == 0) r = atomicAdd(&a.st->w[ST_WORK], 1u);
-        r = __shfl_sync(0xFFFFFFFFu, r, 0);
-        if (r >= nreq) break;
-        const uint32_t word = a.reqs[r];
-        const uint32_t tile = word >> 4, group = word & 15u;
-        const uint32_t tw = __ldg(&a.m.tword[tile]);
-        // every lane of the warp takes part (the phases use warp votes); lanes without a voxel idle
-        bool active = false;
-        i3 cp{0, 0, 0}, mp{0, 0, 0};
-        uint32_t samples = 0;
-        Voxel tv;
-        tv.normal = mk(0.0f, 1.0f, 0.0f); tv.material = 0; tv.albedo = mk(0.0f, 0.0f, 0.0f);
-        tv.spec = tv.albedo; tv.diff = tv.albedo;
-        if ((tw >> 30) == 2u) {
-            const uint32_t slot = tw & SLOT_MASK;
-            const ChunkRec* rc = &a.m.rec[slot];
-            const uint32_t vn = group * 32u + lane;
-            uint32_t li;
-            if (vn < __ldg(&rc->nvox) && select_voxel(rc, vn, cp, li)) {
-                mp = i3{__ldg(&rc->pos[0]), __ldg(&rc->pos[1]), __ldg(&rc->pos[2])};
-                decompress(a.m, __ldg(&rc->voxBase) + vn, tv);
-                samples = __ldg(&a.nsamples[slot]);
-                active = true;
-            }
-        }
-        float4 od = make_float4(0.0f, 0.0f, 0.0f, 0.0f), os = od;
-        light_voxel(L, active, mp, cp, tv, samples, od, os);
-        if (!active) { od = make_float4(0.0f, 0.0f, 0.0f, 0.0f); os = od; }
-        lit += active ? 1u : 0u;
-        a.out[((uint64_t)r * 32u + lane) * 2u] = od;
-        a.out[((uint64_t)r * 32u + lane) * 2u + 1u] = os;
-    }
-    flush_counters(a.st->lstats, L.rc.c, 0, lit);
-}
-
-
 // The lighting launch as persistent per-lane ray streams (dn_light_stream.cuh).
 __global__ void __launch_bounds__(128, DN_STREAM_MIN_BLOCKS) k_light_stream(const __grid_constant__ StreamArgs a)
 {
@@ -490,7 +426,7 @@ static int launch_light(DNgpuVolume* g, StreamArgs& a)
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_packet, 128, 0));
         if (perSM < 1) perSM = 1;
         a.batch = g_packetBatch;
-        static thread_local MaterialTable table;
+        MaterialTable table;            // on the stack: a launch argument, copied at the launch
         memcpy(table.m, a.mats, sizeof(table.m));
         a.gtab = g->dtab;
         COUNT_LAUNCH();
@@ -509,10 +445,10 @@ static int launch_light(DNgpuVolume* g, StreamArgs& a)
 }
 
 // D1/D2: commit the new lighting after the whole launch, then count the sample
-__global__ void k_commit(DevMap m, const uint32_t* reqs, const DevState* st, const float4* out,
+__global__ void k_commit(DevMap m, const uint32_t* reqs, const uint32_t* nreqPtr, const float4* out,
                          float4* diff, float4* spec, uint32_t* nsamples)
 {
-    const uint32_t nreq = st->w[ST_REQ];
+    const uint32_t nreq = *nreqPtr;
     const uint64_t total = (uint64_t)nreq * 32u;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x)
         commit_lane(m, reqs, out, i, (uint32_t)(i >> 5), (uint32_t)(i & 31u), diff, spec, nsamples);
@@ -528,7 +464,7 @@ __global__ void k_sync_stage(const dn_tile_op* ops, uint32_t nops, const dn_chun
 {
     for (uint32_t o = blockIdx.x; o < nops; o += gridDim.x) {
         const dn_tile_op op = ops[o];
-        if (op.tile >= ntiles) { if (threadIdx.x == 0) atomicOr(&st->w[ST_ERR], 1u); continue; }
+        if (op.tile >= ntiles) { if (threadIdx.x == 0) atomicOr(&st->w[ST_ERR], ERRF_TILE); continue; }
         const bool staged = (op.flags & DN_PEND_STAGED) != 0;
         const dn_chunk_record* srcp = staged ? &recs[op.recordIndex] : nullptr;
         const bool bad = staged && (op.slot >= slotCap || srcp->nvox > 512u || (uint64_t)srcp->voxBase + srcp->nvox > voxCap);
@@ -536,7 +472,7 @@ __global__ void k_sync_stage(const dn_tile_op* ops, uint32_t nops, const dn_chun
             // a record that does not fit is not published: the tile stays unloaded
             tpend[op.tile] = bad ? (op.flags & ~DN_PEND_STAGED) : op.flags;
             tpendSlot[op.tile] = bad ? DN_SLOT_NONE : op.slot;
-            if (bad) atomicOr(&st->w[ST_ERR], 2u);
+            if (bad) atomicOr(&st->w[ST_ERR], ERRF_RECORD);
         }
         if (!staged || bad) continue;
         const dn_chunk_record& src = *srcp;
@@ -583,6 +519,7 @@ int dn_stage_ops(DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops, const dn_
             if (g->hstage) cudaFreeHost(g->hstage);
             g->hstage = nullptr;
             size_t nc = total + total / 2 + 4096;
+            COUNT_ALLOC();
             CK(cudaMallocHost((void**)&g->hstage, nc));
             g->hstageCap = nc;
         }
@@ -659,34 +596,19 @@ extern "C" int dn_cuda_light(DNgpuVolume* g, const dn_light_params* p, const dn_
     if (p->K < 1 || p->K > 64) return dn_set_err(DN_CUDA_ERR_ARG, "K = %u", p->K);
     CK(cudaSetDevice(g->device));
     CK(cudaMemsetAsync(&g->st->w[ST_WORK], 0, 4, g->stream));
-    if (g_lightKernel == 0) {
-        // one voxel per lane in lockstep phases (kept for comparison)
-        static thread_local LightArgs* a = nullptr;
-        if (!a) a = new LightArgs();
-        a->m = dev_map(g);
-        a->reqs = g->reqs; a->st = g->st; a->nsamples = g->nsamples; a->out = g->lightOut;
-        a->p = *p;
-        memcpy(a->mats, materials, sizeof(a->mats));
-        int perSM = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light, 128, 0));
-        if (perSM < 1) perSM = 1;
-        COUNT_LAUNCH();
-        k_light<<<g->numSMs * perSM, 128, 0, g->stream>>>(*a);
-        CK(cudaGetLastError());
-    } else {
-        static thread_local StreamArgs* a = nullptr;
-        if (!a) a = new StreamArgs();
-        a->m = dev_map(g);
-        a->reqs = g->reqs; a->workCounter = &g->st->w[ST_WORK]; a->nreqPtr = &g->st->w[ST_REQ];
-        a->nsamples = g->nsamples; a->out = g->lightOut; a->stats = g->st->lstats;
-        a->batch = g_streamBatch;
-        a->p = *p;
-        memcpy(a->mats, materials, sizeof(a->mats));
-        int rc = launch_light(g, *a);
-        if (rc) return rc;
-    }
+    static thread_local StreamArgs* a = nullptr;
+    if (!a) a = new StreamArgs();
+    a->m = dev_map(g);
+    a->reqs = g->reqs; a->workCounter = &g->st->w[ST_WORK]; a->nreqPtr = &g->st->w[ST_REQ];
+    a->nsamples = g->nsamples; a->out = g->lightOut; a->stats = g->st->lstats;
+    a->batch = g_streamBatch;
+    a->p = *p;
+    memcpy(a->mats, materials, sizeof(a->mats));
+    int rc = launch_light(g, *a);
+    if (rc) return rc;
     COUNT_LAUNCH();
-    k_commit<<<g->numSMs * 4, 256, 0, g->stream>>>(dev_map(g), g->reqs, g->st, g->lightOut, g->diff, g->spec, g->nsamples);
+    k_commit<<<g->numSMs * 4, 256, 0, g->stream>>>(dev_map(g), g->reqs, &g->st->w[ST_REQ], g->lightOut, g->diff, g->spec,
+                                                  g->nsamples);
     CK(cudaGetLastError());
     return DN_CUDA_OK;
 }
@@ -702,18 +624,32 @@ extern "C" int dn_cuda_light(DNgpuVolume* g, const dn_light_params* p, const dn_
 // library's device image (every GPU that loads the library holds it until the process exits), so the
 // call itself allocates nothing on the device or the host.
 //
-// Limit: DN_NOALLOC_MAX_REQUESTS request groups (32 voxels each) per call; larger request lists are
-// rejected with DN_CUDA_ERR_CAPACITY and a message naming both numbers.
+// Limit: DN_NOALLOC_MAX_REQUESTS request groups (32 voxels each) per call.  The request count exists
+// only on the device (the sync built it there), so the limit is checked there: k_noalloc_guard copies
+// the count into ST_LIMITED, or 0 with the ERRF_NOALLOC_CAPACITY flag when it exceeds the limit; the
+// lighting and commit kernels of the call light ST_LIMITED groups, so an oversized list is lit not at
+// all and changes nothing, and the next dn_cuda_finish reports DN_CUDA_ERR_CAPACITY.  The host never
+// waits for the device in this call.
 // The array's device address is looked up once per device, on that device's first call (with the
-// device current); that first call should come before any stream capture.  Every call shares the
-// array and it keeps the previous call's contents: nothing in it needs to start at zero, because each
-// call writes every slot it later reads.  Calls that overlap on the GPU (two volumes lit concurrently
-// on different streams) race on the array.
+// device current); that first call should come before any stream capture.  dn_cuda_init and
+// dn_cuda_shutdown forget the looked-up addresses (a device reset invalidates them).  Every call
+// shares the array and it keeps the previous call's contents: nothing in it needs to start at zero,
+// because each call writes every slot it later reads.  Calls that overlap on the GPU (two volumes lit
+// concurrently on different streams) race on the array.
 #define DN_NOALLOC_MAX_REQUESTS 8192u   // 8192 groups x 32 lanes x 2 float4 = 8 MiB
 static __device__ __align__(256) float4 g_noallocScratch[DN_NOALLOC_MAX_REQUESTS * 32u * 2u];
+static_assert(sizeof(g_noallocScratch) == (size_t)DN_NOALLOC_MAX_REQUESTS * 32u * 2u * sizeof(float4),
+              "one diffuse and one specular float4 per lane of every request group the limit admits");
 
 static std::mutex g_noallocMutex;
 static float4* g_noallocAddr[64];      // device address of g_noallocScratch, per device ordinal
+static uint32_t g_noallocLimit = DN_NOALLOC_MAX_REQUESTS;
+
+static void noalloc_forget(void)
+{
+    std::lock_guard<std::mutex> lock(g_noallocMutex);
+    memset(g_noallocAddr, 0, sizeof(g_noallocAddr));
+}
 
 static int noalloc_scratch(int device, float4** out)
 {
@@ -730,6 +666,24 @@ static int noalloc_scratch(int device, float4** out)
     return DN_CUDA_OK;
 }
 
+// the call's request count, or 0 and the capacity flag when the list exceeds the limit; the work counter
+// of the lighting launch starts at zero
+__global__ void k_noalloc_guard(DevState* st, uint32_t limit)
+{
+    const uint32_t n = st->w[ST_REQ];
+    st->w[ST_LIMITED] = n <= limit ? n : 0u;
+    if (n > limit) atomicOr(&st->w[ST_ERR], ERRF_NOALLOC_CAPACITY);
+    st->w[ST_WORK] = 0;
+}
+
+extern "C" uint32_t dn_cuda_light_noalloc_set_limit(uint32_t groups)
+{
+    const uint32_t old = __atomic_load_n(&g_noallocLimit, __ATOMIC_RELAXED);
+    const uint32_t v = (groups == 0u || groups > DN_NOALLOC_MAX_REQUESTS) ? DN_NOALLOC_MAX_REQUESTS : groups;
+    __atomic_store_n(&g_noallocLimit, v, __ATOMIC_RELAXED);
+    return old;
+}
+
 extern "C" int dn_cuda_light_noalloc(DNgpuVolume* g, const dn_light_params* p, const dn_material* materials)
 {
     if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
@@ -739,19 +693,12 @@ extern "C" int dn_cuda_light_noalloc(DNgpuVolume* g, const dn_light_params* p, c
     float4* scratch = nullptr;
     int rc = noalloc_scratch(g->device, &scratch);
     if (rc) return rc;
-    // the request count exists only on the device: read it into the volume's pinned state block
-    CK(cudaMemcpyAsync(&g->hst->w[ST_REQ], &g->st->w[ST_REQ], sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
-    CK(cudaStreamSynchronize(g->stream));
-    const uint32_t nreq = g->hst->w[ST_REQ];
-    if (nreq > DN_NOALLOC_MAX_REQUESTS)
-        return dn_set_err(DN_CUDA_ERR_CAPACITY,
-                       "dn_cuda_light_noalloc: %u lighting request groups exceed the fixed scratch of %u groups "
-                       "(%u voxels); use dn_cuda_light for this map", nreq, DN_NOALLOC_MAX_REQUESTS,
-                       DN_NOALLOC_MAX_REQUESTS * 32u);
-    CK(cudaMemsetAsync(&g->st->w[ST_WORK], 0, 4, g->stream));
+    COUNT_LAUNCH();
+    k_noalloc_guard<<<1, 1, 0, g->stream>>>(g->st, __atomic_load_n(&g_noallocLimit, __ATOMIC_RELAXED));
+    CK(cudaGetLastError());
     StreamArgs a;                       // launch arguments on the stack: no host allocation either
     a.m = dev_map(g);
-    a.reqs = g->reqs; a.workCounter = &g->st->w[ST_WORK]; a.nreqPtr = &g->st->w[ST_REQ];
+    a.reqs = g->reqs; a.workCounter = &g->st->w[ST_WORK]; a.nreqPtr = &g->st->w[ST_LIMITED];
     a.nsamples = g->nsamples; a.out = scratch; a.stats = g->st->lstats;
     a.batch = g_streamBatch;
     a.p = *p;
@@ -759,7 +706,8 @@ extern "C" int dn_cuda_light_noalloc(DNgpuVolume* g, const dn_light_params* p, c
     rc = launch_light(g, a);
     if (rc) return rc;
     COUNT_LAUNCH();
-    k_commit<<<g->numSMs * 4, 256, 0, g->stream>>>(dev_map(g), g->reqs, g->st, scratch, g->diff, g->spec, g->nsamples);
+    k_commit<<<g->numSMs * 4, 256, 0, g->stream>>>(dev_map(g), g->reqs, &g->st->w[ST_LIMITED], scratch, g->diff, g->spec,
+                                                  g->nsamples);
     CK(cudaGetLastError());
     return DN_CUDA_OK;
 }
@@ -862,6 +810,12 @@ extern "C" int dn_cuda_finish(DNgpuVolume* g, uint64_t* numRequests)
     if (g->hst->w[ST_ERR]) {
         uint32_t e = g->hst->w[ST_ERR];
         cudaMemsetAsync(&g->st->w[ST_ERR], 0, 4, g->stream);
+        if (e == ERRF_NOALLOC_CAPACITY)
+            return dn_set_err(DN_CUDA_ERR_CAPACITY,
+                              "dn_cuda_light_noalloc: the request list exceeded the fixed scratch of %u groups (%u voxels); "
+                              "that lighting update was skipped; use dn_cuda_light for this map",
+                              __atomic_load_n(&g_noallocLimit, __ATOMIC_RELAXED),
+                              __atomic_load_n(&g_noallocLimit, __ATOMIC_RELAXED) * 32u);
         return dn_set_err(DN_CUDA_ERR_KERNEL, "kernel error flags 0x%x", e);
     }
     return DN_CUDA_OK;
@@ -991,9 +945,9 @@ extern "C" int dn_cuda_export_lighting(DNgpuVolume* g, uint32_t* index, float* d
 
 // ---------------------------------------------------------------- helpers
 
-extern "C" int dn_cuda_malloc(void** p, size_t bytes) { CK(cudaMalloc(p, bytes ? bytes : 1)); return DN_CUDA_OK; }
+extern "C" int dn_cuda_malloc(void** p, size_t bytes) { COUNT_ALLOC(); CK(cudaMalloc(p, bytes ? bytes : 1)); return DN_CUDA_OK; }
 extern "C" int dn_cuda_free(void* p) { if (p) CK(cudaFree(p)); return DN_CUDA_OK; }
-extern "C" int dn_cuda_malloc_host(void** p, size_t bytes) { CK(cudaMallocHost(p, bytes ? bytes : 1)); return DN_CUDA_OK; }
+extern "C" int dn_cuda_malloc_host(void** p, size_t bytes) { COUNT_ALLOC(); CK(cudaMallocHost(p, bytes ? bytes : 1)); return DN_CUDA_OK; }
 extern "C" int dn_cuda_free_host(void* p) { if (p) CK(cudaFreeHost(p)); return DN_CUDA_OK; }
 extern "C" int dn_cuda_memcpy_d2h(void* dst, const void* src, size_t bytes) { CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost)); return DN_CUDA_OK; }
 // cudaMemcpy from pageable memory may return before the DMA has landed; the legacy-stream synchronise makes
@@ -1034,6 +988,7 @@ extern "C" int dn_cuda_flush_l2(void* stream, size_t bytes)
     if (n > cap) {
         if (buf) cudaFree(buf);
         buf = nullptr;
+        COUNT_ALLOC();
         CK(cudaMalloc((void**)&buf, n * 16));
         cap = n;
     }
@@ -1045,7 +1000,7 @@ extern "C" int dn_cuda_flush_l2(void* stream, size_t bytes)
 
 extern "C" const char* dn_cuda_kernel_names(void)
 {
-    return "k_draw;k_light;k_light_stream;k_light_packet;k_light_tables;k_commit;k_sync_stage;k_compact;k_clamp_requests;k_flush;"
+    return "k_draw;k_light_stream;k_light_packet;k_light_tables;k_commit;k_sync_stage;k_compact;k_clamp_requests;k_flush;"
            "k_draw_batch;k_compact_batch;k_batch_reset;k_batch_prep;k_light_stream_batch;k_light_packet_batch;k_commit_batch;k_batch_gather;"
            "k_shape_count;k_shape_write";
 }

@@ -24,11 +24,15 @@ int dn_set_err(int code, const char* fmt, ...);
 
 // ------------------------------------------------------------------ state
 
-enum { ST_REQ = 0, ST_WORK = 1, ST_ERR = 2 };
+// ST_LIMITED: the request count a dn_cuda_light_noalloc launch lights (its own count, or 0 when the
+// list exceeds the fixed scratch; k_noalloc_guard writes it)
+enum { ST_REQ = 0, ST_WORK = 1, ST_ERR = 2, ST_LIMITED = 3 };
+// error flag bits of ST_ERR (reported by dn_cuda_finish / dn_cuda_batch_finish)
+enum : uint32_t { ERRF_TILE = 1u, ERRF_RECORD = 2u, ERRF_REQUESTS = 4u, ERRF_NOALLOC_CAPACITY = 0x100u };
 enum { S_RAYS = 0, S_PRIMARY, S_OUTER, S_ENTERED, S_INNER, S_HITS, S_LIT, S_COUNT };
 
 struct DevState {
-    uint32_t w[4];                      // nreq, work counter, error flags, pad
+    uint32_t w[4];                      // nreq, work counter, error flags, noalloc request count
     unsigned long long stats[8];        // draw kernels
     unsigned long long lstats[8];       // lighting kernels
 };
@@ -67,15 +71,18 @@ struct DNgpuVolume {
 extern int g_device;
 extern int g_numSMs;
 extern unsigned long long g_launches;   // kernels launched by this library (all threads)
-extern int g_lightKernel;               // 0 lockstep, 1 per-lane ray streams, 2 warp packets (default)
+extern int g_lightKernel;               // 1 per-lane ray streams, 2 warp packets (default)
 extern uint32_t g_streamBatch;          // lanes that wait before per-segment work runs (1..32), ray streams
 extern uint32_t g_packetBatch;          // the same threshold for the packet kernel's ray pools
 #define COUNT_LAUNCH() __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED)
+extern unsigned long long g_allocs;     // device and pinned allocations made by this library (all threads)
+#define COUNT_ALLOC() __atomic_fetch_add(&g_allocs, 1ull, __ATOMIC_RELAXED)
 
 template <class T> static int dalloc(T** p, size_t count)
 {
     *p = nullptr;
     if (count == 0) count = 1;
+    COUNT_ALLOC();
     CK(cudaMalloc((void**)p, count * sizeof(T)));
     return DN_CUDA_OK;
 }
@@ -420,7 +427,7 @@ __device__ __forceinline__ void compact_tiles(const CompactArgs& a, uint64_t bas
         const uint32_t first = wbase + incl - groups;
         for (uint32_t gi = 0; gi < groups; gi++) {
             if ((uint64_t)first + gi < a.reqCap) a.reqs[first + gi] = ((uint32_t)t << 4) | gi;
-            else atomicOr(&a.st->w[ST_ERR], 4u);
+            else atomicOr(&a.st->w[ST_ERR], ERRF_REQUESTS);
         }
     }
 }

@@ -15,7 +15,7 @@
  * reference's lighting main does (running average, clamps, voxelLighting.comp:238-288).
  *
  * Results, traversal side effects (requested / touched / visible flags) and counters are those of the
- * one-voxel-per-lane forms (dn_light.cuh, dn_light_stream.cuh): the same rays are traced with the same
+ * one-voxel-per-lane form (dn_light_stream.cuh): the same rays are traced with the same
  * operations; only the assignment of rays to lanes differs.
  */
 #pragma once

@@ -8,7 +8,7 @@
  *   sample), then numDiffuse diffuse paths (each up to diffuseBounceLimit
  *   segments), then the running average and the write-out.
  * All lanes share one loop whose body is one traversal step of each lane's
- * current ray segment (the flattened two-level DDA of dn_light.cuh), so lanes
+ * current ray segment (seg_step: the two-level DDA flattened into one loop), so lanes
  * on different rays, different jobs or different voxels still execute
  * together.  When a segment ends, the lane waits; the per-segment work
  * (shading the finished segment, choosing and setting up the next one,
@@ -21,7 +21,7 @@
  * 32 voxels.
  */
 #pragma once
-#include "dn_light.cuh"
+#include "dn_device.cuh"
 
 namespace dn {
 

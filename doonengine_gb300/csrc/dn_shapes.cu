@@ -225,6 +225,7 @@ template <class T> int grow_device(T*& p, size_t& cap, size_t need)
     p = nullptr;
     cap = 0;
     const size_t n = need < 1024 ? 1024 : need + need / 2;
+    COUNT_ALLOC();
     CK(cudaMalloc((void**)&p, n * sizeof(T)));
     cap = n;
     return DN_CUDA_OK;
@@ -237,6 +238,7 @@ template <class T> int grow_pinned(T*& p, size_t& cap, size_t need)
     p = nullptr;
     cap = 0;
     const size_t n = need < 1024 ? 1024 : need + need / 2;
+    COUNT_ALLOC();
     CK(cudaMallocHost((void**)&p, n * sizeof(T)));
     cap = n;
     return DN_CUDA_OK;

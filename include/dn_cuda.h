@@ -138,11 +138,19 @@ int dn_cuda_light(struct DNgpuVolume* g, const dn_light_params* p, const dn_mate
  * loop under a fixed device-memory budget, or a host engine whose own allocator owns all device memory --
  * the per-request scratch that dn_cuda_light keeps in the volume (grown with cudaMalloc by dn_cuda_sync)
  * is replaced by a fixed 8 MiB array in the library's device image, held by every GPU that loads the
- * library until the process exits.  Same inputs and outputs as dn_cuda_light and the same results.
- * Limit: 8192 request groups (262144 voxels) per call; more returns DN_CUDA_ERR_CAPACITY with a message.
+ * library until the process exits.  Same inputs, outputs and kernels as dn_cuda_light.
+ * Limit: 8192 request groups (262144 voxels) per call, or the lower limit set below.  The request count
+ * is known only on the device, so the check runs there and the call never waits for the GPU: a list
+ * above the limit is not lit at all (the volume is left unchanged) and the next dn_cuda_finish (DN_finish)
+ * returns DN_CUDA_ERR_CAPACITY with a message naming the limit.
  * The first call on a device looks up the array's device address (with that device current); make that
- * first call before any stream capture.  Calls share the array: calls that overlap on the GPU race. */
+ * first call before any stream capture.  dn_cuda_init and dn_cuda_shutdown drop the looked-up addresses,
+ * so after a device reset call dn_cuda_init again before the next call.  Calls share the array: calls
+ * that overlap on the GPU race. */
 int dn_cuda_light_noalloc(struct DNgpuVolume* g, const dn_light_params* p, const dn_material* materials);
+/* Lowers the per-call limit of dn_cuda_light_noalloc to 'groups' request groups (0 or more than 8192:
+ * back to 8192); returns the previous limit.  Process-wide. */
+uint32_t dn_cuda_light_noalloc_set_limit(uint32_t groups);
 
 /* --- draw: replaces glDispatchCompute(w/16, h/16) of DN_draw (voxel.c:879); outputs are device pointers --- */
 int dn_cuda_draw(struct DNgpuVolume* g, const dn_draw_params* p, const dn_material* materials,
@@ -301,6 +309,8 @@ int dn_cuda_device_sync(void);
 int dn_cuda_flush_l2(void* stream, size_t bytes);
 /* number of kernels this library has launched since load (all volumes) */
 uint64_t dn_cuda_launch_count(void);
+/* number of device and pinned-host allocations this library has made since load (all threads) */
+uint64_t dn_cuda_alloc_count(void);
 /* names of the kernels this library launches, ';'-separated */
 const char* dn_cuda_kernel_names(void);
 
