@@ -250,6 +250,9 @@ def run_ours(args):
         "ms_per_step": dev_ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded heightfield + boxes/spheres; the reference publishes no scenes)",
         "config": dict(workload_desc(cfg, vol, nonempty, args.config), parallelism="replicas: one map per GPU, no collective",
+                       frames_timed="frames %d..%d of the accumulation (frame 0 starts with no chunk loaded; chunks "
+                                    "load one sync after a ray requests them, so the lighting work grows over the "
+                                    "first frames)" % (args.warmup, args.warmup + K - 1),
                        **({"residency": "DN_RESIDENCY_LRU (the reference's voxel-buffer nodes; each sync reads the "
                                         "rays' flags back and walks the tiles on the host)"}
                           if args.residency == "lru" else {})),
@@ -261,6 +264,8 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": "k_light_packet+k_commit (DN_update_lighting)", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": traffic, "algorithmic_bytes_per_launch": per_launch_bytes,
+                     "traffic_source": "scaled, not measured in this run: DRAM bytes per lit voxel of one ncu capture "
+                                       "(profiles/k_light_traffic.json) x this run's lit voxels per launch",
                      "launch_ms": per_launch_s * 1e3},
         "clocks": clk,
         "light_counters_per_step": {k: v / K for k, v in st_light.items()},
@@ -288,10 +293,43 @@ def run_ours(args):
 
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline_sample(vol, view, proj, W, H, args.cpu_seconds)
+    result["rays_by_kind_per_step"] = {"primary": prim_total / K, "lighting": (rays_total - prim_total) / K}
     vol.close()
     img.close()
+
+    # the headline metric's other two parts on the same box: batched vs plain on the batched workload,
+    # and serving latency / throughput on the serving workload (one GPU; replicas skip them)
+    if world == 1 and not args.no_batched:
+        t1 = time.perf_counter()
+        result["batched_vs_plain"] = batched_vs_plain(args, lib, rank, pg, local, args.batched_warmup,
+                                                      args.batched_frames)
+        log("batched vs plain: %.1f s" % (time.perf_counter() - t1))
+    if world == 1 and not args.no_serving:
+        t1 = time.perf_counter()
+        rates = [float(x) for x in args.serving_rates.split(",")]
+        sv = serving_sweep(args, lib, rank, world, 256, rates, args.serving_seconds, args.budget_gb)
+        result["serving"] = serving_summary(sv)
+        log("serving: %.1f s" % (time.perf_counter() - t1))
+        if args.pressure_budget_gb > 0:
+            t1 = time.perf_counter()
+            rates = [float(x) for x in args.pressure_rates.split(",")]
+            sv = serving_sweep(args, lib, rank, world, 256, rates, args.serving_seconds, args.pressure_budget_gb)
+            result["serving_under_eviction"] = serving_summary(sv)
+            log("serving under eviction: %.1f s" % (time.perf_counter() - t1))
     if rank == 0:
         print(json.dumps(result), flush=True)
+
+
+def serving_summary(sv):
+    """The serving line's figures that the headline carries: per offered rate p50 / p99 latency, achieved
+    request rate and rays/s, and the highest achieved rate whose p99 stays within 33 ms."""
+    rows = [{k: r.get(k) for k in ("offered_rps", "achieved_rps", "p50_ms", "p99_ms", "rays_per_s", "completed",
+                                   "drained", "evictions", "restores")} for r in sv["sweep"]]
+    return {"workload": sv["config"]["workload"], "device_budget_gb": sv["config"]["device_budget_gb"],
+            "offered_rps": [r["offered_rps"] for r in rows], "p50_ms": [r["p50_ms"] for r in rows],
+            "p99_ms": [r["p99_ms"] for r in rows], "max_rps_p99_le_33ms": sv["max_rps_with_p99_le_33ms"],
+            "rays_per_s": sv["value"], "evictions": sv["evictions"], "restores": sv["restores"],
+            "resident_bytes": sv["resident_bytes"], "sweep": rows, "build_s": sv["build_s"]}
 
 
 def cpu_baseline_sample(vol, view, proj, W, H, seconds):
@@ -336,164 +374,163 @@ def cpu_baseline_sample(vol, view, proj, W, H, seconds):
 
 # ------------------------------------------------------------ batched workload
 
-def run_batched(args):
-    """Many maps of uneven size and resolution per step: the plain per-scene form (each map's frame issued
-    and finished before the next map's, as one GL context would) against batched frames (DN_batch_run: one
-    launch per phase over all maps, replayed as a CUDA graph)."""
+def batched_vs_plain(args, lib, rank, pg, local, frames_warm, frames_timed, autotune=True):
+    """The batched workload (64 maps of uneven size and resolution) in both forms on identical map state:
+    two identical sets of maps built from the same seeds; every frame number runs the plain per-scene form
+    on set A (each map's DN_draw, DN_sync_gpu, DN_update_lighting, DN_finish, one map at a time, as one GL
+    context issues them) and the batched form on set B (DN_batch_run over all maps + DN_batch_finish).  Both
+    sets therefore trace exactly the same rays in every frame (their counters are compared).  The first
+    ``frames_warm`` frames cover the streaming ramp (chunks load one sync after a ray requests them); the
+    next ``frames_timed`` are timed, each form by wall clock from issue to its results on the host, with
+    the L2 flushed before each form's frame; the batched frames are also timed on the device."""
     import ctypes
-    rank, world, local, pg = dist_setup()
     import doonengine_gb300 as dn
-    from doonengine_gb300 import configs, _lib
-    lib = dn.load()
-    if lib.dn_cuda_init(local) != 0:
-        raise RuntimeError("dn_cuda_init(%d): %s" % (local, lib.dn_cuda_last_error().decode()))
-    dn.init()
+    from doonengine_gb300 import configs
     specs = configs.batched_specs(args.maps, seed=7 + 1000 * rank)
-    maps = []
+    sets = {"plain": [], "batched": []}
     t0 = time.perf_counter()
     tiles = nonempty = pixels = 0
-    for i, sp in enumerate(specs):
-        vol, cfg = configs.build_volume("small", **sp)
-        vol.s.mapId = i
-        W, H = cfg["res"]
-        img = dn.Image(W, H, on_device=True)
-        v, p = vol.view_proj(H / W)
-        maps.append((vol, img, W, H, v, p))
-        tiles += vol.num_tiles
-        nonempty += vol.nonempty_chunks()
-        pixels += W * H
+    for form in ("plain", "batched"):
+        for i, sp in enumerate(specs):
+            vol, cfg = configs.build_volume("small", **sp)
+            vol.s.mapId = i
+            W, H = cfg["res"]
+            img = dn.Image(W, H, on_device=True)
+            v, p = vol.view_proj(H / W)
+            sets[form].append((vol, img, v, p))
+            if form == "plain":
+                tiles += vol.num_tiles
+                nonempty += vol.nonempty_chunks()
+                pixels += W * H
     build_s = time.perf_counter() - t0
-    log("built %d maps in %.1f s (%d tiles, %d non-empty chunks, %d pixels per step)" % (len(maps), build_s, tiles, nonempty, pixels))
-    frame = [0]
+    log("built 2 x %d maps in %.1f s (%d tiles, %d non-empty chunks, %d pixels per frame per set)"
+        % (len(specs), build_s, tiles, nonempty, pixels))
+    A, B = sets["plain"], sets["batched"]
+    batch = dn.Batch([m[0] for m in B])
+    bstream = batch.stream()
+    tuned = None
 
-    def plain_frame():
-        t = 1.0 + 0.25 * frame[0]
-        for vol, img, W, H, v, p in maps:
+    def plain_frame(t):
+        for vol, img, v, p in A:
             vol.draw(img, v, p)
             vol.sync(dn.DN_READ_WRITE, 1)
             vol.update_lighting(1, 1000, t)
             assert vol.finish(), lib.dn_cuda_last_error().decode()
-        frame[0] += 1
 
-    def batch_items():
-        t = 1.0 + 0.25 * frame[0]
-        return [dn.Batch.item(vol, img, v, p, sync=(dn.DN_READ_WRITE, 1), light=(1, 1000, t))
-                for vol, img, W, H, v, p in maps]
-
-    def plain_rays():
-        tot = {"rays": 0, "litVoxels": 0, "primaryRays": 0}
-        for vol, *_ in maps:
-            st = vol.stats()
-            for k in tot:
-                tot[k] += st[k]
-        return tot
-
-    # plain per-scene form
-    for w in range(args.warmup):
-        t1 = time.perf_counter()
-        plain_frame()
-        log("plain warm-up frame %d: %.2f s" % (w, time.perf_counter() - t1))
-    for vol, *_ in maps:
-        vol.reset_stats()
-    lib.dn_cuda_device_sync()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        plain_frame()
-    plain_s = time.perf_counter() - t0
-    pr = plain_rays()
-    log("plain: %d frames in %.2f s, %.3g rays" % (args.steps, plain_s, pr["rays"]))
-
-    # batched form
-    batch = dn.Batch([m[0] for m in maps])
-    stream = batch.stream()
-    for w in range(args.warmup):
-        t1 = time.perf_counter()
-        batch.run(batch_items())
-        frame[0] += 1
+    def batched_frame(t):
+        batch.run([dn.Batch.item(vol, img, v, p, sync=(dn.DN_READ_WRITE, 1), light=(1, 1000, t)) for vol, img, v, p in B])
         assert batch.finish(), lib.dn_cuda_last_error().decode()
-        log("batched warm-up frame %d: %.2f s" % (w, time.perf_counter() - t1))
-        if w == 0 and not args.no_autotune:
-            t1 = time.perf_counter()
+
+    for f in range(frames_warm):
+        t = 1.0 + 0.25 * f
+        plain_frame(t)
+        batched_frame(t)
+        if f == 0 and autotune:
             tuned = batch.autotune()
-            log("autotuned in %.2f s: %s" % (time.perf_counter() - t1, tuned))
-    K = args.steps
-    evs = []
-    for _ in range(2 * K):
-        e = ctypes.c_void_p()
-        lib.dn_cuda_event_create(e)
-        evs.append(e)
+            log("autotuned: %s" % tuned)
+    for vol, *_ in A:
+        vol.reset_stats()
     batch.reset_stats()
-    launches0 = lib.dn_cuda_launch_count()
+    ev = [ctypes.c_void_p(), ctypes.c_void_p()]
+    for e in ev:
+        lib.dn_cuda_event_create(e)
+    plain_s = batched_s = batched_dev_ms = 0.0
+    launches = 0
     clocks = ClockSampler(local)
     barrier(pg)
-    lib.dn_cuda_device_sync()
     clocks.start()
-    t0 = time.perf_counter()
-    for k in range(K):
-        lib.dn_cuda_flush_l2(stream, L2_FLUSH_BYTES)
-        lib.dn_cuda_event_record(evs[2 * k], stream)
-        batch.run(batch_items())
-        frame[0] += 1
-        lib.dn_cuda_event_record(evs[2 * k + 1], stream)
-    assert batch.finish(), lib.dn_cuda_last_error().decode()
-    lib.dn_cuda_device_sync()
+    for k in range(frames_timed):
+        t = 1.0 + 0.25 * (frames_warm + k)
+        lib.dn_cuda_flush_l2(None, L2_FLUSH_BYTES)
+        lib.dn_cuda_device_sync()
+        t0 = time.perf_counter()
+        plain_frame(t)
+        plain_s += time.perf_counter() - t0
+        lib.dn_cuda_flush_l2(bstream, L2_FLUSH_BYTES)
+        lib.dn_cuda_device_sync()
+        l0 = lib.dn_cuda_launch_count()
+        t0 = time.perf_counter()
+        lib.dn_cuda_event_record(ev[0], bstream)
+        batch.run([dn.Batch.item(vol, img, v, p, sync=(dn.DN_READ_WRITE, 1), light=(1, 1000, t)) for vol, img, v, p in B])
+        lib.dn_cuda_event_record(ev[1], bstream)
+        assert batch.finish(), lib.dn_cuda_last_error().decode()
+        batched_s += time.perf_counter() - t0
+        launches += lib.dn_cuda_launch_count() - l0
+        ms = ctypes.c_float()
+        lib.dn_cuda_event_elapsed_ms(ev[0], ev[1], ms)
+        batched_dev_ms += ms.value
     barrier(pg)
-    wall = time.perf_counter() - t0
     clk = clocks.stop()
-    launches = lib.dn_cuda_launch_count() - launches0 - K
-    ms = ctypes.c_float()
-    dev_ms = 0.0
-    for k in range(K):
-        lib.dn_cuda_event_elapsed_ms(evs[2 * k], evs[2 * k + 1], ms)
-        dev_ms += ms.value
-    bst = batch.stats()
-    # wall clock of batched frames ending on the host, comparable to the plain form
-    batch.reset_stats()
-    t0 = time.perf_counter()
-    for k in range(K):
-        batch.run(batch_items())
-        frame[0] += 1
-        assert batch.finish()
-    bwall_s = time.perf_counter() - t0
-    bw = batch.stats()
+    pr = {"rays": 0, "litVoxels": 0, "primaryRays": 0}
+    for vol, *_ in A:
+        st = vol.stats()
+        for key in pr:
+            pr[key] += st[key]
+    br = batch.stats()
     tuning = batch.tuning()
-
-    rays = allreduce_sum(pg, bst["rays"])
-    dev_ms_max = allreduce_max(pg, dev_ms)
-    value = rays / (dev_ms_max / 1e3)
-    plain_value = allreduce_sum(pg, pr["rays"]) / allreduce_max(pg, plain_s)
-    bwall_value = allreduce_sum(pg, bw["rays"]) / allreduce_max(pg, bwall_s)
+    batch.close()
+    for form in sets.values():
+        for vol, img, *_ in form:
+            img.close()
+            vol.close()
+    for e in ev:
+        lib.dn_cuda_event_destroy(e)
+    rays_p = allreduce_sum(pg, pr["rays"])
+    rays_b = allreduce_sum(pg, br["rays"])
+    plain_s = allreduce_max(pg, plain_s)
+    batched_s = allreduce_max(pg, batched_s)
+    batched_dev_ms = allreduce_max(pg, batched_dev_ms)
     res_hist = {}
     for sp in specs:
         key = "%dx%d" % sp["res"]
         res_hist[key] = res_hist.get(key, 0) + 1
-    result = {
-        "metric": METRIC + " (batched)", "value": value, "unit": "rays/s", "n_gpus": world, "steps": K,
-        "warmup": args.warmup, "ms_per_step": dev_ms_max / K, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded heightfields; the reference publishes no scenes)",
-        "config": {"workload": "batched: %d maps, chunk dims U[8,64] per axis, non-empty fraction U[0.05,0.5], "
-                               "own seeded camera each, resolutions from 320x180..1920x1080, K=16, 1 diffuse path "
-                               "per voxel per frame" % len(maps),
-                   "maps": len(maps), "tiles": tiles, "nonempty_chunks": nonempty, "pixels_per_step": pixels,
-                   "resolutions": res_hist, "frame": "draw -> sync -> lighting for every map",
-                   "l2": "flushed between timed steps (256 MiB write, outside the timed events)",
-                   "parallelism": "replicas: own maps per GPU, no collective"},
-        "lit_voxels_per_s": allreduce_sum(pg, bst["litVoxels"]) / (dev_ms_max / 1e3),
-        "primary_rays_per_s": allreduce_sum(pg, bst["primaryRays"]) / (dev_ms_max / 1e3),
-        "rays_per_step": rays / K,
-        "batched_wall_rays_per_s": bwall_value,
-        "plain_wall_rays_per_s": plain_value,
-        "speedup_vs_plain": bwall_value / plain_value if plain_value else None,
+    return {
+        "workload": "batched: %d maps, chunk dims U[8,64] per axis, non-empty fraction U[0.05,0.5], own seeded camera "
+                    "each, resolutions 320x180..1920x1080, K=16, 1 diffuse path per voxel per frame" % len(specs),
+        "maps": len(specs), "tiles": tiles, "nonempty_chunks": nonempty, "pixels_per_frame": pixels,
+        "resolutions": res_hist,
+        "method": "two identical map sets; each frame number runs the plain form on one and the batched form on the "
+                  "other (same rays: counters compared); frames %d..%d timed after %d warm-up frames; wall clock from "
+                  "issue to results on the host, L2 flushed before each form's frame"
+                  % (frames_warm, frames_warm + frames_timed - 1, frames_warm),
+        "plain_rays_per_s": rays_p / plain_s if plain_s else None,
+        "batched_rays_per_s": rays_b / batched_s if batched_s else None,
+        "batched_device_rays_per_s": rays_b / (batched_dev_ms / 1e3) if batched_dev_ms else None,
+        "ratio": (rays_b / batched_s) / (rays_p / plain_s) if plain_s and batched_s and rays_p else None,
+        "rays_per_frame": rays_b / frames_timed,
+        "identical_rays": int(rays_p) == int(rays_b),
+        "lit_voxels_per_frame": br["litVoxels"] / frames_timed,
+        "plain_ms_per_frame": plain_s * 1e3 / frames_timed,
+        "batched_ms_per_frame": batched_s * 1e3 / frames_timed,
+        "batched_gpu_launches_per_frame": launches / frames_timed,
+        "tuning": tuning, "autotuned": tuned is not None, "build_s": build_s, "clocks": clk,
         "plain_form": "per map: DN_draw, DN_sync_gpu, DN_update_lighting, DN_finish (one map at a time)",
-        "batched_form": "DN_batch_run over all maps + DN_batch_finish per step (graph replay)",
-        "tuning": tuning, "build_s": build_s, "wall_s": wall,
-        "gpu_launches": int(allreduce_sum(pg, launches)),
-        "clocks": clk,
+        "batched_form": "DN_batch_run over all maps + DN_batch_finish per frame (CUDA graph replay)",
     }
-    batch.close()
-    for vol, img, *_ in maps:
-        img.close()
-        vol.close()
+
+
+def run_batched(args):
+    """The batched workload as its own bench line (value = batched rays/s, wall clock, both forms on
+    identical frames: batched_vs_plain)."""
+    rank, world, local, pg = dist_setup()
+    import doonengine_gb300 as dn
+    lib = dn.load()
+    if lib.dn_cuda_init(local) != 0:
+        raise RuntimeError("dn_cuda_init(%d): %s" % (local, lib.dn_cuda_last_error().decode()))
+    dn.init()
+    r = batched_vs_plain(args, lib, rank, pg, local, args.warmup, args.steps, autotune=not args.no_autotune)
+    result = {
+        "metric": METRIC + " (batched)", "value": r["batched_rays_per_s"], "unit": "rays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["batched_ms_per_frame"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded heightfields; the reference publishes no scenes)",
+        "config": {"workload": r["workload"], "maps": r["maps"], "tiles": r["tiles"],
+                   "frame": "draw -> sync -> lighting for every map",
+                   "l2": "flushed before each timed frame of each form (256 MiB write, outside the timed region)",
+                   "parallelism": "replicas: own maps per GPU, no collective"},
+        "batched_vs_plain": r, "gpu_launches": int(r["batched_gpu_launches_per_frame"] * args.steps),
+        "clocks": r["clocks"],
+    }
     if rank == 0:
         print(json.dumps(result), flush=True)
 
@@ -759,18 +796,13 @@ def shapes_cpu_baseline(map_size, ops, seconds):
 
 # ------------------------------------------------------------ serving workload
 
-def run_serving(args):
+def serving_sweep(args, lib, rank, world, nmaps, rates, seconds, budget_gb, stop_at_saturation=True):
     """Poisson request streams over many resident maps through the serving loop (serve.h), swept over
-    arrival rates: 70% draws, 25% relights of the visible chunks, 5% edit batches of 1-256 chunks."""
-    import ctypes
-    rank, world, local, pg = dist_setup()
+    arrival rates: 70% draws, 25% relights of the visible chunks, 5% edit batches of 1-256 chunks.
+    Returns the serving line (without printing it)."""
     import doonengine_gb300 as dn
-    from doonengine_gb300 import configs, _lib as L
-    lib = dn.load()
-    if lib.dn_cuda_init(local) != 0:
-        raise RuntimeError("dn_cuda_init(%d): %s" % (local, lib.dn_cuda_last_error().decode()))
-    dn.init()
-    specs = configs.serving_specs(args.maps, seed=11 + 1000 * rank)
+    from doonengine_gb300 import configs
+    specs = configs.serving_specs(nmaps, seed=11 + 1000 * rank)
     vols, views = [], []
     t0 = time.perf_counter()
     tiles = 0
@@ -781,7 +813,7 @@ def run_serving(args):
         tiles += vol.num_tiles
     build_s = time.perf_counter() - t0
     log("built %d maps in %.1f s (%d tiles)" % (len(vols), build_s, tiles))
-    budget = int(args.budget_gb * (1 << 30))
+    budget = int(budget_gb * (1 << 30))
     server = dn.Server(vols, budget_bytes=budget)
     # draw targets: a ring of device images per resolution (the bench does not read them back)
     ring = {r: [dn.Image(r[0], r[1], on_device=True, hit_info=True) for _ in range(args.image_ring)]
@@ -835,11 +867,10 @@ def run_serving(args):
     assert server.drain(1800.0), "warm-up did not drain"
     server.poll()
     sweep = []
-    rates = [float(x) for x in args.rates.split(",")]
     lib.DN_batch_reset_stats(lib.DN_server_batch(server.ptr))
     tot_rays, tot_s = 0, 0.0
     for rate in rates:
-        reqs, offs = make_requests(rate, args.seconds)
+        reqs, offs = make_requests(rate, seconds)
         st0 = server.stats()
         b0 = server.batch_stats()
         t0 = time.perf_counter()
@@ -871,7 +902,8 @@ def run_serving(args):
         # past saturation the queue only grows: stop the sweep there
         if not ok or (row["achieved_rps"] or 0.0) < 0.9 * rate:
             row["saturated"] = True
-            break
+            if stop_at_saturation:
+                break
     st = server.stats()
     good = [r for r in sweep if r["p99_ms"] is not None and r["p99_ms"] <= 33.0 and r["drained"]]
     best = max(good, key=lambda r: r["achieved_rps"]) if good else None
@@ -882,8 +914,9 @@ def run_serving(args):
         "data": "synthetic (seeded heightfields; Poisson arrivals)",
         "config": {"workload": "serving: %d resident maps, chunk dims log-uniform 8^3..96x32x96, requests 70%% draw "
                                "(320x180..1920x1080) / 25%% relight / 5%% edit batches of 1-256 chunks, Poisson "
-                               "arrivals swept over %s req/s, %.0f s each" % (len(vols), args.rates, args.seconds),
-                   "maps": len(vols), "tiles": tiles, "device_budget_gb": args.budget_gb,
+                               "arrivals swept over %s req/s, %.0f s each"
+                               % (len(vols), ",".join("%g" % r for r in rates), seconds),
+                   "maps": len(vols), "tiles": tiles, "device_budget_gb": budget_gb,
                    "parallelism": "replicas: own maps per GPU, no collective"},
         "sweep": sweep,
         "max_rps_with_p99_le_33ms": best["achieved_rps"] if best else None,
@@ -896,6 +929,18 @@ def run_serving(args):
             im.close()
     for v in vols:
         v.close()
+    return result
+
+
+def run_serving(args):
+    rank, world, local, pg = dist_setup()
+    import doonengine_gb300 as dn
+    lib = dn.load()
+    if lib.dn_cuda_init(local) != 0:
+        raise RuntimeError("dn_cuda_init(%d): %s" % (local, lib.dn_cuda_last_error().decode()))
+    dn.init()
+    rates = [float(x) for x in args.rates.split(",")]
+    result = serving_sweep(args, lib, rank, world, args.maps, rates, args.seconds, args.budget_gb)
     if rank == 0:
         print(json.dumps(result), flush=True)
 
@@ -920,7 +965,7 @@ def run_reference(args):
     om = O.OracleMap(vol.map_size)
     rng = np.random.default_rng(0)
     pix_n = args.ref_pixels if args.ref_pixels > 0 else W * H
-    req_cap = args.ref_requests
+    req_cap = args.ref_requests if args.ref_requests > 0 else None
 
     def clear_updated():
         # the product's DN_sync_gpu clears 'updated' after streaming (voxel.c:1534); the oracle only reads it
@@ -936,23 +981,35 @@ def run_reference(args):
             om.draw(vol.s, iv, icv, ip, W, H, pixels=pix, nthreads=ncores)
         om.sync(vol.s, 2, 1)
         clear_updated()
-        p = om.light_params(vol.s, 1, 1000, 1.0 + 0.25 * f)
         reqs = om.requests()
-        sel = rng.permutation(len(reqs))[:req_cap].astype(np.uint32)
-        if len(sel):
-            om.light_requests(vol.s, p, sel, nthreads=ncores)
+        if req_cap is None:
+            # the whole lighting update, committed like DN_update_lighting's (sample counts grow, so later
+            # frames trace K shadow rays per voxel instead of the first sample's one): the GPU arm's work
+            om.light(vol.s, 1, 1000, 1.0 + 0.25 * f, nthreads=ncores)
+        else:
+            p = om.light_params(vol.s, 1, 1000, 1.0 + 0.25 * f)
+            sel = rng.permutation(len(reqs))[:req_cap].astype(np.uint32)
+            if len(sel):
+                om.light_requests(vol.s, p, sel, nthreads=ncores)
+        return len(reqs)
 
     for f in range(args.warmup):
         frame(f)
     om.reset_counters()
+    groups = 0
     t0 = time.perf_counter()
     for k in range(args.steps):
-        frame(args.warmup + k)
+        groups += frame(args.warmup + k)
     el = time.perf_counter() - t0
     c = om.counters()
     value = c["rays"] / el
-    sample = ("per step: %d sampled pixels of the %dx%d draw + up to %d sampled lighting request groups, "
-              "the CPU restatement of the reference shaders with OpenMP" % (pix_n, W, H, req_cap))
+    if pix_n >= W * H and req_cap is None:
+        sample = ("per step: the whole frame, the same work as the GPU arm's step of the same number: all %dx%d "
+                  "pixels of the draw and all %.0f lighting request groups of the frame (mean), the CPU "
+                  "restatement of the reference shaders with OpenMP" % (W, H, groups / max(1, args.steps)))
+    else:
+        sample = ("per step: %d sampled pixels of the %dx%d draw + %s sampled lighting request groups, the CPU "
+                  "restatement of the reference shaders with OpenMP" % (pix_n, W, H, req_cap if req_cap else "all"))
     result = {"metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
               "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -960,6 +1017,9 @@ def run_reference(args):
               "config": workload_desc(cfg, vol, nonempty, args.config),
               "cpu_baseline": {"value": value, "unit": "rays/s", "cores": ncores, "kind": "port", "sample": sample},
               "e2e": {"value": value, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+              "rays_per_step": c["rays"] / args.steps,
+              "rays_by_kind_per_step": {"primary": c["primary"] / args.steps,
+                                        "lighting": (c["rays"] - c["primary"]) / args.steps},
               "note": "the reference path runs only as GLSL through OpenGL, which is unavailable on this box; "
                       "this arm times the CPU restatement of its algorithm"}
     om.close()
@@ -978,7 +1038,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-pixels", type=int, default=0, help="pixels per reference step (0 = the full image)")
-    ap.add_argument("--ref-requests", type=int, default=2048, help="lighting request groups per reference step")
+    ap.add_argument("--ref-requests", type=int, default=0,
+                    help="lighting request groups per reference step (0 = all of the frame's, the GPU arm's mix)")
     ap.add_argument("--workload", default="plain", choices=["plain", "batched", "serving", "streaming", "shapes"],
                     help="plain: one map per step (the headline); batched: many maps per step")
     ap.add_argument("--maps", type=int, default=64, help="maps of the batched workload")
@@ -991,6 +1052,17 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device budget")
     ap.add_argument("--image-ring", type=int, default=16, help="serving: draw targets per resolution")
     ap.add_argument("--drain-timeout", type=float, default=20.0)
+    ap.add_argument("--no-batched", action="store_true", help="plain workload: skip the batched-vs-plain part")
+    ap.add_argument("--no-serving", action="store_true", help="plain workload: skip the serving parts")
+    ap.add_argument("--batched-warmup", type=int, default=8, help="plain workload's batched part: warm-up frames")
+    ap.add_argument("--batched-frames", type=int, default=4, help="plain workload's batched part: timed frames")
+    ap.add_argument("--serving-rates", default="500,800,1000,1200,1400,1600,2000",
+                    help="plain workload's serving part: offered req/s")
+    ap.add_argument("--serving-seconds", type=float, default=2.0, help="plain workload's serving part: s per rate")
+    ap.add_argument("--pressure-budget-gb", type=float, default=60.0,
+                    help="plain workload: a second serving sweep under this device budget (below the resident "
+                         "set, so whole maps are evicted to pinned host memory under load); 0 skips it")
+    ap.add_argument("--pressure-rates", default="300,600,900", help="offered req/s of the eviction sweep")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3 (at least three untimed steps)")
