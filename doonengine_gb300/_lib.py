@@ -91,7 +91,7 @@ class DNimage(Structure):
 
 class DNstats(Structure):
     _fields_ = [("rays", c_uint64), ("primaryRays", c_uint64), ("outerSteps", c_uint64), ("chunksEntered", c_uint64),
-                ("innerSteps", c_uint64), ("hits", c_uint64), ("litVoxels", c_uint64)]
+                ("innerSteps", c_uint64), ("hits", c_uint64), ("litVoxels", c_uint64), ("degenerate", c_uint64)]
 
 
 class DnLightParams(Structure):

@@ -52,6 +52,7 @@ struct DNgpuBatch {
     dn_batch_tuning tuning;
     int maxBlocksPerSM;         // of the ray-stream kernel
     int maxBlocksPacket;        // of the packet kernel
+    int maxBlocksDiffuse;       // of the diffuse-path kernel that follows it
     std::vector<uint64_t> lastKey;
     std::vector<uint64_t> graphKey;
     cudaGraphExec_t graph;
@@ -158,6 +159,13 @@ __global__ void __launch_bounds__(128, DN_PACKET_MIN_BLOCKS) k_light_packet_batc
     packet_loop<true>(nullptr, &a, warps[threadIdx.x >> 5]);
 }
 
+// the diffuse paths of the voxels k_light_packet_batch lit, as per-lane path streams over every map's queue
+__global__ void __launch_bounds__(128, DN_DIFF_MIN_BLOCKS) k_light_diffuse_batch(const __grid_constant__ BatchLightArgs a)
+{
+    __shared__ Job jobs[128];
+    stream_loop<true, true>(nullptr, &a, nullptr, jobs[threadIdx.x]);
+}
+
 __global__ void k_commit_batch(const BatchLightMap* l, const uint32_t* reqStart, uint32_t nl)
 {
     const uint64_t total = (uint64_t)reqStart[nl] * 32u;
@@ -225,12 +233,14 @@ extern "C" int dn_cuda_batch_create(DNgpuBatch** out)
         if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "memset: %s", cudaGetErrorString(e));
     }
     if (!rc) {
-        int perSM = 0, perSM2 = 0;
+        int perSM = 0, perSM2 = 0, perSM3 = 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_stream_batch, 128, 0);
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM2, k_light_packet_batch, 128, 0);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM3, k_light_diffuse_batch, 128, 0);
         if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "occupancy: %s", cudaGetErrorString(e));
         b->maxBlocksPerSM = perSM < 1 ? 1 : perSM;
         b->maxBlocksPacket = perSM2 < 1 ? 1 : perSM2;
+        b->maxBlocksDiffuse = perSM3 < 1 ? 1 : perSM3;
         // every resident block the kernel allows
         b->tuning.blocksPerSM = (uint32_t)(b->tuning.kernel == 2u ? b->maxBlocksPacket : b->maxBlocksPerSM);
     }
@@ -332,6 +342,15 @@ static int issue_light(DNgpuBatch* b, const BatchLightArgs& la, cudaStream_t s, 
     if (packets) k_light_packet_batch<<<(unsigned)(g_numSMs * (int)b->tuning.blocksPerSM), 128, 0, s>>>(la);
     else k_light_stream_batch<<<(unsigned)(g_numSMs * (int)b->tuning.blocksPerSM), 128, 0, s>>>(la);
     CK(cudaGetLastError());
+    if (packets) {
+        // the diffuse paths: a second pass over the same queue
+        BatchLightArgs ld = la;
+        ld.batch = g_streamBatch;
+        CK(cudaMemsetAsync(la.workCounter, 0, 4, s));
+        COUNT_LAUNCH();
+        k_light_diffuse_batch<<<(unsigned)(g_numSMs * b->maxBlocksDiffuse), 128, 0, s>>>(ld);
+        CK(cudaGetLastError());
+    }
     return DN_CUDA_OK;
 }
 
@@ -503,6 +522,7 @@ extern "C" int dn_cuda_batch_frame(DNgpuBatch* b, const dn_batch_item* items, ui
             BatchDrawEntry& e = hd[id];
             memset(&e, 0, sizeof(e));
             e.d.m = dev_map(g);
+            e.d.m.degen = &b->bst->stats[S_DEGEN];
             e.d.p = it.draw;
             e.d.color = it.hostImage ? g->dimg : (float4*)it.colorOut;
             e.d.hit = it.hitOut ? (it.hostImage ? g->dhit : it.hitOut) : nullptr;
@@ -531,6 +551,7 @@ extern "C" int dn_cuda_batch_frame(DNgpuBatch* b, const dn_batch_item* items, ui
             BatchLightMap& e = hl[il];
             memset(&e, 0, offsetof(BatchLightMap, sdir));
             e.m = dev_map(g);
+            e.m.degen = &b->bst->lstats[S_DEGEN];
             e.reqs = g->reqs; e.nsamples = g->nsamples; e.out = g->lightOut;
             e.nreqPtr = &g->st->w[ST_REQ]; e.reqCap = g->reqCap;
             e.p = it.light;
@@ -629,6 +650,7 @@ extern "C" int dn_cuda_batch_stats(DNgpuBatch* b, int kind, dn_stats* out)
     for (int k = 0; k < 8; k++) s[k] = (kind != 2 ? b->hbst->stats[k] : 0ull) + (kind != 1 ? b->hbst->lstats[k] : 0ull);
     out->rays = s[S_RAYS]; out->primary = s[S_PRIMARY]; out->outerSteps = s[S_OUTER];
     out->chunksEntered = s[S_ENTERED]; out->innerSteps = s[S_INNER]; out->hits = s[S_HITS]; out->litVoxels = s[S_LIT];
+    out->degenerate = s[S_DEGEN];
     return rc;
 }
 

@@ -417,8 +417,17 @@ __global__ void __launch_bounds__(128, DN_PACKET_MIN_BLOCKS) k_light_packet(cons
     packet_loop<false>(&a, nullptr, warps[threadIdx.x >> 5]);
 }
 
-// launches the lighting kernel g_lightKernel selects (1 ray streams, 2 warp packets; packets need
-// specBounceLimit <= PK_MAX_SPEC_SEGMENTS and fall back to streams otherwise) with its batch threshold
+// The diffuse paths of the voxels k_light_packet lit, as per-lane path streams over the whole request list:
+// a lane whose voxel's paths are done takes the next voxel, so no lane waits for another lane's long path.
+__global__ void __launch_bounds__(128, DN_DIFF_MIN_BLOCKS) k_light_diffuse(const __grid_constant__ StreamArgs a)
+{
+    __shared__ Job jobs[128];
+    stream_loop<false, true>(&a, nullptr, nullptr, jobs[threadIdx.x]);
+}
+
+// launches the lighting kernel g_lightKernel selects (1 ray streams, 2 warp packets followed by the
+// diffuse-path kernel; packets need specBounceLimit <= PK_MAX_SPEC_SEGMENTS and fall back to streams
+// otherwise) with its batch threshold
 static int launch_light(DNgpuVolume* g, StreamArgs& a)
 {
     int perSM = 0;
@@ -433,6 +442,13 @@ static int launch_light(DNgpuVolume* g, StreamArgs& a)
         k_light_tables<<<1, 256, 0, g->stream>>>(table, a.p, g->dtab);
         COUNT_LAUNCH();
         k_light_packet<<<g->numSMs * perSM, 128, 0, g->stream>>>(a);
+        CK(cudaGetLastError());
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_diffuse, 128, 0));
+        if (perSM < 1) perSM = 1;
+        CK(cudaMemsetAsync(a.workCounter, 0, 4, g->stream));
+        a.batch = g_streamBatch;
+        COUNT_LAUNCH();
+        k_light_diffuse<<<g->numSMs * perSM, 128, 0, g->stream>>>(a);
     } else {
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_stream, 128, 0));
         if (perSM < 1) perSM = 1;
@@ -599,6 +615,7 @@ extern "C" int dn_cuda_light(DNgpuVolume* g, const dn_light_params* p, const dn_
     static thread_local StreamArgs* a = nullptr;
     if (!a) a = new StreamArgs();
     a->m = dev_map(g);
+    a->m.degen = &g->st->lstats[S_DEGEN];
     a->reqs = g->reqs; a->workCounter = &g->st->w[ST_WORK]; a->nreqPtr = &g->st->w[ST_REQ];
     a->nsamples = g->nsamples; a->out = g->lightOut; a->stats = g->st->lstats;
     a->batch = g_streamBatch;
@@ -698,6 +715,7 @@ extern "C" int dn_cuda_light_noalloc(DNgpuVolume* g, const dn_light_params* p, c
     CK(cudaGetLastError());
     StreamArgs a;                       // launch arguments on the stack: no host allocation either
     a.m = dev_map(g);
+    a.m.degen = &g->st->lstats[S_DEGEN];
     a.reqs = g->reqs; a.workCounter = &g->st->w[ST_WORK]; a.nreqPtr = &g->st->w[ST_LIMITED];
     a.nsamples = g->nsamples; a.out = scratch; a.stats = g->st->lstats;
     a.batch = g_streamBatch;
@@ -752,6 +770,7 @@ static int launch_draw(DNgpuVolume* g, const dn_draw_params* p, const dn_materia
     static thread_local DrawArgs* a = nullptr;
     if (!a) a = new DrawArgs();
     a->d.m = dev_map(g);
+    a->d.m.degen = &g->st->stats[S_DEGEN];
     a->d.p = *p;
     a->d.color = color; a->d.hit = hit; a->d.face = face; a->d.stats = g->st->stats;
     memcpy(a->mats, materials, sizeof(a->mats));
@@ -832,6 +851,7 @@ extern "C" int dn_cuda_stats_kind(DNgpuVolume* g, int kind, dn_stats* out)
         s[k] = (kind != 2 ? g->hst->stats[k] : 0ull) + (kind != 1 ? g->hst->lstats[k] : 0ull);
     out->rays = s[S_RAYS]; out->primary = s[S_PRIMARY]; out->outerSteps = s[S_OUTER];
     out->chunksEntered = s[S_ENTERED]; out->innerSteps = s[S_INNER]; out->hits = s[S_HITS]; out->litVoxels = s[S_LIT];
+    out->degenerate = s[S_DEGEN];
     return rc;
 }
 
@@ -1000,7 +1020,8 @@ extern "C" int dn_cuda_flush_l2(void* stream, size_t bytes)
 
 extern "C" const char* dn_cuda_kernel_names(void)
 {
-    return "k_draw;k_light_stream;k_light_packet;k_light_tables;k_commit;k_sync_stage;k_compact;k_clamp_requests;k_flush;"
-           "k_draw_batch;k_compact_batch;k_batch_reset;k_batch_prep;k_light_stream_batch;k_light_packet_batch;k_commit_batch;k_batch_gather;"
+    return "k_draw;k_light_stream;k_light_packet;k_light_diffuse;k_light_tables;k_commit;k_sync_stage;k_compact;k_clamp_requests;k_flush;"
+           "k_draw_batch;k_compact_batch;k_batch_reset;k_batch_prep;k_light_stream_batch;k_light_packet_batch;k_light_diffuse_batch;"
+           "k_commit_batch;k_batch_gather;"
            "k_shape_count;k_shape_write";
 }

@@ -159,6 +159,7 @@ struct DevMap {
     const uint2* __restrict__ vox;       // normal word, linear albedo word
     const float4* __restrict__ diff;
     const float4* __restrict__ spec;
+    unsigned long long* degen;           // D16: segments ended at once for a degenerate direction (counter)
 };
 
 struct Voxel { f3 normal; uint32_t material; f3 albedo; f3 spec; f3 diff; };
@@ -241,11 +242,15 @@ struct RayCtx {
     bool capped;
 };
 
-// D16: a traversal segment that has visited this many cells ends as a miss.  A ray whose direction has a
-// finite, non-zero component on every axis leaves the map long before (every DDA step advances one axis
-// monotonically: at most sx+sy+sz chunk cells and 24 voxel cells per chunk entered); the cap ends only
-// degenerate rays -- a direction component exactly zero or NaN makes the reference's side distances NaN
-// after one step (0 * inf), after which no axis may be stepped again and its loop would never end.
+// D16: a traversal segment whose direction has a zero or NaN component -- its reciprocal is then infinite
+// or NaN -- traverses nothing and ends at once as a miss (counted in DevMap::degen).  The reference's side
+// distances become NaN after one step of such a ray (0 * inf), after which no axis may be stepped again and
+// its loops (voxelShared.comp:339, 435) never end; reflect() without an added EPSILON
+// (voxelLighting.comp:132, 163) produces such directions.  With a finite direction every DDA step advances
+// one axis monotonically (at most sx+sy+sz chunk cells and 24 voxel cells per chunk entered); the cell cap
+// below ends only repeated refraction inside transparent voxels (the draw).
+__device__ __forceinline__ bool finite_dir(f3 inv) { return isfinite(inv.x) && isfinite(inv.y) && isfinite(inv.z); }
+__device__ __forceinline__ void count_degenerate(const DevMap& m) { if (m.degen) atomicAdd(m.degen, 1ull); }
 __device__ __forceinline__ uint32_t step_cap(uint32_t sx, uint32_t sy, uint32_t sz)
 {
     const uint64_t c = 256ull * ((uint64_t)sx + sy + sz) + 4096ull;
@@ -301,6 +306,7 @@ static __device__ __forceinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapP
                     f3 n = (dot(vox.normal, rayDir) < 0.0f) ? normalize(vox.normal) : hitNormal;
                     rayDir = refract(rayDir, n, ts.lastVoxRefract / mat.refractIndex);
                     inv = mk(1.0f / rayDir.x, 1.0f / rayDir.y, 1.0f / rayDir.z);
+                    if (!finite_dir(inv)) { count_degenerate(m); c.capped = true; return false; }
                     init_dda(rayDir, inv, rayPos, pos, delta, step, side);
                     lastSide = mk(0.0f, 0.0f, 0.0f);
                 }
@@ -317,6 +323,7 @@ static __device__ __forceinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapP
                 rayDir = refract(rayDir, n, ts.lastVoxRefract);
                 if (rayDir.x == 0.0f && rayDir.y == 0.0f && rayDir.z == 0.0f) rayDir = old;
                 inv = mk(1.0f / rayDir.x, 1.0f / rayDir.y, 1.0f / rayDir.z);
+                if (!finite_dir(inv)) { count_degenerate(m); c.capped = true; return false; }
                 init_dda(rayDir, inv, rayPos, pos, delta, step, side);
                 lastSide = mk(0.0f, 0.0f, 0.0f);
             }
@@ -342,6 +349,7 @@ static __device__ __forceinline__ bool step_map(RayCtx& c, TState& ts, f3& rayDi
     c.c.rays++;
     c.segSteps = 0;
     c.capped = false;
+    if (!finite_dir(inv)) { count_degenerate(m); return false; }
     const uint32_t cap = step_cap(m.sx, m.sy, m.sz);
     i3 pos, step; f3 delta, side, lastSide = mk(0.0f, 0.0f, 0.0f);
     init_dda(rayDir, inv, rayPos, pos, delta, step, side);

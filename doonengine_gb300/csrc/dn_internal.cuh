@@ -29,7 +29,7 @@ int dn_set_err(int code, const char* fmt, ...);
 enum { ST_REQ = 0, ST_WORK = 1, ST_ERR = 2, ST_LIMITED = 3 };
 // error flag bits of ST_ERR (reported by dn_cuda_finish / dn_cuda_batch_finish)
 enum : uint32_t { ERRF_TILE = 1u, ERRF_RECORD = 2u, ERRF_REQUESTS = 4u, ERRF_NOALLOC_CAPACITY = 0x100u };
-enum { S_RAYS = 0, S_PRIMARY, S_OUTER, S_ENTERED, S_INNER, S_HITS, S_LIT, S_COUNT };
+enum { S_RAYS = 0, S_PRIMARY, S_OUTER, S_ENTERED, S_INNER, S_HITS, S_LIT, S_DEGEN, S_COUNT };
 
 struct DevState {
     uint32_t w[4];                      // nreq, work counter, error flags, noalloc request count
@@ -96,6 +96,7 @@ static inline dn::DevMap dev_map(const DNgpuVolume* g)
     m.stepCap = cap > (1ull << 23) ? (1u << 23) : (uint32_t)cap;
     m.tword = g->tword; m.tbits = g->tbits; m.treq = g->treq; m.ttouch = g->ttouch; m.tvis = g->tvis;
     m.rec = g->rec; m.vox = g->vox; m.diff = g->diff; m.spec = g->spec;
+    m.degen = nullptr;                   // set by the launch: the draw's or the lighting's counter
     return m;
 }
 

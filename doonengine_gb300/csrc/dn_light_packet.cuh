@@ -10,9 +10,11 @@
  * almost parallel, its specular rays share their origin and lobe).  Ended segments are shaded once
  * `batch` lanes have one.  Each ray's contributions go to shared memory; when the pool is empty, each
  * voxel's sums are formed by one lane walking its rays (and their segments) in ray order, so every sum
- * is accumulated in exactly the reference's order.  The diffuse paths (numDiffuse per voxel, up to
- * diffuseBounceLimit segments each) run one lane per voxel, and each lane finishes its voxel as the
- * reference's lighting main does (running average, clamps, voxelLighting.comp:238-288).
+ * is accumulated in exactly the reference's order.  The kernel writes each voxel's specular lighting and
+ * leaves its direct light for the diffuse kernel (dn_light_stream.cuh, stream_loop<.., true>), which traces
+ * the diffuse paths (numDiffuse per voxel, up to diffuseBounceLimit segments each) as per-lane path
+ * streams over all request groups and finishes each voxel as the reference's lighting main does (running
+ * average, clamps, voxelLighting.comp:238-288).
  *
  * Results, traversal side effects (requested / touched / visible flags) and counters are those of the
  * one-voxel-per-lane form (dn_light_stream.cuh): the same rays are traced with the same
@@ -394,103 +396,18 @@ __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLi
             __syncwarp();
         }
 
-        // ---- (2) diffuse paths (voxelLighting.comp:149-203), one lane per voxel
-        f3 pacc = mk(0.0f, 0.0f, 0.0f);
-        if (diffMask) {
-            const bool mine = (diffMask >> lane) & 1u;
-            const PacketVoxel& pv = W.v[lane];
-            jd.key = pv.key; jd.tnormal = pv.tnormal; jd.tmat = pv.tmat;
-            jd.firstSample = (pv.flags & PV_FIRST) != 0u;
-            uint32_t pi = 0;
-            live = mine;
-            stepping = false;
-            hs = 3u;                       // "start the next path"
-            for (int guard = 0; guard < (1 << 30); guard++) {
-                if (live && !stepping) {
-                    bool pathDone = hs != 3u;
-                    if (hs == 1u) {
-                        Voxel hv;
-                        decompress(m, hitIdx, hv);
-                        jd.jB = hv.normal;
-                        jd.jU = hv.material;
-                        const f3 d = vabs(sub(vfloor(muls(pv.pos0, 8.0f)), vfloor(muls(s.pos, 8.0f))));
-                        if (!(dot(d, d) < 1.0f)) {
-                            const Material& hm = mats[hv.material];
-                            if (hm.emissive) {
-                                pacc.x = pacc.x + jd.jA.x * (hv.albedo.x * p.emissiveStrength * s.cmul + s.cadd.x);
-                                pacc.y = pacc.y + jd.jA.y * (hv.albedo.y * p.emissiveStrength * s.cmul + s.cadd.y);
-                                pacc.z = pacc.z + jd.jA.z * (hv.albedo.z * p.emissiveStrength * s.cmul + s.cadd.z);
-                            } else {
-                                jd.jA.x = jd.jA.x * (hv.albedo.x * s.cmul + s.cadd.x);
-                                jd.jA.y = jd.jA.y * (hv.albedo.y * s.cmul + s.cadd.y);
-                                jd.jA.z = jd.jA.z * (hv.albedo.z * s.cmul + s.cadd.z);
-                                jd.jC = s.dir;
-                                jd.b++;
-                                if (jd.b < p.diffuseBounceLimit) {
-                                    const f3 nd = diffuse_dir(jd, p, mats, rngSin);
-                                    const TState keep = s.ts;
-                                    seg_begin(s, s.pos, nd, rcp3(nd));
-                                    s.ts = keep;
-                                    c.rays++;
-                                    pathDone = false;
-                                    stepping = true;
-                                }
-                            }
-                        }
-                    } else if (hs == 2u) {
-                        const float kd = gmax(dot(s.dir, sunDir), 0.0f);
-                        pacc.x = pacc.x + (jd.jA.x * kd * sun.x * s.cmul + s.cadd.x);
-                        pacc.y = pacc.y + (jd.jA.y * kd * sun.y * s.cmul + s.cadd.y);
-                        pacc.z = pacc.z + (jd.jA.z * kd * sun.z * s.cmul + s.cadd.z);
-                    }
-                    if (pathDone) { pacc = add(pacc, pv.direct); pi++; }
-                    hs = 0;
-                    if (!stepping) {
-                        // the voxel's next path, if any (paths without segments finish at once)
-                        live = false;
-                        while (pi < p.numDiffuse) {
-                            pacc = add(pacc, mk(p.ambient[0], p.ambient[1], p.ambient[2]));
-                            if (p.diffuseBounceLimit == 0u) { pacc = add(pacc, pv.direct); pi++; continue; }
-                            jd.i = pi; jd.b = 0;
-                            jd.jA = mk(1.0f, 1.0f, 1.0f);
-                            jd.jB = adds(jd.tnormal, EPS);
-                            jd.jC = mk(0.0f, 0.0f, 0.0f);
-                            jd.jU = jd.tmat;
-                            const f3 nd = diffuse_dir(jd, p, mats, rngSin);
-                            seg_begin(s, pv.pos0, nd, rcp3(nd));
-                            c.rays++;
-                            live = true;
-                            stepping = true;
-                            break;
-                        }
-                    }
-                }
-                if (!__any_sync(0xFFFFFFFFu, live)) break;
-                while (__any_sync(0xFFFFFFFFu, stepping)) {
-                    if (stepping) {
-                        const uint32_t rr = seg_step(s, m, mats, p.sunStrength, c, hitIdx);
-                        if (rr) { stepping = false; hs = rr; }
-                    }
-                }
-            }
-        }
-        // ---- (3) write the voxel's new lighting (voxelLighting.comp:266-288, FP32)
+        // ---- (2) write the voxel's specular lighting (voxelLighting.comp:266-288, FP32).  Its diffuse paths
+        // run in the diffuse kernel that follows (k_light_diffuse: per-lane path streams, so that one long
+        // path does not hold the other 31 lanes), which reads the direct light left here in the diffuse slot
+        // and replaces it with the voxel's new diffuse lighting; a voxel without diffuse paths gets zero.
         __syncwarp();
         if (myFlags & PV_VALID) {
             const PacketVoxel& pv = W.v[lane];
-            f3 dacc = mk(0.0f, 0.0f, 0.0f);
-            if (myFlags & PV_DIFF) {
-                const float4 prev = __ldg(&m.diff[pv.vidx]);
-                const float den = pv.indirect + (float)p.numDiffuse;
-                dacc.x = (prev.x * pv.indirect + pacc.x) / den;
-                dacc.y = (prev.y * pv.indirect + pacc.y) / den;
-                dacc.z = (prev.z * pv.indirect + pacc.z) / den;
-            }
             const f3 sp = (myFlags & PV_SPEC) ? pv.spec : mk(0.0f, 0.0f, 0.0f);
             const float4 outS = make_float4(gmin(gmax(sp.x, 0.0f), 1.0f), gmin(gmax(sp.y, 0.0f), 1.0f),
                                             gmin(gmax(sp.z, 0.0f), 1.0f), 0.0f);
-            const float4 outD = make_float4(gmin(gmax(dacc.x, 0.0f), 1.0f), gmin(gmax(dacc.y, 0.0f), 1.0f),
-                                            gmin(gmax(dacc.z, 0.0f), 1.0f), 0.0f);
+            const float4 outD = (myFlags & PV_DIFF) ? make_float4(pv.direct.x, pv.direct.y, pv.direct.z, 0.0f)
+                                                    : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             const uint64_t o = ((uint64_t)req * 32u + lane) * 2u;
             out[o] = outD;
             out[o + 1] = outS;

@@ -28,6 +28,9 @@ namespace dn {
 #ifndef DN_STREAM_MIN_BLOCKS
 #define DN_STREAM_MIN_BLOCKS 4   // 4 blocks of 4 warps per SM (measured best: leaves L1 room for the tile map)
 #endif
+#ifndef DN_DIFF_MIN_BLOCKS
+#define DN_DIFF_MIN_BLOCKS 6     // the diffuse-path kernel (k_light_diffuse): 6 blocks of 4 warps per SM
+#endif
 
 enum : uint32_t { PH_FETCH = 0, PH_SPEC = 1, PH_SHADOW = 2, PH_DIFF = 3, PH_FINAL = 4, PH_DONE = 5 };
 
@@ -68,7 +71,7 @@ struct Seg {
     const ChunkRec* rec;
     uint32_t base;
     uint32_t flags;      // bit0 inner level, bit1 ignore (current level), bit2 saved outer ignore, bit3 requested,
-                         // bits 8-31 cells visited by the segment (D16 step cap)
+                         // bit4 degenerate direction (D16), bits 8-31 cells visited by the segment (D16 cell cap)
     f3 cadd;
     float cmul;
     TState ts;
@@ -85,6 +88,9 @@ __device__ __forceinline__ void seg_begin(Seg& s, f3 pos, f3 dir, f3 inv)
     init_dda(dir, inv, pos, s.cpos, delta, s.step, s.cside);
     s.clastMin = 0.0f;   // min3 of the zero vector
     s.flags = 2u;        // ignore the first voxel
+    // D16: a zero or NaN direction component traverses nothing; the first step ends the segment as a miss
+    // (a position outside the map) and counts it
+    if (!finite_dir(inv)) { s.cpos.x = -1; s.flags = 2u | 16u; }
 }
 
 // Advances one traversal step.  Returns 0 while the segment continues, 1 on an opaque hit (s.pos moved to
@@ -115,7 +121,10 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
     const bool occ = inb && (inner ? (((bits & 1u) != 0u) && !(s.flags & 2u)) : (cst == 2u));
     if (!inb || occ) {
         if (!inner) {
-            if (!inb) return 2u;
+            if (!inb) {
+                if (s.flags & 16u) count_degenerate(m);
+                return 2u;
+            }
             // a loaded chunk: enter it (voxelShared.comp:441-449)
             c.outer++;
             c.entered++;
@@ -180,15 +189,17 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
             s.flags |= 8u;
         }
     }
-    // iterate_DDA on the current level (voxelShared.comp:309-317)
-    const float gyz = gmin(s.cside.y, s.cside.z), gzx = gmin(s.cside.z, s.cside.x), gxy = gmin(s.cside.x, s.cside.y);
-    s.clastMin = gmin(gxy, s.cside.z);   // min3(lastSideDist) of the next step
+    // iterate_DDA on the current level (voxelShared.comp:309-317).  With a finite direction (D16) every side
+    // distance is finite and non-negative (never -0), so fminf gives GLSL min's value (y < x ? y : x) and
+    // adding delta only on the stepped axes gives exactly side + (mask ? 1 : 0) * delta.
+    const float gyz = fminf(s.cside.y, s.cside.z), gzx = fminf(s.cside.z, s.cside.x), gxy = fminf(s.cside.x, s.cside.y);
+    s.clastMin = fminf(gxy, s.cside.z);   // min3(lastSideDist) of the next step
     const bool mx = s.cside.x <= gyz;
     const bool my = s.cside.y <= gzx;
     const bool mz = s.cside.z <= gxy;
-    s.cside.x = s.cside.x + (mx ? 1.0f : 0.0f) * delta.x;
-    s.cside.y = s.cside.y + (my ? 1.0f : 0.0f) * delta.y;
-    s.cside.z = s.cside.z + (mz ? 1.0f : 0.0f) * delta.z;
+    if (mx) s.cside.x = s.cside.x + delta.x;
+    if (my) s.cside.y = s.cside.y + delta.y;
+    if (mz) s.cside.z = s.cside.z + delta.z;
     s.cpos.x += (int32_t)mx * step.x; s.cpos.y += (int32_t)my * step.y; s.cpos.z += (int32_t)mz * step.z;
     s.flags &= ~2u;
     return 0u;
@@ -250,6 +261,10 @@ __device__ __forceinline__ f3 diffuse_dir(const Job& j, const dn_light_params& p
 
 // Consumes the finished segment (hitState 1 hit / 2 miss) and sets up the next segment of this lane's
 // voxel; returns true when a segment was started.  Leaves the job in PH_FETCH when the voxel is done.
+// DIFFONLY: the voxel's diffuse paths only (its specular and direct light came from the ray-fan kernel,
+// which left the direct light in the diffuse output slot); the final write replaces that slot with the
+// voxel's new diffuse lighting and leaves the specular slot and the lit-voxel count alone.
+template <bool DIFFONLY = false>
 __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint32_t hitIdx, const DevMap& m,
                                         const dn_light_params& p, const Material* mats, const float (*sdir)[3],
                                         const float (*sinv)[3], float4* out, Counters& c, uint32_t& lit)
@@ -422,8 +437,10 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
                                             gmin(gmax(j.acc.z, 0.0f), 1.0f), 0.0f);
             const uint64_t o = ((uint64_t)j.req * 32u + j.vlane) * 2u;
             out[o] = outD;
-            out[o + 1] = outS;
-            lit++;
+            if constexpr (!DIFFONLY) {
+                out[o + 1] = outS;
+                lit++;
+            }
             j.phase = PH_FETCH;
         }
         return false;
@@ -432,6 +449,9 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
 }
 
 // Sets up voxel (req, vlane); returns false (and writes zero outputs) when the slot holds no voxel.
+// DIFFONLY: false (writing nothing) also for a voxel without diffuse paths; otherwise the job starts at its
+// diffuse paths with the direct light the ray-fan kernel left in the voxel's diffuse output slot.
+template <bool DIFFONLY = false>
 __device__ __forceinline__ bool voxel_setup(Job& j, uint32_t req, uint32_t vlane, const DevMap& m, const dn_light_params& p,
                                             const Material* mats, const uint32_t* reqs, const uint32_t* nsamples, float4* out)
 {
@@ -443,9 +463,11 @@ __device__ __forceinline__ bool voxel_setup(Job& j, uint32_t req, uint32_t vlane
     i3 cp; uint32_t li;
     const ChunkRec* rc = &m.rec[tw & SLOT_MASK];
     if ((tw >> 30) != 2u || vn >= __ldg(&rc->nvox) || !select_voxel(rc, vn, cp, li)) {
-        const uint64_t o = ((uint64_t)req * 32u + vlane) * 2u;
-        out[o] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        out[o + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if constexpr (!DIFFONLY) {
+            const uint64_t o = ((uint64_t)req * 32u + vlane) * 2u;
+            out[o] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            out[o + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
         return false;
     }
     const i3 mp{__ldg(&rc->pos[0]), __ldg(&rc->pos[1]), __ldg(&rc->pos[2])};
@@ -469,9 +491,18 @@ __device__ __forceinline__ bool voxel_setup(Job& j, uint32_t req, uint32_t vlane
     const float off = HALF_INV_CHUNK - EPS;
     j.pos0 = add(rp, muls(j.tnormal, off));
     const Material& tm = mats[j.tmat];
+    j.doDiff = tm.specular < 1.0f;
+    if constexpr (DIFFONLY) {
+        if (!j.doDiff) return false;
+        const float4 d = out[((uint64_t)req * 32u + vlane) * 2u];
+        j.direct = mk(d.x, d.y, d.z);
+        j.spec = mk(0.0f, 0.0f, 0.0f); j.acc = j.spec;
+        j.k = 0; j.b = 0; j.i = 0;
+        j.phase = PH_DIFF;
+        return true;
+    }
     const f3 viewDir = sub(j.pos0, mk(p.camPos[0], p.camPos[1], p.camPos[2]));
     j.doSpec = tm.specular > 0.0f && dot(viewDir, j.tnormal) < 0.0f && tm.reflectType <= 1u;
-    j.doDiff = tm.specular < 1.0f;
     if (j.doSpec) j.refl = reflect(normalize(viewDir), j.tnormal);
     j.spec = mk(0.0f, 0.0f, 0.0f); j.acc = j.spec; j.direct = j.spec;
     j.k = 0; j.b = 0; j.i = 0;
@@ -524,8 +555,10 @@ __device__ __forceinline__ void shadow_dir(const dn_light_params& p, int k, floa
 // The persistent loop of a lighting launch.  MANY = false: one map whose arguments live in the launch's
 // parameter space (one) and whose materials and shadow directions were staged into sh.  MANY = true: a
 // queue over the requests of many maps (many); each lane keeps a register copy of its current voxel's map
-// and reads that map's parameters, materials and shadow directions from device memory.
-template <bool MANY>
+// and reads that map's parameters, materials and shadow directions from device memory.  DIFFONLY: the
+// diffuse paths of the voxels the ray-fan kernel lit (advance<true>); one map's materials are read from
+// its device tables (one->gtab) and sh is not used.
+template <bool MANY, bool DIFFONLY = false>
 __device__ __forceinline__ void stream_loop(const StreamArgs* one, const BatchLightArgs* many, const StreamShared* sh,
                                             Job& j)
 {
@@ -546,7 +579,11 @@ __device__ __forceinline__ void stream_loop(const StreamArgs* one, const BatchLi
     if constexpr (MANY) { lm = many->maps[0].m; le = &many->maps[0]; lmi = 0; }
     auto M = [&]() -> const DevMap& { if constexpr (MANY) return lm; else return one->m; };
     auto P = [&]() -> const dn_light_params& { if constexpr (MANY) return le->p; else return one->p; };
-    auto MATS = [&]() -> const Material* { if constexpr (MANY) return le->mats; else return sh->mats; };
+    auto MATS = [&]() -> const Material* {
+        if constexpr (MANY) return le->mats;
+        else if constexpr (DIFFONLY) return one->gtab->mats;
+        else return sh->mats;
+    };
     Seg s;
     bool rayActive = false;
     uint32_t hitState = 0, hitIdx = 0;
@@ -591,9 +628,10 @@ __device__ __forceinline__ void stream_loop(const StreamArgs* one, const BatchLi
                             const BatchLightMap& e = many->maps[winMap];
                             if (winMap != lmi) { lm = e.m; le = &e; lmi = winMap; }
                             j.map = winMap;
-                            voxel_setup(j, winReq, winNext + rank, lm, e.p, e.mats, e.reqs, e.nsamples, e.out);
+                            voxel_setup<DIFFONLY>(j, winReq, winNext + rank, lm, e.p, e.mats, e.reqs, e.nsamples, e.out);
                         } else {
-                            voxel_setup(j, winReq, winNext + rank, one->m, one->p, sh->mats, one->reqs, one->nsamples, one->out);
+                            voxel_setup<DIFFONLY>(j, winReq, winNext + rank, one->m, one->p, MATS(), one->reqs, one->nsamples,
+                                                  one->out);
                         }
                     }
                     const uint32_t took = (uint32_t)__popc(need) < 32u - winNext ? (uint32_t)__popc(need) : 32u - winNext;
@@ -603,7 +641,11 @@ __device__ __forceinline__ void stream_loop(const StreamArgs* one, const BatchLi
                 if (!rayActive && j.phase != PH_DONE && j.phase != PH_FETCH) {
                     if constexpr (MANY) {
                         if (j.map != lmi) { le = &many->maps[j.map]; lm = le->m; lmi = j.map; }
-                        rayActive = advance(j, s, hitState, hitIdx, lm, le->p, le->mats, le->sdir, le->sinv, le->out, c, lit);
+                        rayActive = advance<DIFFONLY>(j, s, hitState, hitIdx, lm, le->p, le->mats, le->sdir, le->sinv, le->out,
+                                                      c, lit);
+                    } else if constexpr (DIFFONLY) {
+                        rayActive = advance<true>(j, s, hitState, hitIdx, one->m, one->p, MATS(), one->gtab->sdir,
+                                                  one->gtab->sinv, one->out, c, lit);
                     } else {
                         rayActive = advance(j, s, hitState, hitIdx, one->m, one->p, sh->mats, sh->sdir, sh->sinv, one->out, c, lit);
                     }

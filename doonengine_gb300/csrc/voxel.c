@@ -1384,7 +1384,7 @@ bool DN_get_stats(DNvolume* vol, DNstats* out)
 	if (dn_cuda_stats(vol->gpu, &s) != DN_CUDA_OK) return false;
 	out->rays = s.rays; out->primaryRays = s.primary; out->outerSteps = s.outerSteps;
 	out->chunksEntered = s.chunksEntered; out->innerSteps = s.innerSteps; out->hits = s.hits;
-	out->litVoxels = s.litVoxels;
+	out->litVoxels = s.litVoxels; out->degenerate = s.degenerate;
 	return true;
 }
 
@@ -1623,7 +1623,7 @@ bool DN_batch_get_stats(DNbatch* b, DNstats* out)
 	if (!b || !out || dn_cuda_batch_stats(b->gpu, 0, &s) != DN_CUDA_OK) return false;
 	out->rays = s.rays; out->primaryRays = s.primary; out->outerSteps = s.outerSteps;
 	out->chunksEntered = s.chunksEntered; out->innerSteps = s.innerSteps; out->hits = s.hits;
-	out->litVoxels = s.litVoxels;
+	out->litVoxels = s.litVoxels; out->degenerate = s.degenerate;
 	return true;
 }
 

@@ -174,6 +174,7 @@ typedef struct DNstats
 	uint64_t innerSteps;      /* voxel cells visited */
 	uint64_t hits;            /* voxels read */
 	uint64_t litVoxels;       /* voxels whose lighting was updated */
+	uint64_t degenerate;      /* segments ended at once for a zero or NaN direction component */
 } DNstats;
 
 /* INITIALIZATION (voxel.h:153-184) */

@@ -100,6 +100,7 @@ typedef struct dn_draw_params {
 
 typedef struct dn_stats {
     uint64_t rays, primary, outerSteps, chunksEntered, innerSteps, hits, litVoxels;
+    uint64_t degenerate;    /* segments ended at once for a zero or NaN direction component */
 } dn_stats;
 
 /* --- device lifetime: replaces DN_init's buffer / program setup (voxel.c:119-154) and DN_quit (156-163) --- */

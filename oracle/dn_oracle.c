@@ -543,10 +543,14 @@ typedef struct ctx {
     int capped;
 } ctx;
 
-/* D16: a step_map call that has visited this many cells (outer plus inner iterations) ends as a miss.
- * Rays with a finite, non-zero direction component on every axis leave the map long before; only
- * degenerate rays (a zero or NaN component: 0 * inf makes a side distance NaN, after which the
- * reference's loop never ends) reach it. */
+/* D16: a segment whose direction has a zero or NaN component (its reciprocal is then infinite or NaN)
+ * traverses nothing: it ends at once as a miss.  In the reference such a ray makes a side distance NaN
+ * (0 * inf) after one step, after which no axis can step and its loops (voxelShared.comp:339, 435) never
+ * end; reflect() without an added EPSILON (voxelLighting.comp:132, 163) produces them.  A segment that
+ * has visited step_cap cells also ends as a miss: with a finite direction that bound is never reached
+ * without refraction (at most sx+sy+sz chunk cells, 24 voxel cells per chunk entered); it ends repeated
+ * refraction inside transparent voxels. */
+static inline int finite_dir(v3 inv) { return isfinite(inv.x) && isfinite(inv.y) && isfinite(inv.z); }
 static inline uint32_t step_cap(uint32_t sx, uint32_t sy, uint32_t sz)
 {
     uint64_t c = 256ull * ((uint64_t)sx + sy + sz) + 4096ull;
@@ -697,6 +701,7 @@ static int step_chunk(ctx* c, tstate* ts, iv3 mapPos, uint32_t tile, v3* rayDir,
                     v3 n = (dot3(vox->normal, *rayDir) < 0.0f) ? vnormalize(vox->normal) : *hitNormal;
                     *rayDir = vrefract(*rayDir, n, ts->lastVoxRefract / mat->refractIndex);
                     *inv = V(1.0f / rayDir->x, 1.0f / rayDir->y, 1.0f / rayDir->z);
+                    if (!finite_dir(*inv)) { c->c.degenerate++; c->capped = 1; return 0; }
                     init_dda(*rayDir, *inv, *rayPos, &pos, &delta, &step, &side);
                     lastSide = V(0.0f, 0.0f, 0.0f);
                 }
@@ -713,6 +718,7 @@ static int step_chunk(ctx* c, tstate* ts, iv3 mapPos, uint32_t tile, v3* rayDir,
                 *rayDir = vrefract(*rayDir, n, ts->lastVoxRefract);
                 if (rayDir->x == 0.0f && rayDir->y == 0.0f && rayDir->z == 0.0f) *rayDir = old;
                 *inv = V(1.0f / rayDir->x, 1.0f / rayDir->y, 1.0f / rayDir->z);
+                if (!finite_dir(*inv)) { c->c.degenerate++; c->capped = 1; return 0; }
                 init_dda(*rayDir, *inv, *rayPos, &pos, &delta, &step, &side);
                 lastSide = V(0.0f, 0.0f, 0.0f);
             }
@@ -737,6 +743,7 @@ static int step_map(ctx* c, tstate* ts, v3* rayDir, v3 inv, v3* rayPos, int igno
     c->c.rays++;
     c->segSteps = 0;
     c->capped = 0;
+    if (!finite_dir(inv)) { c->c.degenerate++; return 0; }
     const uint32_t cap = step_cap(m->sx, m->sy, m->sz);
     iv3 pos, step; v3 delta, side, lastSide = V(0.0f, 0.0f, 0.0f);
     init_dda(*rayDir, inv, *rayPos, &pos, &delta, &step, &side);
@@ -1044,6 +1051,7 @@ static void add_counters(dno_counters* d, const dno_counters* s)
     d->rays += s->rays; d->primary += s->primary; d->outerSteps += s->outerSteps;
     d->chunksEntered += s->chunksEntered; d->innerSteps += s->innerSteps; d->hits += s->hits;
     d->litVoxels += s->litVoxels;
+    d->degenerate += s->degenerate;
 }
 
 static dno_light_params fix_params(const dno_light_params* p)

@@ -189,6 +189,7 @@ typedef struct dno_counters {
     uint64_t innerSteps;      /* voxel cells visited */
     uint64_t hits;            /* voxels decompressed (H) */
     uint64_t litVoxels;       /* voxels whose lighting was computed */
+    uint64_t degenerate;      /* segments ended at once by D16 (a zero or NaN direction component) */
 } dno_counters;
 
 /* Sync: restatement of DN_sync_gpu's per-tile loop (voxel.c:719-786) with the

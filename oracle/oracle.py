@@ -42,7 +42,7 @@ class DrawParams(Structure):
 
 class Counters(Structure):
     _fields_ = [("rays", c_uint64), ("primary", c_uint64), ("outerSteps", c_uint64), ("chunksEntered", c_uint64),
-                ("innerSteps", c_uint64), ("hits", c_uint64), ("litVoxels", c_uint64)]
+                ("innerSteps", c_uint64), ("hits", c_uint64), ("litVoxels", c_uint64), ("degenerate", c_uint64)]
 
 
 class ShapeOp(Structure):

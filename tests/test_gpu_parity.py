@@ -25,7 +25,7 @@ def test_frames_match_oracle(gpu_ready, name):
         # traversal counters are exact integers on both sides
         for k_gpu, k_or in (("rays", "rays"), ("primaryRays", "primary"), ("outerSteps", "outerSteps"),
                             ("chunksEntered", "chunksEntered"), ("innerSteps", "innerSteps"), ("hits", "hits"),
-                            ("litVoxels", "litVoxels")):
+                            ("litVoxels", "litVoxels"), ("degenerate", "degenerate")):
             assert st[k_gpu] == oc[k_or], (k_gpu, st[k_gpu], oc[k_or])
         assert st["litVoxels"] > 0
     finally:
@@ -184,11 +184,11 @@ def test_camera_inside_map_and_host_image(gpu_ready):
         pair.close()
 
 
-def test_degenerate_ray_is_capped(gpu_ready):
+def test_degenerate_ray_ends_at_once(gpu_ready):
     """A primary ray whose direction has an exactly zero x component: normalize((-1e-4, 0.6, 0.8)) + EPS
-    gives x = 0 in float32, so the DDA's x side distance becomes 0 * inf = NaN after one step and the
-    reference's loop could never finish.  Both sides end it as a miss after the D16 step cap, with the
-    same pixels and the same counters."""
+    gives x = 0 in float32, so the reference's x side distance would become 0 * inf = NaN after one step and
+    its loop could never finish.  Both sides end such a segment at once as a miss (D16), with the same
+    pixels and the same counters: no cell visited, one degenerate segment per pixel."""
     import ctypes
     from doonengine_gb300 import _lib
     lib = dn.load()
@@ -225,10 +225,30 @@ def test_degenerate_ray_is_capped(gpu_ready):
         ora = pair.om.draw(s, iv, icv, ip, W, H)
         compare_draw(gpu, ora, "degenerate ray")
         st = pair.vol.stats_kind(1)
-        sx, sy, sz = pair.vol.map_size
-        cap = 256 * (sx + sy + sz) + 4096
-        assert st["outerSteps"] + st["innerSteps"] == W * H * cap, st     # every pixel's ray reached the cap
+        assert st["outerSteps"] + st["innerSteps"] == 0, st
+        assert st["degenerate"] == W * H and st["rays"] == W * H, st
+        assert (gpu[1] == 0xFFFFFFFF).all()
         img.close()
+    finally:
+        pair.close()
+
+
+def test_degenerate_lighting_segments_match_oracle(gpu_ready):
+    """Lighting segments with an exactly zero direction component occur on their own in the batched
+    workload: specular bounces (reflect() without an added EPSILON, voxelLighting.comp:132) and diffuse
+    lobe directions (163).  Map 63 of the batched workload's 64 holds one in frame 2 and three by frame 4.
+    Every frame must match the oracle, the degenerate-segment counter included (D16)."""
+    from doonengine_gb300 import configs
+    spec = configs.batched_specs(64, seed=7)[63]
+    pair = Pair("small", **spec)
+    pair.vol.s.mapId = 63
+    try:
+        for _ in range(5):
+            pair.step()
+        st = pair.vol.stats()
+        oc = pair.om.counters()
+        assert st["degenerate"] == oc["degenerate"] >= 3, (st["degenerate"], oc["degenerate"])
+        assert st["rays"] == oc["rays"] and st["outerSteps"] == oc["outerSteps"]
     finally:
         pair.close()
 
