@@ -324,7 +324,8 @@ def serving_summary(sv):
     """The serving line's figures that the headline carries: per offered rate p50 / p99 latency, achieved
     request rate and rays/s, and the highest achieved rate whose p99 stays within 33 ms."""
     rows = [{k: r.get(k) for k in ("offered_rps", "achieved_rps", "p50_ms", "p99_ms", "rays_per_s", "completed",
-                                   "drained", "evictions", "restores")} for r in sv["sweep"]]
+                                   "drained", "evictions", "restores", "evicted_gb", "restored_gb", "server_admit_s",
+                                   "server_issue_s", "device_s")} for r in sv["sweep"]]
     return {"workload": sv["config"]["workload"], "device_budget_gb": sv["config"]["device_budget_gb"],
             "offered_rps": [r["offered_rps"] for r in rows], "p50_ms": [r["p50_ms"] for r in rows],
             "p99_ms": [r["p99_ms"] for r in rows], "max_rps_p99_le_33ms": sv["max_rps_with_p99_le_33ms"],
@@ -425,7 +426,9 @@ def batched_vs_plain(args, lib, rank, pg, local, frames_warm, frames_timed, auto
         t = 1.0 + 0.25 * f
         plain_frame(t)
         batched_frame(t)
-        if f == 0 and autotune:
+        if f == frames_warm - 1 and autotune:
+            # tuned on the last warm-up frame's lighting, past the streaming ramp (the first frames light
+            # almost nothing, so timings there say nothing about the timed frames)
             tuned = batch.autotune()
             log("autotuned: %s" % tuned)
     for vol, *_ in A:
@@ -896,8 +899,15 @@ def serving_sweep(args, lib, rank, world, nmaps, rates, seconds, budget_gb, stop
                "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
                "rays_per_s": rays / el if el else None, "by_kind": by_kind,
                "ticks": st1["ticks"] - st0["ticks"], "items": st1["items"] - st0["items"],
-               "evictions": st1["evictions"] - st0["evictions"], "restores": st1["restores"] - st0["restores"]}
-        log("rate %g: %s" % (rate, {k: row[k] for k in ("completed", "achieved_rps", "p50_ms", "p99_ms", "rays_per_s")}))
+               "evictions": st1["evictions"] - st0["evictions"], "restores": st1["restores"] - st0["restores"],
+               "evicted_gb": (st1["evictedBytes"] - st0["evictedBytes"]) / 2**30,
+               "restored_gb": (st1["restoredBytes"] - st0["restoredBytes"]) / 2**30,
+               "server_admit_s": st1["admitSeconds"] - st0["admitSeconds"],
+               "server_issue_s": st1["issueSeconds"] - st0["issueSeconds"],
+               "device_s": st1["deviceSeconds"] - st0["deviceSeconds"]}
+        log("rate %g: %s" % (rate, {k: row[k] for k in ("completed", "achieved_rps", "p50_ms", "p99_ms", "rays_per_s",
+                                                       "evictions", "restores", "server_admit_s", "server_issue_s",
+                                                       "device_s")}))
         sweep.append(row)
         # past saturation the queue only grows: stop the sweep there
         if not ok or (row["achieved_rps"] or 0.0) < 0.9 * rate:

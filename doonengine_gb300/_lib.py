@@ -156,7 +156,8 @@ class DNserveConfig(Structure):
 class DNserveStats(Structure):
     _fields_ = [("submitted", c_uint64), ("completed", c_uint64), ("failed", c_uint64), ("ticks", c_uint64),
                 ("items", c_uint64), ("evictions", c_uint64), ("restores", c_uint64), ("residentBytes", c_uint64),
-                ("residentVolumes", c_uint32)]
+                ("residentVolumes", c_uint32), ("admitSeconds", c_double), ("issueSeconds", c_double),
+                ("deviceSeconds", c_double), ("evictedBytes", c_uint64), ("restoredBytes", c_uint64)]
 
 
 class DnBatchTuning(Structure):

@@ -159,6 +159,17 @@ __global__ void __launch_bounds__(128, DN_PACKET_MIN_BLOCKS) k_light_packet_batc
     packet_loop<true>(nullptr, &a, warps[threadIdx.x >> 5]);
 }
 
+// the opaque-chunk marks (mark_opaque_word) of every map of a lighting launch: block i marks map i
+__global__ void __launch_bounds__(256) k_mark_opaque_batch(const BatchLightMap* l)
+{
+    __shared__ uint32_t opq[8];
+    const BatchLightMap& e = l[blockIdx.x];
+    opaque_materials(e.mats, opq);
+    const uint64_t nwords = ((uint64_t)e.m.sx * e.m.sy * e.m.sz + 15) / 16;
+    for (uint64_t wi = threadIdx.x; wi < nwords; wi += blockDim.x)
+        mark_opaque_word(const_cast<uint32_t*>(e.m.tbits), e.m.tword, e.m.rec, wi, opq);
+}
+
 // the diffuse paths of the voxels k_light_packet_batch lit, as per-lane path streams over every map's queue
 __global__ void __launch_bounds__(128, DN_DIFF_MIN_BLOCKS) k_light_diffuse_batch(const __grid_constant__ BatchLightArgs a)
 {
@@ -338,6 +349,9 @@ struct FramePlan {
 // packets: the lighting kernel of dn_light_packet.cuh (every map's specBounceLimit within its limit)
 static int issue_light(DNgpuBatch* b, const BatchLightArgs& la, cudaStream_t s, bool packets)
 {
+    COUNT_LAUNCH();
+    k_mark_opaque_batch<<<la.nmaps, 256, 0, s>>>(la.maps);
+    CK(cudaGetLastError());
     COUNT_LAUNCH();
     if (packets) k_light_packet_batch<<<(unsigned)(g_numSMs * (int)b->tuning.blocksPerSM), 128, 0, s>>>(la);
     else k_light_stream_batch<<<(unsigned)(g_numSMs * (int)b->tuning.blocksPerSM), 128, 0, s>>>(la);

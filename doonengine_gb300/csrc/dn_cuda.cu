@@ -60,6 +60,11 @@ extern "C" const char* dn_cuda_error_string(int code)
 
 int g_device = -1;
 int g_numSMs = 0;
+bool g_asyncAlloc = false;
+// pinned host blocks kept by restored volumes for their next eviction, and the cap on their sum
+// (DN_PINNED_RETAIN_GB, default 64 GiB): within it a map's evictions after the first pin nothing
+static unsigned long long g_pinnedRetained = 0;
+static unsigned long long g_pinnedRetainMax = 64ull << 30;
 unsigned long long g_launches = 0;
 unsigned long long g_allocs = 0;
 static unsigned long long g_generation = 0;
@@ -101,6 +106,20 @@ extern "C" int dn_cuda_init(int device)
     CK(cudaSetDevice(device));
     CK(cudaFree(0));
     CK(cudaDeviceGetAttribute(&g_numSMs, cudaDevAttrMultiProcessorCount, device));
+    if (const char* e = getenv("DN_PINNED_RETAIN_GB")) g_pinnedRetainMax = (unsigned long long)(atof(e) * (1ull << 30));
+    // stream-ordered allocation for volume arrays that come and go with eviction: the device's default pool
+    // keeps what it frees (release threshold unlimited), so a restore reuses an evicted map's memory
+    // without returning to the driver, and a free does not wait for the whole device
+    int pools = 0;
+    g_asyncAlloc = false;
+    if (cudaDeviceGetAttribute(&pools, cudaDevAttrMemoryPoolsSupported, device) == cudaSuccess && pools) {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t keep = ~0ull;
+            if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) == cudaSuccess) g_asyncAlloc = true;
+        }
+    }
+    cudaGetLastError();
     g_device = device;
     noalloc_forget();
     return DN_CUDA_OK;
@@ -108,6 +127,16 @@ extern "C" int dn_cuda_init(int device)
 
 extern "C" void dn_cuda_shutdown(void) { g_device = -1; noalloc_forget(); }
 
+
+uint32_t vol_array_bit(DNgpuVolume* g, const void* field)
+{
+    const void* fields[] = {&g->tword, &g->treq, &g->tvis, &g->ttouch, &g->tbits, &g->tlast, &g->tpend, &g->tpendSlot,
+                            &g->rec, &g->nsamples, &g->vox, &g->diff, &g->spec, &g->reqs, &g->st, &g->dtab,
+                            &g->lightOut, &g->dstage, &g->dimg, &g->dhit, &g->dface};
+    for (uint32_t i = 0; i < sizeof(fields) / sizeof(fields[0]); i++)
+        if (fields[i] == field) return 1u << i;
+    return 0u;
+}
 
 static int alloc_tiles(DNgpuVolume* g)
 {
@@ -131,7 +160,8 @@ static int alloc_tiles(DNgpuVolume* g)
 
 static void free_tiles(DNgpuVolume* g)
 {
-    dfree(g->tword); dfree(g->tbits); dfree(g->treq); dfree(g->tvis); dfree(g->ttouch); dfree(g->tlast); dfree(g->tpend); dfree(g->tpendSlot);
+    vfree(g, g->tword); vfree(g, g->tbits); vfree(g, g->treq); vfree(g, g->tvis); vfree(g, g->ttouch); vfree(g, g->tlast);
+    vfree(g, g->tpend); vfree(g, g->tpendSlot);
 }
 
 extern "C" void dn_cuda_map_destroy(DNgpuVolume* g)
@@ -141,12 +171,17 @@ extern "C" void dn_cuda_map_destroy(DNgpuVolume* g)
     if (g->batch) dn_cuda_batch_remove(g->batch, g);
     if (g->stream) cudaStreamSynchronize(g->stream);
     free_tiles(g);
-    dfree(g->rec); dfree(g->nsamples); dfree(g->vox); dfree(g->diff); dfree(g->spec);
-    dfree(g->reqs); dfree(g->lightOut); dfree(g->st); dfree(g->dtab); dfree(g->dstage);
-    dfree(g->dimg); dfree(g->dhit); dfree(g->dface);
+    vfree(g, g->rec); vfree(g, g->nsamples); vfree(g, g->vox); vfree(g, g->diff); vfree(g, g->spec);
+    vfree(g, g->reqs); vfree(g, g->lightOut); vfree(g, g->st); vfree(g, g->dtab); vfree(g, g->dstage);
+    vfree(g, g->dimg); vfree(g, g->dhit); vfree(g, g->dface);
+    if (g->stream) cudaStreamSynchronize(g->stream);
     if (g->hstage) cudaFreeHost(g->hstage);
     if (g->hst) cudaFreeHost(g->hst);
     if (g->evicted) cudaFreeHost(g->evicted);
+    if (g->hostKeep) {
+        cudaFreeHost(g->hostKeep);
+        __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
+    }
     if (g->stageFree) cudaEventDestroy(g->stageFree);
     if (g->ownStream) cudaStreamDestroy(g->ownStream);
     delete g;
@@ -158,10 +193,10 @@ static int reserve_requests(DNgpuVolume* g, uint64_t cap)
     uint64_t nc = g->reqCap ? g->reqCap : 1024;
     while (nc < cap) nc *= 2;
     CK(cudaStreamSynchronize(g->stream));
-    dfree(g->reqs); dfree(g->lightOut);
+    vfree(g, g->reqs); vfree(g, g->lightOut);
     dn_new_generation(g);
     int rc;
-    if ((rc = dalloc(&g->reqs, nc)) || (rc = dalloc(&g->lightOut, nc * 64))) { g->reqCap = 0; return rc; }
+    if ((rc = valloc(g, g->reqs, nc)) || (rc = valloc(g, g->lightOut, nc * 64))) { g->reqCap = 0; return rc; }
     g->reqCap = nc;
     // the old request list is gone: nothing may be lit from it
     if (g->st) CK(cudaMemsetAsync(&g->st->w[ST_REQ], 0, 4, g->stream));
@@ -235,7 +270,7 @@ template <class T> static int grow_copy(DNgpuVolume* g, T** p, uint64_t oldCount
     if (rc) return rc;
     if (*p && oldCount) CK(cudaMemcpyAsync(np, *p, oldCount * sizeof(T), cudaMemcpyDeviceToDevice, g->stream));
     CK(cudaStreamSynchronize(g->stream));
-    dfree(*p);
+    vfree(g, *p);
     *p = np;
     dn_new_generation(g);
     return DN_CUDA_OK;
@@ -289,32 +324,59 @@ extern "C" uint64_t dn_cuda_map_footprint(DNgpuVolume* g)
 
 extern "C" int dn_cuda_map_is_resident(DNgpuVolume* g) { return g && !g->evicted; }
 
+// Eviction and restore never wait for the device.  Both run in the volume's stream order (the batch's
+// stream while the volume is a member): eviction queues the copies of the persistent arrays into the
+// volume's pinned block and then frees the arrays -- stream-ordered when they came from the pool, which is
+// where every restore puts them -- and restore queues the allocations and the copies back.  The pinned
+// block stays with the volume after a restore (up to the process-wide retention cap), so only a map's
+// first eviction pins host memory.
 extern "C" int dn_cuda_map_evict(DNgpuVolume* g)
 {
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
     if (g->evicted) return DN_CUDA_OK;
     CK(cudaSetDevice(g->device));
-    CK(cudaStreamSynchronize(g->stream));
     PersistentArray a[16];
     const int k = persistent_arrays(g, a);
     size_t total = 0;
     for (int i = 0; i < k; i++) total += align16(a[i].bytes);
+    if (!total) total = 16;
     unsigned char* h = nullptr;
-    COUNT_ALLOC();
-    CK(cudaMallocHost((void**)&h, total ? total : 1));
+    if (g->hostKeep && g->hostKeepCap >= total) {
+        h = g->hostKeep;
+        __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
+    } else {
+        if (g->hostKeep) {
+            // too small for the map as it is now: the copies a restore queued from it must finish first
+            CK(cudaStreamSynchronize(g->stream));
+            cudaFreeHost(g->hostKeep);
+            __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
+        }
+        g->hostKeep = nullptr;
+        g->hostKeepCap = 0;
+        COUNT_ALLOC();
+        CK(cudaMallocHost((void**)&h, total));
+    }
+    const size_t cap = (h == g->hostKeep) ? g->hostKeepCap : total;
+    g->hostKeep = nullptr;
+    g->hostKeepCap = 0;
     size_t o = 0;
     for (int i = 0; i < k; i++) {
         cudaError_t e = cudaMemcpyAsync(h + o, *a[i].ptr, a[i].bytes, cudaMemcpyDeviceToHost, g->stream);
-        if (e != cudaSuccess) { cudaStreamSynchronize(g->stream); cudaFreeHost(h); return dn_set_err(DN_CUDA_ERR_LAUNCH, "evict: %s", cudaGetErrorString(e)); }
+        if (e != cudaSuccess) {
+            cudaStreamSynchronize(g->stream);
+            cudaFreeHost(h);
+            return dn_set_err(DN_CUDA_ERR_LAUNCH, "evict: %s", cudaGetErrorString(e));
+        }
         o += align16(a[i].bytes);
     }
-    cudaError_t e = cudaStreamSynchronize(g->stream);
-    if (e != cudaSuccess) { cudaFreeHost(h); return dn_set_err(DN_CUDA_ERR_LAUNCH, "evict: %s", cudaGetErrorString(e)); }
-    for (int i = 0; i < k; i++) { cudaFree(*a[i].ptr); *a[i].ptr = nullptr; }
-    dfree(g->lightOut); dfree(g->dstage); dfree(g->dimg); dfree(g->dhit); dfree(g->dface);
+    // the frees follow the copies in the stream's order (a cudaFree of an array from cudaMalloc waits anyway)
+    free_tiles(g);
+    vfree(g, g->rec); vfree(g, g->nsamples); vfree(g, g->vox); vfree(g, g->diff); vfree(g, g->spec);
+    vfree(g, g->reqs); vfree(g, g->st); vfree(g, g->dtab);
+    vfree(g, g->lightOut); vfree(g, g->dstage); vfree(g, g->dimg); vfree(g, g->dhit); vfree(g, g->dface);
     g->dstageCap = 0; g->dimgCap = 0;
     g->evicted = h;
-    g->evictedBytes = total;
+    g->evictedBytes = cap;
     dn_new_generation(g);
     return DN_CUDA_OK;
 }
@@ -327,15 +389,28 @@ extern "C" int dn_cuda_map_restore(DNgpuVolume* g)
     PersistentArray a[16];
     const int k = persistent_arrays(g, a);
     int rc = DN_CUDA_OK;
-    for (int i = 0; i < k && !rc; i++) {
-        COUNT_ALLOC();
-        cudaError_t e = cudaMalloc(a[i].ptr, a[i].bytes ? a[i].bytes : 1);
-        if (e != cudaSuccess) { *a[i].ptr = nullptr; rc = dn_set_err(DN_CUDA_ERR_NOMEM, "restore: %s", cudaGetErrorString(e)); }
-    }
-    if (!rc) rc = dalloc(&g->lightOut, (size_t)g->reqCap * 64);
+    // the arrays in persistent_arrays' order, each from the pool on the volume's stream
+    rc = valloc(g, g->tword, g->ntiles);
+    if (!rc) rc = valloc(g, g->treq, g->ntiles);
+    if (!rc) rc = valloc(g, g->tvis, g->ntiles);
+    if (!rc) rc = valloc(g, g->ttouch, g->ntiles);
+    if (!rc) rc = valloc(g, g->tbits, (g->ntiles + 31) / 32 * 2);
+    if (!rc) rc = valloc(g, g->tlast, g->ntiles);
+    if (!rc) rc = valloc(g, g->tpend, g->ntiles);
+    if (!rc) rc = valloc(g, g->tpendSlot, g->ntiles);
+    if (!rc) rc = valloc(g, g->rec, g->slotCap);
+    if (!rc) rc = valloc(g, g->nsamples, g->slotCap);
+    if (!rc) rc = valloc(g, g->vox, g->voxCap);
+    if (!rc) rc = valloc(g, g->diff, g->voxCap);
+    if (!rc) rc = valloc(g, g->spec, g->voxCap);
+    if (!rc) rc = valloc(g, g->reqs, g->reqCap);
+    if (!rc) rc = valloc(g, g->st, 1);
+    if (!rc) rc = valloc(g, g->dtab, 1);
+    if (!rc) rc = valloc(g, g->lightOut, (size_t)g->reqCap * 64);
     if (rc) {
-        for (int i = 0; i < k; i++) if (*a[i].ptr) { cudaFree(*a[i].ptr); *a[i].ptr = nullptr; }
-        dfree(g->lightOut);
+        free_tiles(g);
+        vfree(g, g->rec); vfree(g, g->nsamples); vfree(g, g->vox); vfree(g, g->diff); vfree(g, g->spec);
+        vfree(g, g->reqs); vfree(g, g->st); vfree(g, g->dtab); vfree(g, g->lightOut);
         return rc;
     }
     size_t o = 0;
@@ -343,8 +418,17 @@ extern "C" int dn_cuda_map_restore(DNgpuVolume* g)
         CK(cudaMemcpyAsync(*a[i].ptr, g->evicted + o, a[i].bytes, cudaMemcpyHostToDevice, g->stream));
         o += align16(a[i].bytes);
     }
-    CK(cudaStreamSynchronize(g->stream));
-    cudaFreeHost(g->evicted);
+    // keep the pinned block for the next eviction when the retention cap allows it; otherwise free it once
+    // the copies have read it
+    const unsigned long long cap = g->evictedBytes;
+    if (__atomic_add_fetch(&g_pinnedRetained, cap, __ATOMIC_RELAXED) <= g_pinnedRetainMax) {
+        g->hostKeep = g->evicted;
+        g->hostKeepCap = (size_t)cap;
+    } else {
+        __atomic_fetch_sub(&g_pinnedRetained, cap, __ATOMIC_RELAXED);
+        CK(cudaStreamSynchronize(g->stream));
+        cudaFreeHost(g->evicted);
+    }
     g->evicted = nullptr;
     g->evictedBytes = 0;
     dn_new_generation(g);
@@ -417,6 +501,16 @@ __global__ void __launch_bounds__(128, DN_PACKET_MIN_BLOCKS) k_light_packet(cons
     packet_loop<false>(&a, nullptr, warps[threadIdx.x >> 5]);
 }
 
+// the opaque-chunk marks of one map for a lighting launch with the given materials (mark_opaque_word)
+__global__ void __launch_bounds__(256) k_mark_opaque(uint32_t* tbits, const uint32_t* tword, const ChunkRec* rec,
+                                                     uint64_t nwords, const __grid_constant__ MaterialTable t)
+{
+    __shared__ uint32_t opq[8];
+    opaque_materials(t.m, opq);
+    for (uint64_t wi = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; wi < nwords; wi += (uint64_t)gridDim.x * blockDim.x)
+        mark_opaque_word(tbits, tword, rec, wi, opq);
+}
+
 // The diffuse paths of the voxels k_light_packet lit, as per-lane path streams over the whole request list:
 // a lane whose voxel's paths are done takes the next voxel, so no lane waits for another lane's long path.
 __global__ void __launch_bounds__(128, DN_DIFF_MIN_BLOCKS) k_light_diffuse(const __grid_constant__ StreamArgs a)
@@ -431,12 +525,21 @@ __global__ void __launch_bounds__(128, DN_DIFF_MIN_BLOCKS) k_light_diffuse(const
 static int launch_light(DNgpuVolume* g, StreamArgs& a)
 {
     int perSM = 0;
+    MaterialTable table;                // on the stack: a launch argument, copied at the launch
+    memcpy(table.m, a.mats, sizeof(table.m));
+    {
+        const uint64_t nwords = (g->ntiles + 15) / 16;
+        const uint64_t blocks = (nwords + 255) / 256;
+        const uint32_t maxBlocks = (uint32_t)(g->numSMs > 0 ? g->numSMs * 4 : 512);
+        COUNT_LAUNCH();
+        k_mark_opaque<<<(uint32_t)(blocks < maxBlocks ? blocks : maxBlocks), 256, 0, g->stream>>>(
+            g->tbits, g->tword, g->rec, nwords, table);
+        CK(cudaGetLastError());
+    }
     if (g_lightKernel == 2 && a.p.specBounceLimit <= PK_MAX_SPEC_SEGMENTS) {
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_packet, 128, 0));
         if (perSM < 1) perSM = 1;
         a.batch = g_packetBatch;
-        MaterialTable table;            // on the stack: a launch argument, copied at the launch
-        memcpy(table.m, a.mats, sizeof(table.m));
         a.gtab = g->dtab;
         COUNT_LAUNCH();
         k_light_tables<<<1, 256, 0, g->stream>>>(table, a.p, g->dtab);
@@ -495,15 +598,23 @@ __global__ void k_sync_stage(const dn_tile_op* ops, uint32_t nops, const dn_chun
         ChunkRec* dst = &rec[op.slot];
         const uint32_t* s32 = (const uint32_t*)&src;
         uint32_t* d32 = (uint32_t*)dst;
+        __shared__ uint32_t mats[8];
+        if (threadIdx.x < 8) mats[threadIdx.x] = 0;
+        __syncthreads();
         if (threadIdx.x < 24) d32[threadIdx.x] = s32[threadIdx.x];
         if (threadIdx.x == 0) nsamples[op.slot] = 0;
         const uint64_t off = voxOff[op.recordIndex];
         for (uint32_t i = threadIdx.x; i < src.nvox; i += blockDim.x) {
             const uint64_t d = (uint64_t)src.voxBase + i;
-            vox[d] = make_uint2(words[2 * (off + i)], words[2 * (off + i) + 1]);
+            const uint32_t nw = words[2 * (off + i)];
+            vox[d] = make_uint2(nw, words[2 * (off + i) + 1]);
             diff[d] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             spec[d] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            atomicOr(&mats[(nw >> 24) >> 5], 1u << ((nw >> 24) & 31u));
         }
+        __syncthreads();
+        if (threadIdx.x < 8) dst->matSet[threadIdx.x] = mats[threadIdx.x];
+        __syncthreads();
     }
 }
 
@@ -541,9 +652,9 @@ int dn_stage_ops(DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops, const dn_
         }
         if (total > g->dstageCap) {
             CK(cudaStreamSynchronize(g->stream));
-            dfree(g->dstage);
+            vfree(g, g->dstage);
             size_t nc = total + total / 2 + 4096;
-            int rc = dalloc(&g->dstage, nc);
+            int rc = valloc(g, g->dstage, nc);
             if (rc) { g->dstageCap = 0; return rc; }
             g->dstageCap = nc;
         }
@@ -734,10 +845,10 @@ int dn_reserve_image_staging(DNgpuVolume* g, size_t n)
 {
     if (n <= g->dimgCap) return DN_CUDA_OK;
     CK(cudaStreamSynchronize(g->stream));
-    dfree(g->dimg); dfree(g->dhit); dfree(g->dface);
+    vfree(g, g->dimg); vfree(g, g->dhit); vfree(g, g->dface);
     dn_new_generation(g);
     int rc;
-    if ((rc = dalloc(&g->dimg, n)) || (rc = dalloc(&g->dhit, n)) || (rc = dalloc(&g->dface, n))) { g->dimgCap = 0; return rc; }
+    if ((rc = valloc(g, g->dimg, n)) || (rc = valloc(g, g->dhit, n)) || (rc = valloc(g, g->dface, n))) { g->dimgCap = 0; return rc; }
     g->dimgCap = n;
     return DN_CUDA_OK;
 }
@@ -1020,8 +1131,8 @@ extern "C" int dn_cuda_flush_l2(void* stream, size_t bytes)
 
 extern "C" const char* dn_cuda_kernel_names(void)
 {
-    return "k_draw;k_light_stream;k_light_packet;k_light_diffuse;k_light_tables;k_commit;k_sync_stage;k_compact;k_clamp_requests;k_flush;"
-           "k_draw_batch;k_compact_batch;k_batch_reset;k_batch_prep;k_light_stream_batch;k_light_packet_batch;k_light_diffuse_batch;"
-           "k_commit_batch;k_batch_gather;"
+    return "k_draw;k_light_stream;k_light_packet;k_light_diffuse;k_light_tables;k_mark_opaque;k_commit;k_sync_stage;k_compact;k_clamp_requests;k_flush;"
+           "k_draw_batch;k_compact_batch;k_batch_reset;k_batch_prep;k_mark_opaque_batch;k_light_stream_batch;k_light_packet_batch;"
+           "k_light_diffuse_batch;k_commit_batch;k_batch_gather;"
            "k_shape_count;k_shape_write";
 }

@@ -126,14 +126,15 @@ __device__ __forceinline__ f3 sphere_hash(uint32_t key, uint32_t stream, uint32_
 
 // ------------------------------------------------------------ map layout
 
-// chunk record, 128 B: occupancy mask (bit x + 8*(y + 8*z)), partial counts, voxel count, position, pool base
+// chunk record, 128 B: occupancy mask (bit x + 8*(y + 8*z)), partial counts, voxel count, position, pool base,
+// and the set of materials its voxels use (bit m of matSet[m >> 5]; written when the chunk is staged)
 struct __align__(128) ChunkRec {
     uint32_t mask[16];
     uint32_t partial[3];
     uint32_t nvox;
     int32_t pos[3];
     uint32_t voxBase;
-    uint32_t pad[8];
+    uint32_t matSet[8];
 };
 
 struct Material {             // 32 B, DNmaterial

@@ -66,7 +66,14 @@ struct DNgpuVolume {
     int numSMs;
     // eviction: every persistent device array copied to one pinned host block, device arrays freed
     unsigned char* evicted; size_t evictedBytes;
+    // the pinned block of the last restore, kept for the next eviction (within the process-wide retention cap)
+    unsigned char* hostKeep; size_t hostKeepCap;
+    // arrays allocated from the device's stream-ordered pool (bit per array, vol_array_bit): freed with
+    // cudaFreeAsync on the volume's stream instead of cudaFree (which waits for the whole device)
+    uint32_t poolMask;
 };
+
+
 
 extern int g_device;
 extern int g_numSMs;
@@ -87,6 +94,37 @@ template <class T> static int dalloc(T** p, size_t count)
     return DN_CUDA_OK;
 }
 template <class T> static void dfree(T*& p) { if (p) cudaFree(p); p = nullptr; }
+
+// the bit of one of the volume's device arrays (its field address) in poolMask; 0 for other pointers
+uint32_t vol_array_bit(DNgpuVolume* g, const void* field);
+extern bool g_asyncAlloc;               // the device supports stream-ordered allocation (cudaMallocAsync)
+
+// frees one of the volume's device arrays: stream-ordered on the volume's stream when it came from the pool
+template <class T> static void vfree(DNgpuVolume* g, T*& p)
+{
+    if (!p) return;
+    const uint32_t bit = vol_array_bit(g, &p);
+    if (bit && (g->poolMask & bit)) cudaFreeAsync(p, g->stream);
+    else cudaFree(p);
+    g->poolMask &= ~bit;
+    p = nullptr;
+}
+// allocates one of the volume's device arrays from the stream-ordered pool, ordered on the volume's stream
+// (work issued afterwards on that stream may use it)
+template <class T> static int valloc(DNgpuVolume* g, T*& p, size_t count)
+{
+    p = nullptr;
+    if (count == 0) count = 1;
+    const uint32_t bit = vol_array_bit(g, &p);
+    COUNT_ALLOC();
+    if (g_asyncAlloc && bit) {
+        CK(cudaMallocAsync((void**)&p, count * sizeof(T), g->stream));
+        g->poolMask |= bit;
+    } else {
+        CK(cudaMalloc((void**)&p, count * sizeof(T)));
+    }
+    return DN_CUDA_OK;
+}
 
 static inline dn::DevMap dev_map(const DNgpuVolume* g)
 {
@@ -135,6 +173,41 @@ __device__ __forceinline__ void flush_counters(unsigned long long* stats, const 
 #pragma unroll
         for (int k = 0; k < 7; k++) if (v[k]) atomicAdd(&stats[k], (unsigned long long)v[k]);
     }
+}
+
+// ------------------------------------------------- opaque chunks of a lighting launch
+
+// The lighting step (seg_step) reads the 2-bit tile map; before each lighting launch a loaded chunk whose
+// voxels all use materials that are opaque under the launch's materials is marked 3 instead of 2.  A ray
+// that reaches an occupied voxel of such a chunk ends there without reading the voxel's word and material
+// (its pool index is formed when the segment is shaded).  The next sync rewrites the map with 0 / 1 / 2.
+
+// opq[8] (shared memory): bit m set when material m is opaque (opacity exactly 1, voxelShared.comp:360)
+__device__ __forceinline__ void opaque_materials(const dn::Material* mats, uint32_t* opq)
+{
+    if (threadIdx.x < 8) opq[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint32_t m = threadIdx.x; m < 256; m += blockDim.x)
+        if (mats[m].opacity == 1.0f) atomicOr(&opq[m >> 5], 1u << (m & 31u));
+    __syncthreads();
+}
+
+// word wi of the map's 2-bit tile map (16 tiles): every loaded tile to 3 (all materials opaque) or 2
+__device__ __forceinline__ void mark_opaque_word(uint32_t* tbits, const uint32_t* tword, const dn::ChunkRec* rec,
+                                                 uint64_t wi, const uint32_t* opq)
+{
+    const uint32_t w = tbits[wi];
+    uint32_t out = w;
+    for (uint32_t k = 0; k < 16; k++) {
+        if (((w >> (2 * k)) & 2u) == 0u) continue;
+        const uint32_t slot = __ldg(&tword[wi * 16 + k]) & dn::SLOT_MASK;
+        const uint32_t* ms = rec[slot].matSet;
+        uint32_t other = 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) other |= __ldg(&ms[j]) & ~opq[j];
+        out = (out & ~(3u << (2 * k))) | ((other ? 2u : 3u) << (2 * k));
+    }
+    if (out != w) tbits[wi] = out;
 }
 
 // ------------------------------------------------------------------ draw

@@ -283,7 +283,7 @@ __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLi
                     f3 sc = mk(0.0f, 0.0f, 0.0f);
                     if (hs == 1u) {
                         Voxel hv;
-                        decompress(m, hitIdx, hv);
+                        decompress(m, hit_index(s, hitIdx), hv);
                         const i3 hp{f2i(truncf(s.pos.x)), f2i(truncf(s.pos.y)), f2i(truncf(s.pos.z))};
                         if (in_map(m, hp)) {
                             uint8_t* vp = &m.tvis[map_index(m, hp)];

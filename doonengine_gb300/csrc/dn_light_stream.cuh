@@ -69,9 +69,10 @@ struct Seg {
     f3 cside, oside, cp;
     float clastMin, olastMin;
     const ChunkRec* rec;
-    uint32_t base;
     uint32_t flags;      // bit0 inner level, bit1 ignore (current level), bit2 saved outer ignore, bit3 requested,
-                         // bit4 degenerate direction (D16), bits 8-31 cells visited by the segment (D16 cell cap)
+                         // bit4 degenerate direction (D16), bit5 the current chunk's materials are all opaque,
+                         // bit6 the segment ended on a voxel of such a chunk (hitIdx holds its local index),
+                         // bits 8-31 cells visited by the segment (D16 cell cap)
     f3 cadd;
     float cmul;
     TState ts;
@@ -94,9 +95,12 @@ __device__ __forceinline__ void seg_begin(Seg& s, f3 pos, f3 dir, f3 inv)
 }
 
 // Advances one traversal step.  Returns 0 while the segment continues, 1 on an opaque hit (s.pos moved to
-// the hit, hitIdx = pool index of the voxel), 2 when it leaves the map.  The common case (a chunk cell that
-// is not loaded, or a voxel cell that is empty) runs one code path for both levels; entering a chunk, leaving
-// it, reaching a voxel and leaving the map are the divergent events.
+// the hit; hitIdx = pool index of the voxel, or its local index in s.rec when flags bit 6 is set -- hit_index()
+// gives the pool index), 2 when it leaves the map.  The common case (a chunk cell that is not loaded, or a
+// voxel cell that is empty) runs one code path for both levels; entering a chunk, leaving it, reaching a voxel
+// and leaving the map are the divergent events.  In a chunk marked 3 in the tile map (every material of its
+// voxels opaque under the launch's materials, mark_opaque_word) the first occupied voxel ends the ray without
+// its word, rank or material being read: the reference would find it opaque (voxelShared.comp:360-364).
 __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Material* mats, const float* sunStrength,
                                              Counters& c, uint32_t& hitIdx)
 {
@@ -118,7 +122,7 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
     // brings either to the low bits (cst is only read at the chunk level)
     const uint32_t bits = w >> (inner ? (idx & 31u) : ((idx & 15u) << 1));
     const uint32_t cst = bits & 3u;
-    const bool occ = inb && (inner ? (((bits & 1u) != 0u) && !(s.flags & 2u)) : (cst == 2u));
+    const bool occ = inb && (inner ? (((bits & 1u) != 0u) && !(s.flags & 2u)) : (cst >= 2u));
     if (!inb || occ) {
         if (!inner) {
             if (!inb) {
@@ -144,8 +148,8 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
             s.cside.z = (sg.z * ((float)s.cpos.z - cp.z) + sg.z * 0.5f + 0.5f) * delta.z;
             s.clastMin = 0.0f;
             s.rec = &m.rec[__ldg(&m.tword[idx]) & SLOT_MASK];
-            s.base = __ldg(&s.rec->voxBase);
-            s.flags = (s.flags & ~4u) | 1u | ((s.flags & 2u) << 1);   // inner level; the chunk inherits ignoreFirst
+            // inner level; the chunk inherits ignoreFirst; bit5: the chunk is marked opaque
+            s.flags = (s.flags & ~(4u | 32u)) | 1u | ((s.flags & 2u) << 1) | (cst == 3u ? 32u : 0u);
             return 0u;
         }
         if (!inb) {
@@ -155,7 +159,15 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
         } else {
             c.inner++;
             c.hits++;
-            const uint32_t vi = s.base + vox_rank(s.rec, idx);
+            if (s.flags & 32u) {
+                const float t = s.clastMin + EPS;
+                const f3 cp = add(s.cp, muls(s.dir, t));
+                s.pos = add(mk((float)s.opos.x, (float)s.opos.y, (float)s.opos.z), muls(cp, INV_CHUNK));
+                hitIdx = idx;
+                s.flags |= 64u;
+                return 1u;
+            }
+            const uint32_t vi = __ldg(&s.rec->voxBase) + vox_rank(s.rec, idx);
             const uint2 vw = __ldg(&m.vox[vi]);
             const uint32_t material = vw.x >> 24;
             const Material& mat = mats[material];
@@ -206,6 +218,12 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
 }
 
 __device__ __forceinline__ f3 rcp3(f3 d) { return mk(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z)); }
+
+// the pool index of the voxel a segment ended on (seg_step's hitIdx)
+__device__ __forceinline__ uint32_t hit_index(const Seg& s, uint32_t hitIdx)
+{
+    return (s.flags & 64u) ? __ldg(&s.rec->voxBase) + vox_rank(s.rec, hitIdx) : hitIdx;
+}
 
 // per-lane job state of the voxel being lit
 struct Job {
@@ -276,7 +294,7 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
         const bool hit = hitState == 1u;
         hitState = 0;
         Voxel hv;
-        if (hit) decompress(m, hitIdx, hv);
+        if (hit) decompress(m, hit_index(s, hitIdx), hv);
         if (j.phase == PH_SPEC) {
             // specular_ray body after step_map (voxelLighting.comp:98-144)
             bool done = true;

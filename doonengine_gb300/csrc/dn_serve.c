@@ -41,6 +41,7 @@ typedef struct VolumeSlot
 typedef struct Tick
 {
 	void* event;
+	void* started;          /* recorded before the tick's evictions, restores and launches */
 	Pending** reqs;
 	size_t nreqs, cap;
 	unsigned int* vols;
@@ -109,7 +110,8 @@ DNserver* DN_server_create(const DNserveConfig* cfg)
 	s->batch = DN_batch_create();
 	if (!s->batch) { free(s); return NULL; }
 	for (int i = 0; i < 2; i++)
-		if (dn_cuda_event_create(&s->ticks[i].event) != DN_CUDA_OK) {
+		if (dn_cuda_event_create(&s->ticks[i].event) != DN_CUDA_OK ||
+		    dn_cuda_event_create(&s->ticks[i].started) != DN_CUDA_OK) {
 			DN_batch_destroy(s->batch);
 			free(s);
 			return NULL;
@@ -211,9 +213,11 @@ static bool enforce_budget(DNserver* s, uint64_t extra, const uint8_t* inTick)
 			if (victim < 0 || c->lastTick < s->slots[victim].lastTick) victim = (int)i;
 		}
 		if (victim < 0) return false;
+		const uint64_t bytes = dn_cuda_map_footprint(s->slots[victim].vol->gpu);
 		if (dn_cuda_map_evict(s->slots[victim].vol->gpu) != DN_CUDA_OK) return false;
 		s->slots[victim].resident = 0;
 		s->stats.evictions++;
+		s->stats.evictedBytes += bytes;
 		used = resident_bytes(s, NULL);
 	}
 	return true;
@@ -233,6 +237,7 @@ static bool admit(DNserver* s, unsigned int v, const uint8_t* inTick)
 	if (dn_cuda_map_restore(slot->vol->gpu) != DN_CUDA_OK) return false;
 	slot->resident = 1;
 	s->stats.restores++;
+	s->stats.restoredBytes += dn_cuda_map_footprint(slot->vol->gpu);
 	return true;
 }
 
@@ -280,9 +285,11 @@ static int launch_tick(DNserver* s)
 	sort_candidates(s, s->order, nc);
 	uint8_t* inTick = (uint8_t*)calloc(s->nslots, 1);
 	if (!inTick) return 0;
+	Tick* t = &s->ticks[(s->tickHead + s->tickCount) % 2];
+	const double t0 = DN_server_clock();
+	dn_cuda_event_record(t->started, DN_batch_stream(s->batch));
 	/* volumes grow as they stage chunks: bring the resident set back under the budget first */
 	enforce_budget(s, 0, inTick);
-	Tick* t = &s->ticks[(s->tickHead + s->tickCount) % 2];
 	t->nreqs = 0;
 	t->nvols = 0;
 	size_t nitems = 0;
@@ -339,12 +346,19 @@ static int launch_tick(DNserver* s)
 		nitems++;
 	}
 	free(inTick);
-	if (!nitems) return 0;
+	const double t1 = DN_server_clock();
+	s->stats.admitSeconds += t1 - t0;
+	if (!nitems) {
+		/* nothing ran; the start event may have been recorded: close the (empty) interval */
+		dn_cuda_event_record(t->event, DN_batch_stream(s->batch));
+		return 0;
+	}
 	s->tickNo++;
 	s->stats.ticks++;
 	s->stats.items += nitems;
 	int ok = DN_batch_run(s->batch, s->items, (unsigned int)nitems) ? 1 : 0;
 	if (ok && dn_cuda_event_record(t->event, DN_batch_stream(s->batch)) != DN_CUDA_OK) ok = 0;
+	s->stats.issueSeconds += DN_server_clock() - t1;
 	s->tickCount++;
 	if (!ok) {
 		/* the tick's requests fail; make the event fire now so the completion path retires them */
@@ -367,6 +381,8 @@ static int retire_tick(DNserver* s, int block)
 		return 0;
 	}
 	const double now = DN_server_clock();
+	float ms = 0.0f;
+	if (dn_cuda_event_elapsed_ms(t->started, t->event, &ms) == DN_CUDA_OK) s->stats.deviceSeconds += ms * 1e-3;
 	pthread_mutex_lock(&s->lock);
 	if (grow((void**)&s->done, &s->doneCap, s->ndone + t->nreqs, sizeof(DNcompletion))) {
 		for (size_t i = 0; i < t->nreqs; i++) {
@@ -523,6 +539,7 @@ void DN_server_destroy(DNserver* s)
 		free(s->ticks[i].reqs);
 		free(s->ticks[i].vols);
 		dn_cuda_event_destroy(s->ticks[i].event);
+		dn_cuda_event_destroy(s->ticks[i].started);
 	}
 	for (unsigned int i = 0; i < s->nslots; i++) {
 		/* volumes go back to the caller resident and out of the server's batch */

@@ -81,6 +81,11 @@ typedef struct DNserveStats
 	uint64_t evictions, restores;
 	uint64_t residentBytes;
 	unsigned int residentVolumes;
+	/* where the time goes: the serving thread's residency decisions (evictions and restores issued) and
+	 * tick issue (DN_batch_run), the device time of retired ticks (restore / evict copies included), and
+	 * the bytes evicted and restored */
+	double admitSeconds, issueSeconds, deviceSeconds;
+	uint64_t evictedBytes, restoredBytes;
 } DNserveStats;
 
 DNserver* DN_server_create(const DNserveConfig* config);
