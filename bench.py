@@ -325,7 +325,8 @@ def serving_summary(sv):
     request rate and rays/s, and the highest achieved rate whose p99 stays within 33 ms."""
     rows = [{k: r.get(k) for k in ("offered_rps", "achieved_rps", "p50_ms", "p99_ms", "rays_per_s", "completed",
                                    "drained", "evictions", "restores", "evicted_gb", "restored_gb", "server_admit_s",
-                                   "server_issue_s", "device_s")} for r in sv["sweep"]]
+                                   "server_evict_s", "server_restore_s", "server_issue_s", "device_s")}
+            for r in sv["sweep"]]
     return {"workload": sv["config"]["workload"], "device_budget_gb": sv["config"]["device_budget_gb"],
             "offered_rps": [r["offered_rps"] for r in rows], "p50_ms": [r["p50_ms"] for r in rows],
             "p99_ms": [r["p99_ms"] for r in rows], "max_rps_p99_le_33ms": sv["max_rps_with_p99_le_33ms"],
@@ -598,10 +599,14 @@ def run_streaming(args):
         lib.dn_scene_reroll(vol.ptr, sel.ctypes.data, n, seed * 7919 + f, 14)
         return n, time.perf_counter() - h0
 
+    host_sync = [0.0]
+
     def gpu_frame(f):
         v, p = vol.view_proj(H / W)
         vol.draw(img, v, p)
-        vol.sync(dn.DN_READ_WRITE, split)
+        h0 = time.perf_counter()
+        vol.sync(dn.DN_READ_WRITE, split)          # host part: pack the edited chunks, stage one upload
+        host_sync[0] += time.perf_counter() - h0
         vol.update_lighting(1, 1000, 1.0 + 0.25 * f)
 
     for f in range(args.warmup):
@@ -622,6 +627,7 @@ def run_streaming(args):
     clocks.start()
     t0 = time.perf_counter()
     host_edit_s, edited = 0.0, 0
+    host_sync[0] = 0.0
     for k in range(K):
         f = args.warmup + k
         n, hs = edit_and_camera(f)
@@ -659,6 +665,10 @@ def run_streaming(args):
         "lit_voxels_per_s": allreduce_sum(pg, st["litVoxels"]) / (dev_ms_max / 1e3),
         "primary_rays_per_s": allreduce_sum(pg, st["primaryRays"]) / (dev_ms_max / 1e3),
         "chunks_edited_per_step": edited / K, "host_edit_ms_per_step": host_edit_s * 1e3 / K,
+        "host_sync_ms_per_step": host_sync[0] * 1e3 / K,
+        "host_edit_note": "host_edit: the workload generating its edits (dn_scene_reroll re-rolls the voxels of the "
+                          "chosen chunks through the edit API); host_sync: DN_sync_gpu's host part (packing of the "
+                          "edited chunks, pool ranges, one pinned upload)",
         "wall_ms_per_step": wall * 1e3 / K, "build_s": build_s,
         "gpu_launches": int(allreduce_sum(pg, launches)), "clocks": clk,
     }
@@ -904,10 +914,12 @@ def serving_sweep(args, lib, rank, world, nmaps, rates, seconds, budget_gb, stop
                "restored_gb": (st1["restoredBytes"] - st0["restoredBytes"]) / 2**30,
                "server_admit_s": st1["admitSeconds"] - st0["admitSeconds"],
                "server_issue_s": st1["issueSeconds"] - st0["issueSeconds"],
+               "server_evict_s": st1["evictSeconds"] - st0["evictSeconds"],
+               "server_restore_s": st1["restoreSeconds"] - st0["restoreSeconds"],
                "device_s": st1["deviceSeconds"] - st0["deviceSeconds"]}
         log("rate %g: %s" % (rate, {k: row[k] for k in ("completed", "achieved_rps", "p50_ms", "p99_ms", "rays_per_s",
-                                                       "evictions", "restores", "server_admit_s", "server_issue_s",
-                                                       "device_s")}))
+                                                       "evictions", "restores", "server_admit_s", "server_evict_s",
+                                                       "server_restore_s", "server_issue_s", "device_s")}))
         sweep.append(row)
         # past saturation the queue only grows: stop the sweep there
         if not ok or (row["achieved_rps"] or 0.0) < 0.9 * rate:

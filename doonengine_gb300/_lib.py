@@ -157,12 +157,14 @@ class DNserveStats(Structure):
     _fields_ = [("submitted", c_uint64), ("completed", c_uint64), ("failed", c_uint64), ("ticks", c_uint64),
                 ("items", c_uint64), ("evictions", c_uint64), ("restores", c_uint64), ("residentBytes", c_uint64),
                 ("residentVolumes", c_uint32), ("admitSeconds", c_double), ("issueSeconds", c_double),
-                ("deviceSeconds", c_double), ("evictedBytes", c_uint64), ("restoredBytes", c_uint64)]
+                ("deviceSeconds", c_double), ("evictedBytes", c_uint64), ("restoredBytes", c_uint64),
+                ("evictSeconds", c_double), ("restoreSeconds", c_double)]
 
 
 class DnBatchTuning(Structure):
     """dn_batch_tuning of include/dn_cuda.h"""
-    _fields_ = [("streamBatch", c_uint32), ("blocksPerSM", c_uint32), ("useGraph", c_uint32), ("kernel", c_uint32)]
+    _fields_ = [("streamBatch", c_uint32), ("blocksPerSM", c_uint32), ("useGraph", c_uint32), ("kernel", c_uint32),
+                ("poolRays", c_uint32), ("diffuseBatch", c_uint32)]
 
 # (name, restype, argtypes)
 _SIGS = [
@@ -325,6 +327,7 @@ _SIGS = [
     ("dn_cuda_map_is_resident", c_int, [c_void_p]),
     ("dn_cuda_map_evict", c_int, [c_void_p]),
     ("dn_cuda_map_restore", c_int, [c_void_p]),
+    ("dn_cuda_map_reserve_host", c_int, [c_void_p]),
     ("dn_cuda_event_query", c_int, [c_void_p]),
     ("dn_cuda_kernel_names", c_char_p, []),
     ("dn_cuda_launch_count", c_uint64, []),

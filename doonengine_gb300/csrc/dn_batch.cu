@@ -153,10 +153,13 @@ __global__ void __launch_bounds__(128, DN_STREAM_MIN_BLOCKS) k_light_stream_batc
     stream_loop<true>(nullptr, &a, nullptr, jobs[threadIdx.x]);
 }
 
+// POOL: rays per fan kind per pool (the rays a warp pulls from a request group at a time); the autotuner
+// picks 64 or 128 (dn_batch_tuning.poolRays)
+template <uint32_t POOL>
 __global__ void __launch_bounds__(128, DN_PACKET_MIN_BLOCKS) k_light_packet_batch(const __grid_constant__ BatchLightArgs a)
 {
-    __shared__ PacketWarp warps[4];
-    packet_loop<true>(nullptr, &a, warps[threadIdx.x >> 5]);
+    __shared__ PacketWarpT<POOL> warps[4];
+    packet_loop<true, POOL>(nullptr, &a, warps[threadIdx.x >> 5]);
 }
 
 // the opaque-chunk marks (mark_opaque_word) of every map of a lighting launch: block i marks map i
@@ -221,6 +224,7 @@ extern "C" int dn_cuda_batch_create(DNgpuBatch** out)
     b->tuning.kernel = g_lightKernel == 2 ? 2u : 1u;
     b->tuning.streamBatch = b->tuning.kernel == 2u ? g_packetBatch : g_streamBatch;
     b->tuning.blocksPerSM = DN_STREAM_MIN_BLOCKS; b->tuning.useGraph = 1;
+    b->tuning.poolRays = PK_POOL_FAN; b->tuning.diffuseBatch = g_streamBatch;
     b->lastPackets = false;
     b->graph = nullptr;
     b->lastLightValid = false;
@@ -246,7 +250,7 @@ extern "C" int dn_cuda_batch_create(DNgpuBatch** out)
     if (!rc) {
         int perSM = 0, perSM2 = 0, perSM3 = 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_stream_batch, 128, 0);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM2, k_light_packet_batch, 128, 0);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM2, k_light_packet_batch<128>, 128, 0);
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM3, k_light_diffuse_batch, 128, 0);
         if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "occupancy: %s", cudaGetErrorString(e));
         b->maxBlocksPerSM = perSM < 1 ? 1 : perSM;
@@ -353,13 +357,15 @@ static int issue_light(DNgpuBatch* b, const BatchLightArgs& la, cudaStream_t s, 
     k_mark_opaque_batch<<<la.nmaps, 256, 0, s>>>(la.maps);
     CK(cudaGetLastError());
     COUNT_LAUNCH();
-    if (packets) k_light_packet_batch<<<(unsigned)(g_numSMs * (int)b->tuning.blocksPerSM), 128, 0, s>>>(la);
-    else k_light_stream_batch<<<(unsigned)(g_numSMs * (int)b->tuning.blocksPerSM), 128, 0, s>>>(la);
+    const unsigned grid = (unsigned)(g_numSMs * (int)b->tuning.blocksPerSM);
+    if (packets && b->tuning.poolRays == 64u) k_light_packet_batch<64><<<grid, 128, 0, s>>>(la);
+    else if (packets) k_light_packet_batch<128><<<grid, 128, 0, s>>>(la);
+    else k_light_stream_batch<<<grid, 128, 0, s>>>(la);
     CK(cudaGetLastError());
     if (packets) {
         // the diffuse paths: a second pass over the same queue
         BatchLightArgs ld = la;
-        ld.batch = g_streamBatch;
+        ld.batch = b->tuning.diffuseBatch;
         CK(cudaMemsetAsync(la.workCounter, 0, 4, s));
         COUNT_LAUNCH();
         k_light_diffuse_batch<<<(unsigned)(g_numSMs * b->maxBlocksDiffuse), 128, 0, s>>>(ld);
@@ -690,6 +696,8 @@ extern "C" int dn_cuda_batch_set_tuning(DNgpuBatch* b, const dn_batch_tuning* t)
     if (!b || !t) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (t->streamBatch < 1 || t->streamBatch > 32) return dn_set_err(DN_CUDA_ERR_ARG, "streamBatch %u", t->streamBatch);
     if (t->kernel != 1u && t->kernel != 2u) return dn_set_err(DN_CUDA_ERR_ARG, "kernel %u (1 streams, 2 packets)", t->kernel);
+    if (t->poolRays != 64u && t->poolRays != 128u) return dn_set_err(DN_CUDA_ERR_ARG, "poolRays %u (64 or 128)", t->poolRays);
+    if (t->diffuseBatch < 1 || t->diffuseBatch > 32) return dn_set_err(DN_CUDA_ERR_ARG, "diffuseBatch %u", t->diffuseBatch);
     const int maxBlocks = t->kernel == 2u ? b->maxBlocksPacket : b->maxBlocksPerSM;
     if (t->blocksPerSM < 1 || (int)t->blocksPerSM > maxBlocks)
         return dn_set_err(DN_CUDA_ERR_ARG, "blocksPerSM %u (1..%d)", t->blocksPerSM, maxBlocks);
@@ -768,6 +776,12 @@ extern "C" int dn_cuda_batch_autotune(DNgpuBatch* b, dn_batch_tuning* chosen)
     }
     const uint32_t batches[] = {4u, 8u, 12u, 16u, 20u, 24u, 28u, 32u};
     for (uint32_t sb : batches) { dn_batch_tuning t = best; t.streamBatch = sb; if (!rc) trial(t); }
+    if (best.kernel == 2u && packetsOk) {
+        // rays a warp pulls per pool, then the diffuse kernel's refill threshold
+        { dn_batch_tuning t = best; t.poolRays = best.poolRays == 128u ? 64u : 128u; if (!rc) trial(t); }
+        const uint32_t dbatches[] = {8u, 12u, 16u, 20u, 24u, 28u};
+        for (uint32_t db : dbatches) { dn_batch_tuning t = best; t.diffuseBatch = db; if (!rc) trial(t); }
+    }
     const uint32_t bpsMax = (uint32_t)(best.kernel == 2u ? b->maxBlocksPacket : b->maxBlocksPerSM);
     for (uint32_t bps = 2; bps <= bpsMax && bps <= 8; bps++) {
         dn_batch_tuning t = best; t.blocksPerSM = bps; if (!rc) trial(t);

@@ -143,10 +143,10 @@ static int alloc_tiles(DNgpuVolume* g)
     uint64_t n = g->ntiles;
     int rc;
     dn_new_generation(g);
-    if ((rc = dalloc(&g->tword, n)) || (rc = dalloc(&g->treq, n)) || (rc = dalloc(&g->tvis, n)) ||
-        (rc = dalloc(&g->tbits, (n + 31) / 32 * 2)) ||
-        (rc = dalloc(&g->ttouch, n)) || (rc = dalloc(&g->tlast, n)) || (rc = dalloc(&g->tpend, n)) ||
-        (rc = dalloc(&g->tpendSlot, n)))
+    if ((rc = valloc(g, g->tword, n)) || (rc = valloc(g, g->treq, n)) || (rc = valloc(g, g->tvis, n)) ||
+        (rc = valloc(g, g->tbits, (n + 31) / 32 * 2)) ||
+        (rc = valloc(g, g->ttouch, n)) || (rc = valloc(g, g->tlast, n)) || (rc = valloc(g, g->tpend, n)) ||
+        (rc = valloc(g, g->tpendSlot, n)))
         return rc;
     CK(cudaMemsetAsync(g->tword, 0, n * 4, g->stream));
     CK(cudaMemsetAsync(g->tbits, 0, (n + 31) / 32 * 8, g->stream));
@@ -180,7 +180,7 @@ extern "C" void dn_cuda_map_destroy(DNgpuVolume* g)
     if (g->evicted) cudaFreeHost(g->evicted);
     if (g->hostKeep) {
         cudaFreeHost(g->hostKeep);
-        __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
+        if (!g->hostKeepReserved) __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
     }
     if (g->stageFree) cudaEventDestroy(g->stageFree);
     if (g->ownStream) cudaStreamDestroy(g->ownStream);
@@ -224,13 +224,13 @@ extern "C" int dn_cuda_map_create(uint32_t sx, uint32_t sy, uint32_t sz, uint32_
     e = cudaEventCreateWithFlags(&g->stageFree, cudaEventDisableTiming);
     if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "event: %s", cudaGetErrorString(e));
     if (!rc) rc = alloc_tiles(g);
-    if (!rc) rc = dalloc(&g->rec, slotCap);
-    if (!rc) rc = dalloc(&g->nsamples, slotCap);
-    if (!rc) rc = dalloc(&g->vox, voxelCap);
-    if (!rc) rc = dalloc(&g->diff, voxelCap);
-    if (!rc) rc = dalloc(&g->spec, voxelCap);
-    if (!rc) rc = dalloc(&g->st, 1);
-    if (!rc) rc = dalloc(&g->dtab, 1);
+    if (!rc) rc = valloc(g, g->rec, slotCap);
+    if (!rc) rc = valloc(g, g->nsamples, slotCap);
+    if (!rc) rc = valloc(g, g->vox, voxelCap);
+    if (!rc) rc = valloc(g, g->diff, voxelCap);
+    if (!rc) rc = valloc(g, g->spec, voxelCap);
+    if (!rc) rc = valloc(g, g->st, 1);
+    if (!rc) rc = valloc(g, g->dtab, 1);
     if (!rc) rc = reserve_requests(g, 1024);
     if (!rc) {
         COUNT_ALLOC();
@@ -266,12 +266,15 @@ extern "C" int dn_cuda_map_resize(DNgpuVolume* g, uint32_t sx, uint32_t sy, uint
 template <class T> static int grow_copy(DNgpuVolume* g, T** p, uint64_t oldCount, uint64_t newCount)
 {
     T* np = nullptr;
-    int rc = dalloc(&np, newCount);
-    if (rc) return rc;
+    const uint32_t bit = vol_array_bit(g, p);
+    COUNT_ALLOC();
+    if (g_asyncAlloc && bit) CK(cudaMallocAsync((void**)&np, (newCount ? newCount : 1) * sizeof(T), g->stream));
+    else CK(cudaMalloc((void**)&np, (newCount ? newCount : 1) * sizeof(T)));
     if (*p && oldCount) CK(cudaMemcpyAsync(np, *p, oldCount * sizeof(T), cudaMemcpyDeviceToDevice, g->stream));
     CK(cudaStreamSynchronize(g->stream));
     vfree(g, *p);
     *p = np;
+    if (g_asyncAlloc && bit) g->poolMask |= bit;
     dn_new_generation(g);
     return DN_CUDA_OK;
 }
@@ -343,13 +346,14 @@ extern "C" int dn_cuda_map_evict(DNgpuVolume* g)
     unsigned char* h = nullptr;
     if (g->hostKeep && g->hostKeepCap >= total) {
         h = g->hostKeep;
-        __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
+        if (!g->hostKeepReserved) __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
     } else {
         if (g->hostKeep) {
             // too small for the map as it is now: the copies a restore queued from it must finish first
             CK(cudaStreamSynchronize(g->stream));
             cudaFreeHost(g->hostKeep);
-            __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
+            if (!g->hostKeepReserved) __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
+            g->hostKeepReserved = false;
         }
         g->hostKeep = nullptr;
         g->hostKeepCap = 0;
@@ -378,6 +382,39 @@ extern "C" int dn_cuda_map_evict(DNgpuVolume* g)
     g->evicted = h;
     g->evictedBytes = cap;
     dn_new_generation(g);
+    return DN_CUDA_OK;
+}
+
+extern "C" int dn_cuda_map_reserve_host(DNgpuVolume* g)
+{
+    if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
+    if (g->evicted) return DN_CUDA_OK;
+    CK(cudaSetDevice(g->device));
+    PersistentArray a[16];
+    const int k = persistent_arrays(g, a);
+    size_t total = 0;
+    for (int i = 0; i < k; i++) total += align16(a[i].bytes);
+    if (!total) total = 16;
+    if (g->hostKeep && g->hostKeepCap >= total) {
+        if (!g->hostKeepReserved) {
+            __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
+            g->hostKeepReserved = true;
+        }
+        return DN_CUDA_OK;
+    }
+    if (g->hostKeep) {
+        CK(cudaStreamSynchronize(g->stream));
+        cudaFreeHost(g->hostKeep);
+        if (!g->hostKeepReserved) __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
+        g->hostKeep = nullptr;
+        g->hostKeepCap = 0;
+    }
+    // room to grow by a sixteenth before the next eviction needs a new block
+    const size_t cap = total + total / 16 + 4096;
+    COUNT_ALLOC();
+    CK(cudaMallocHost((void**)&g->hostKeep, cap));
+    g->hostKeepCap = cap;
+    g->hostKeepReserved = true;
     return DN_CUDA_OK;
 }
 
@@ -421,7 +458,10 @@ extern "C" int dn_cuda_map_restore(DNgpuVolume* g)
     // keep the pinned block for the next eviction when the retention cap allows it; otherwise free it once
     // the copies have read it
     const unsigned long long cap = g->evictedBytes;
-    if (__atomic_add_fetch(&g_pinnedRetained, cap, __ATOMIC_RELAXED) <= g_pinnedRetainMax) {
+    if (g->hostKeepReserved) {
+        g->hostKeep = g->evicted;
+        g->hostKeepCap = (size_t)cap;
+    } else if (__atomic_add_fetch(&g_pinnedRetained, cap, __ATOMIC_RELAXED) <= g_pinnedRetainMax) {
         g->hostKeep = g->evicted;
         g->hostKeepCap = (size_t)cap;
     } else {
@@ -651,7 +691,9 @@ int dn_stage_ops(DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops, const dn_
             g->hstageCap = nc;
         }
         if (total > g->dstageCap) {
-            CK(cudaStreamSynchronize(g->stream));
+            // a pooled buffer is freed in stream order after the kernels that read it; a cudaMalloc one
+            // needs the stream drained first
+            if (!(g->poolMask & vol_array_bit(g, &g->dstage))) CK(cudaStreamSynchronize(g->stream));
             vfree(g, g->dstage);
             size_t nc = total + total / 2 + 4096;
             int rc = valloc(g, g->dstage, nc);

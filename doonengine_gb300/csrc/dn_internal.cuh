@@ -68,6 +68,7 @@ struct DNgpuVolume {
     unsigned char* evicted; size_t evictedBytes;
     // the pinned block of the last restore, kept for the next eviction (within the process-wide retention cap)
     unsigned char* hostKeep; size_t hostKeepCap;
+    bool hostKeepReserved;              // the block was reserved (dn_cuda_map_reserve_host): never given back early
     // arrays allocated from the device's stream-ordered pool (bit per array, vol_array_bit): freed with
     // cudaFreeAsync on the volume's stream instead of cudaFree (which waits for the whole device)
     uint32_t poolMask;

@@ -52,13 +52,15 @@ enum : uint32_t { PV_VALID = 1u, PV_FIRST = 2u, PV_SPEC = 4u, PV_DIFF = 8u };
 #endif
 constexpr uint32_t PK_POOL_FAN = DN_PK_POOL_FAN;
 
-struct PacketWarp {
+template <uint32_t POOL>
+struct PacketWarpT {
     PacketVoxel v[32];
-    float con[PK_POOL_FAN][PK_MAX_SPEC_SEGMENTS][3];   // specular contributions of each pooled ray, in segment order
-    float sh[PK_POOL_FAN][3];                          // shadow contribution of each pooled ray
-    uint8_t ncon[PK_POOL_FAN];                         // contributions of each specular ray
-    uint8_t shHas[PK_POOL_FAN];                        // the shadow ray was unoccluded
+    float con[POOL][PK_MAX_SPEC_SEGMENTS][3];   // specular contributions of each pooled ray, in segment order
+    float sh[POOL][3];                          // shadow contribution of each pooled ray
+    uint8_t ncon[POOL];                         // contributions of each specular ray
+    uint8_t shHas[POOL];                        // the shadow ray was unoccluded
 };
+using PacketWarp = PacketWarpT<PK_POOL_FAN>;
 
 // sets up voxel (req, lane) of the group (voxel_setup of dn_light_stream.cuh); invalid slots get zero output
 __device__ __forceinline__ void packet_setup(PacketVoxel& pv, uint32_t req, uint32_t lane, const DevMap& m,
@@ -142,8 +144,8 @@ __device__ __forceinline__ int pass_voxel(uint32_t mask, uint32_t base, uint32_t
 // memory, and when the pool is empty every voxel's sums are formed in the reference's order; (2) the
 // diffuse paths, one lane per voxel; (3) the running average and the write-out.  One stepping loop
 // serves both traced phases.
-template <bool MANY>
-__device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLightArgs* many, PacketWarp& W)
+template <bool MANY, uint32_t POOL = PK_POOL_FAN>
+__device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLightArgs* many, PacketWarpT<POOL>& W)
 {
     const uint32_t lane = lane_id_s();
     uint32_t nreq = 0;
@@ -192,7 +194,7 @@ __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLi
         const uint32_t firstMask = diffMask & __ballot_sync(0xFFFFFFFFu, (myFlags & PV_FIRST) != 0u);
         const uint32_t workMask = specMask | diffMask;
         const uint32_t nWork = (uint32_t)__popc(workMask);
-        const uint32_t perPool = K < PK_POOL_FAN ? PK_POOL_FAN / K : 1u;
+        const uint32_t perPool = K < POOL ? POOL / K : 1u;
 
         // per-lane ray state
         Seg s;

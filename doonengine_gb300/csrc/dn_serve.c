@@ -214,7 +214,9 @@ static bool enforce_budget(DNserver* s, uint64_t extra, const uint8_t* inTick)
 		}
 		if (victim < 0) return false;
 		const uint64_t bytes = dn_cuda_map_footprint(s->slots[victim].vol->gpu);
+		const double e0 = DN_server_clock();
 		if (dn_cuda_map_evict(s->slots[victim].vol->gpu) != DN_CUDA_OK) return false;
+		s->stats.evictSeconds += DN_server_clock() - e0;
 		s->slots[victim].resident = 0;
 		s->stats.evictions++;
 		s->stats.evictedBytes += bytes;
@@ -234,7 +236,9 @@ static bool admit(DNserver* s, unsigned int v, const uint8_t* inTick)
 		resident_bytes(s, &n);
 		if (n) return false;
 	}
+	const double r0 = DN_server_clock();
 	if (dn_cuda_map_restore(slot->vol->gpu) != DN_CUDA_OK) return false;
+	s->stats.restoreSeconds += DN_server_clock() - r0;
 	slot->resident = 1;
 	s->stats.restores++;
 	s->stats.restoredBytes += dn_cuda_map_footprint(slot->vol->gpu);
@@ -471,6 +475,10 @@ static void* serve_main(void* arg)
 bool DN_server_start(DNserver* s)
 {
 	if (!s || s->started) return false;
+	/* volumes beyond the budget will be evicted: pin each one's host block now, not under load */
+	if (s->cfg.deviceBudgetBytes && resident_bytes(s, NULL) > s->cfg.deviceBudgetBytes)
+		for (unsigned int i = 0; i < s->nslots; i++)
+			if (dn_cuda_map_reserve_host(s->slots[i].vol->gpu) != DN_CUDA_OK) return false;
 	s->stop = 0;
 	if (pthread_create(&s->thread, NULL, serve_main, s) != 0) return false;
 	s->started = 1;

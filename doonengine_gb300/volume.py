@@ -1,7 +1,7 @@
 """Python mirror of the DN_* API: a thin object wrapper over libdoonengine.so for tests, benchmarks and
 tools.  Every call goes through the C ABI; nothing here computes lighting or traverses rays."""
 import ctypes
-from ctypes import POINTER, byref, c_float, c_int64, c_size_t, c_uint8, c_uint32, c_uint64, c_void_p
+from ctypes import POINTER, byref, c_double, c_float, c_int64, c_size_t, c_uint8, c_uint32, c_uint64, c_void_p
 
 import numpy as np
 
@@ -422,14 +422,17 @@ class Batch:
         t = L.DnBatchTuning()
         if self.lib.dn_cuda_batch_get_tuning(self._gpu(), byref(t)) != 0:
             raise RuntimeError("dn_cuda_batch_get_tuning failed")
-        return {"streamBatch": t.streamBatch, "blocksPerSM": t.blocksPerSM, "useGraph": t.useGraph, "kernel": t.kernel}
+        return {k: int(getattr(t, k)) for k, _ in L.DnBatchTuning._fields_}
 
-    def set_tuning(self, streamBatch=None, blocksPerSM=None, useGraph=None, kernel=None):
+    def set_tuning(self, streamBatch=None, blocksPerSM=None, useGraph=None, kernel=None, poolRays=None,
+                   diffuseBatch=None):
         cur = self.tuning()
         t = L.DnBatchTuning(streamBatch if streamBatch is not None else cur["streamBatch"],
                             blocksPerSM if blocksPerSM is not None else cur["blocksPerSM"],
                             useGraph if useGraph is not None else cur["useGraph"],
-                            kernel if kernel is not None else cur["kernel"])
+                            kernel if kernel is not None else cur["kernel"],
+                            poolRays if poolRays is not None else cur["poolRays"],
+                            diffuseBatch if diffuseBatch is not None else cur["diffuseBatch"])
         if self.lib.dn_cuda_batch_set_tuning(self._gpu(), byref(t)) != 0:
             raise RuntimeError("dn_cuda_batch_set_tuning failed: %s" % self.lib.dn_cuda_last_error().decode())
 
@@ -512,7 +515,7 @@ class Server:
     def stats(self):
         st = L.DNserveStats()
         self.lib.DN_server_get_stats(self.ptr, byref(st))
-        return {k: int(getattr(st, k)) for k, _ in L.DNserveStats._fields_}
+        return {k: (float if t is c_double else int)(getattr(st, k)) for k, t in L.DNserveStats._fields_}
 
     def batch_stats(self):
         s = L.DNstats()

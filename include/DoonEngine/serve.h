@@ -15,7 +15,8 @@
  *
  * Admission: a tick only includes volumes whose device state fits the device budget together with every
  * other resident volume; when it does not fit, the least recently used idle volumes are evicted whole to
- * pinned host memory (dn_cuda_map_evict) and restored on their next request.
+ * pinned host memory (dn_cuda_map_evict) and restored on their next request.  Evictions and restores are
+ * queued in the batch's stream order (no host wait); their copies count in the tick's device time.
  */
 #ifndef DN_SERVE_H
 #define DN_SERVE_H
@@ -86,6 +87,7 @@ typedef struct DNserveStats
 	 * the bytes evicted and restored */
 	double admitSeconds, issueSeconds, deviceSeconds;
 	uint64_t evictedBytes, restoredBytes;
+	double evictSeconds, restoreSeconds;     /* the serving thread's time inside dn_cuda_map_evict / _restore */
 } DNserveStats;
 
 DNserver* DN_server_create(const DNserveConfig* config);
@@ -94,6 +96,9 @@ DNserver* DN_server_create(const DNserveConfig* config);
 void DN_server_destroy(DNserver* server);
 /* registers a device volume (it joins the server's batch); returns its index, or -1 */
 int DN_server_add_volume(DNserver* server, DNvolume* vol);
+/* starts the serving thread.  When the volumes' device footprint exceeds the budget, each volume's pinned
+ * host block for eviction is reserved here (dn_cuda_map_reserve_host), so that no eviction under load pins
+ * host memory; false if that reservation fails */
 bool DN_server_start(DNserver* server);
 /* thread-safe; returns the request id (> 0), or 0 for an invalid request */
 uint64_t DN_server_submit(DNserver* server, const DNrequest* request);

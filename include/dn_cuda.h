@@ -194,10 +194,13 @@ typedef struct dn_batch_item {
 
 /* knobs of the batched lighting launch, chosen by dn_cuda_batch_autotune */
 typedef struct dn_batch_tuning {
-    uint32_t streamBatch;       /* lanes of a warp that wait before per-segment work runs, 1..32 */
-    uint32_t blocksPerSM;       /* resident lighting blocks per SM, 1..4 */
+    uint32_t streamBatch;       /* compaction period of the ray pools: lanes of a warp whose segment ended
+                                   before the warp regroups (shades them and refills them from the pool), 1..32 */
+    uint32_t blocksPerSM;       /* resident lighting blocks per SM */
     uint32_t useGraph;          /* replay repeated frames as a CUDA graph */
     uint32_t kernel;            /* lighting kernel: 1 per-lane ray streams, 2 warp packets of ray fans */
+    uint32_t poolRays;          /* rays per warp: rays of each fan kind a warp pulls into one pool, 64 or 128 */
+    uint32_t diffuseBatch;      /* the diffuse-path kernel's compaction period (lanes waiting before refill) */
 } dn_batch_tuning;
 
 int dn_cuda_batch_create(struct DNgpuBatch** out);
@@ -232,6 +235,10 @@ uint64_t dn_cuda_map_footprint(struct DNgpuVolume* g);
 int dn_cuda_map_is_resident(struct DNgpuVolume* g);
 int dn_cuda_map_evict(struct DNgpuVolume* g);
 int dn_cuda_map_restore(struct DNgpuVolume* g);
+/* pins the host block the map's evictions copy into now (its current size plus a sixteenth), so that no
+ * later eviction pins memory; the block stays with the map until it is destroyed (a server with a device
+ * budget below its volumes' total reserves one for each at start) */
+int dn_cuda_map_reserve_host(struct DNgpuVolume* g);
 /* 1 when the work recorded by ev has completed, 0 while pending, negative on error */
 int dn_cuda_event_query(void* ev);
 

@@ -163,6 +163,15 @@ def test_batch_autotune_keeps_results(gpu_ready):
             batch_frame(batch, bat, t)
             for i in range(len(SPECS)):
                 same_state(solo[i], bat[i], "frame %d map %d (untuned)" % (f, i))
+        # the other pool size (rays a warp pulls per pool) and another diffuse compaction period
+        batch.set_tuning(poolRays=64 if tun["poolRays"] == 128 else 128, diffuseBatch=5, kernel=2,
+                         blocksPerSM=2, useGraph=1)
+        for f in range(6, 8):
+            t = 2.0 + f
+            solo_frame(solo, t)
+            batch_frame(batch, bat, t)
+            for i in range(len(SPECS)):
+                same_state(solo[i], bat[i], "frame %d map %d (pool %d)" % (f, i, batch.tuning()["poolRays"]))
     finally:
         batch.close()
         close_all(solo, bat)
