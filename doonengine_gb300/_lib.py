@@ -327,7 +327,8 @@ _SIGS = [
     ("dn_cuda_map_is_resident", c_int, [c_void_p]),
     ("dn_cuda_map_evict", c_int, [c_void_p]),
     ("dn_cuda_map_restore", c_int, [c_void_p]),
-    ("dn_cuda_map_reserve_host", c_int, [c_void_p]),
+    ("dn_cuda_host_reserve", c_int, [c_uint64]),
+    ("dn_cuda_host_pinned", c_uint64, []),
     ("dn_cuda_event_query", c_int, [c_void_p]),
     ("dn_cuda_kernel_names", c_char_p, []),
     ("dn_cuda_launch_count", c_uint64, []),

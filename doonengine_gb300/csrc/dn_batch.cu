@@ -51,7 +51,8 @@ struct DNgpuBatch {
     uint32_t gatherCount;
     dn_batch_tuning tuning;
     int maxBlocksPerSM;         // of the ray-stream kernel
-    int maxBlocksPacket;        // of the packet kernel
+    int maxBlocksPacket;        // of the packet kernel with PK_POOL_FAN-ray pools
+    int maxBlocksPacketAlt;     // of the packet kernel with the other pool size (PK_POOL_ALT)
     int maxBlocksDiffuse;       // of the diffuse-path kernel that follows it
     std::vector<uint64_t> lastKey;
     std::vector<uint64_t> graphKey;
@@ -154,7 +155,7 @@ __global__ void __launch_bounds__(128, DN_STREAM_MIN_BLOCKS) k_light_stream_batc
 }
 
 // POOL: rays per fan kind per pool (the rays a warp pulls from a request group at a time); the autotuner
-// picks 64 or 128 (dn_batch_tuning.poolRays)
+// picks PK_POOL_FAN or PK_POOL_ALT (dn_batch_tuning.poolRays)
 template <uint32_t POOL>
 __global__ void __launch_bounds__(128, DN_PACKET_MIN_BLOCKS) k_light_packet_batch(const __grid_constant__ BatchLightArgs a)
 {
@@ -250,7 +251,10 @@ extern "C" int dn_cuda_batch_create(DNgpuBatch** out)
     if (!rc) {
         int perSM = 0, perSM2 = 0, perSM3 = 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_light_stream_batch, 128, 0);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM2, k_light_packet_batch<128>, 128, 0);
+        int perSMAlt = 0;
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM2, k_light_packet_batch<PK_POOL_FAN>, 128, 0);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSMAlt, k_light_packet_batch<PK_POOL_ALT>, 128, 0);
+        b->maxBlocksPacketAlt = perSMAlt < 1 ? 1 : perSMAlt;
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM3, k_light_diffuse_batch, 128, 0);
         if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "occupancy: %s", cudaGetErrorString(e));
         b->maxBlocksPerSM = perSM < 1 ? 1 : perSM;
@@ -358,8 +362,8 @@ static int issue_light(DNgpuBatch* b, const BatchLightArgs& la, cudaStream_t s, 
     CK(cudaGetLastError());
     COUNT_LAUNCH();
     const unsigned grid = (unsigned)(g_numSMs * (int)b->tuning.blocksPerSM);
-    if (packets && b->tuning.poolRays == 64u) k_light_packet_batch<64><<<grid, 128, 0, s>>>(la);
-    else if (packets) k_light_packet_batch<128><<<grid, 128, 0, s>>>(la);
+    if (packets && b->tuning.poolRays == PK_POOL_ALT) k_light_packet_batch<PK_POOL_ALT><<<grid, 128, 0, s>>>(la);
+    else if (packets) k_light_packet_batch<PK_POOL_FAN><<<grid, 128, 0, s>>>(la);
     else k_light_stream_batch<<<grid, 128, 0, s>>>(la);
     CK(cudaGetLastError());
     if (packets) {
@@ -696,9 +700,11 @@ extern "C" int dn_cuda_batch_set_tuning(DNgpuBatch* b, const dn_batch_tuning* t)
     if (!b || !t) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (t->streamBatch < 1 || t->streamBatch > 32) return dn_set_err(DN_CUDA_ERR_ARG, "streamBatch %u", t->streamBatch);
     if (t->kernel != 1u && t->kernel != 2u) return dn_set_err(DN_CUDA_ERR_ARG, "kernel %u (1 streams, 2 packets)", t->kernel);
-    if (t->poolRays != 64u && t->poolRays != 128u) return dn_set_err(DN_CUDA_ERR_ARG, "poolRays %u (64 or 128)", t->poolRays);
+    if (t->poolRays != PK_POOL_FAN && t->poolRays != PK_POOL_ALT)
+        return dn_set_err(DN_CUDA_ERR_ARG, "poolRays %u (%u or %u)", t->poolRays, PK_POOL_FAN, PK_POOL_ALT);
     if (t->diffuseBatch < 1 || t->diffuseBatch > 32) return dn_set_err(DN_CUDA_ERR_ARG, "diffuseBatch %u", t->diffuseBatch);
-    const int maxBlocks = t->kernel == 2u ? b->maxBlocksPacket : b->maxBlocksPerSM;
+    const int maxBlocks = t->kernel == 2u ? (t->poolRays == PK_POOL_FAN ? b->maxBlocksPacket : b->maxBlocksPacketAlt)
+                                          : b->maxBlocksPerSM;
     if (t->blocksPerSM < 1 || (int)t->blocksPerSM > maxBlocks)
         return dn_set_err(DN_CUDA_ERR_ARG, "blocksPerSM %u (1..%d)", t->blocksPerSM, maxBlocks);
     b->tuning = *t;
@@ -778,11 +784,19 @@ extern "C" int dn_cuda_batch_autotune(DNgpuBatch* b, dn_batch_tuning* chosen)
     for (uint32_t sb : batches) { dn_batch_tuning t = best; t.streamBatch = sb; if (!rc) trial(t); }
     if (best.kernel == 2u && packetsOk) {
         // rays a warp pulls per pool, then the diffuse kernel's refill threshold
-        { dn_batch_tuning t = best; t.poolRays = best.poolRays == 128u ? 64u : 128u; if (!rc) trial(t); }
+        {
+            dn_batch_tuning t = best;
+            t.poolRays = best.poolRays == PK_POOL_FAN ? PK_POOL_ALT : PK_POOL_FAN;
+            const uint32_t mx = (uint32_t)(t.poolRays == PK_POOL_FAN ? b->maxBlocksPacket : b->maxBlocksPacketAlt);
+            if (t.blocksPerSM > mx) t.blocksPerSM = mx;
+            if (!rc) trial(t);
+        }
         const uint32_t dbatches[] = {8u, 12u, 16u, 20u, 24u, 28u};
         for (uint32_t db : dbatches) { dn_batch_tuning t = best; t.diffuseBatch = db; if (!rc) trial(t); }
     }
-    const uint32_t bpsMax = (uint32_t)(best.kernel == 2u ? b->maxBlocksPacket : b->maxBlocksPerSM);
+    const uint32_t bpsMax = (uint32_t)(best.kernel == 2u ? (best.poolRays == PK_POOL_FAN ? b->maxBlocksPacket
+                                                                                    : b->maxBlocksPacketAlt)
+                                                       : b->maxBlocksPerSM);
     for (uint32_t bps = 2; bps <= bpsMax && bps <= 8; bps++) {
         dn_batch_tuning t = best; t.blocksPerSM = bps; if (!rc) trial(t);
     }

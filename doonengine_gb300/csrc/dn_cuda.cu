@@ -19,6 +19,7 @@
 #include <stdlib.h>
 #include <new>
 #include <mutex>
+#include <vector>
 #include <stdarg.h>
 
 using namespace dn;
@@ -63,8 +64,14 @@ int g_numSMs = 0;
 bool g_asyncAlloc = false;
 // pinned host blocks kept by restored volumes for their next eviction, and the cap on their sum
 // (DN_PINNED_RETAIN_GB, default 64 GiB): within it a map's evictions after the first pin nothing
-static unsigned long long g_pinnedRetained = 0;
-static unsigned long long g_pinnedRetainMax = 64ull << 30;
+// the pinned host memory evictions copy into: 64 MiB slabs, pinned once and reused by every volume.  A slab's
+// event marks the end of the last copy that read it (a restore), so that the next eviction writing it waits
+// for that copy on the device, never on the host.
+static const size_t HOST_SLAB = 64ull << 20;
+struct HostSlab { unsigned char* p; cudaEvent_t lastRead; };
+static std::mutex g_slabMutex;
+static std::vector<HostSlab> g_slabs;
+static std::vector<uint32_t> g_freeSlabs;
 unsigned long long g_launches = 0;
 unsigned long long g_allocs = 0;
 static unsigned long long g_generation = 0;
@@ -106,7 +113,6 @@ extern "C" int dn_cuda_init(int device)
     CK(cudaSetDevice(device));
     CK(cudaFree(0));
     CK(cudaDeviceGetAttribute(&g_numSMs, cudaDevAttrMultiProcessorCount, device));
-    if (const char* e = getenv("DN_PINNED_RETAIN_GB")) g_pinnedRetainMax = (unsigned long long)(atof(e) * (1ull << 30));
     // stream-ordered allocation for volume arrays that come and go with eviction: the device's default pool
     // keeps what it frees (release threshold unlimited), so a restore reuses an evicted map's memory
     // without returning to the driver, and a free does not wait for the whole device
@@ -177,10 +183,11 @@ extern "C" void dn_cuda_map_destroy(DNgpuVolume* g)
     if (g->stream) cudaStreamSynchronize(g->stream);
     if (g->hstage) cudaFreeHost(g->hstage);
     if (g->hst) cudaFreeHost(g->hst);
-    if (g->evicted) cudaFreeHost(g->evicted);
-    if (g->hostKeep) {
-        cudaFreeHost(g->hostKeep);
-        if (!g->hostKeepReserved) __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
+    if (g->evicted) {
+        // an evicted volume's slabs go back to the pool (no copy reads them any more)
+        std::lock_guard<std::mutex> lock(g_slabMutex);
+        for (uint32_t i = 0; i < g->evictedSlabs; i++) g_freeSlabs.push_back(g->evicted[i]);
+        free(g->evicted);
     }
     if (g->stageFree) cudaEventDestroy(g->stageFree);
     if (g->ownStream) cudaStreamDestroy(g->ownStream);
@@ -312,7 +319,6 @@ static int persistent_arrays(DNgpuVolume* g, PersistentArray* out)
     return k;
 }
 
-static size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 extern "C" uint64_t dn_cuda_map_footprint(DNgpuVolume* g)
 {
@@ -327,12 +333,45 @@ extern "C" uint64_t dn_cuda_map_footprint(DNgpuVolume* g)
 
 extern "C" int dn_cuda_map_is_resident(DNgpuVolume* g) { return g && !g->evicted; }
 
+// pins slabs until the pool holds 'bytes' (free or in use); returns false when pinning fails
+static bool slabs_grow_to(size_t bytes)
+{
+    while (g_slabs.size() * HOST_SLAB < bytes) {
+        HostSlab sl{nullptr, nullptr};
+        COUNT_ALLOC();
+        if (cudaMallocHost((void**)&sl.p, HOST_SLAB) != cudaSuccess) { cudaGetLastError(); return false; }
+        if (cudaEventCreateWithFlags(&sl.lastRead, cudaEventDisableTiming) != cudaSuccess) {
+            cudaFreeHost(sl.p);
+            cudaGetLastError();
+            return false;
+        }
+        g_freeSlabs.push_back((uint32_t)g_slabs.size());
+        g_slabs.push_back(sl);
+    }
+    return true;
+}
+
+extern "C" int dn_cuda_host_reserve(uint64_t bytes)
+{
+    if (g_device < 0) return dn_set_err(DN_CUDA_ERR_DEVICE, "dn_cuda_init was not called");
+    CK(cudaSetDevice(g_device));
+    std::lock_guard<std::mutex> lock(g_slabMutex);
+    if (!slabs_grow_to((size_t)bytes)) return dn_set_err(DN_CUDA_ERR_NOMEM, "pinning %llu bytes of host memory failed",
+                                                         (unsigned long long)bytes);
+    return DN_CUDA_OK;
+}
+
+extern "C" uint64_t dn_cuda_host_pinned(void)
+{
+    std::lock_guard<std::mutex> lock(g_slabMutex);
+    return (uint64_t)g_slabs.size() * HOST_SLAB;
+}
+
 // Eviction and restore never wait for the device.  Both run in the volume's stream order (the batch's
-// stream while the volume is a member): eviction queues the copies of the persistent arrays into the
-// volume's pinned block and then frees the arrays -- stream-ordered when they came from the pool, which is
-// where every restore puts them -- and restore queues the allocations and the copies back.  The pinned
-// block stays with the volume after a restore (up to the process-wide retention cap), so only a map's
-// first eviction pins host memory.
+// stream while the volume is a member): eviction queues the copies of the persistent arrays into slabs of
+// the pinned pool and then frees the arrays (stream-ordered: they come from the device's pool), and restore
+// queues the allocations and the copies back, then returns the slabs with an event after the copies.  Only
+// slabs the pool does not hold yet are pinned (dn_cuda_host_reserve pins them ahead).
 extern "C" int dn_cuda_map_evict(DNgpuVolume* g)
 {
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
@@ -341,80 +380,50 @@ extern "C" int dn_cuda_map_evict(DNgpuVolume* g)
     PersistentArray a[16];
     const int k = persistent_arrays(g, a);
     size_t total = 0;
-    for (int i = 0; i < k; i++) total += align16(a[i].bytes);
-    if (!total) total = 16;
-    unsigned char* h = nullptr;
-    if (g->hostKeep && g->hostKeepCap >= total) {
-        h = g->hostKeep;
-        if (!g->hostKeepReserved) __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
-    } else {
-        if (g->hostKeep) {
-            // too small for the map as it is now: the copies a restore queued from it must finish first
-            CK(cudaStreamSynchronize(g->stream));
-            cudaFreeHost(g->hostKeep);
-            if (!g->hostKeepReserved) __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
-            g->hostKeepReserved = false;
+    for (int i = 0; i < k; i++) total += a[i].bytes;
+    const uint32_t n = (uint32_t)((total + HOST_SLAB - 1) / HOST_SLAB);
+    uint32_t* ids = (uint32_t*)malloc(sizeof(uint32_t) * (n ? n : 1));
+    if (!ids) return dn_set_err(DN_CUDA_ERR_NOMEM, "host");
+    {
+        std::lock_guard<std::mutex> lock(g_slabMutex);
+        if (g_freeSlabs.size() < n && !slabs_grow_to((g_slabs.size() + n - g_freeSlabs.size()) * HOST_SLAB)) {
+            free(ids);
+            return dn_set_err(DN_CUDA_ERR_NOMEM, "evict: pinning host memory for %llu bytes failed", (unsigned long long)total);
         }
-        g->hostKeep = nullptr;
-        g->hostKeepCap = 0;
-        COUNT_ALLOC();
-        CK(cudaMallocHost((void**)&h, total));
+        for (uint32_t i = 0; i < n; i++) { ids[i] = g_freeSlabs.back(); g_freeSlabs.pop_back(); }
     }
-    const size_t cap = (h == g->hostKeep) ? g->hostKeepCap : total;
-    g->hostKeep = nullptr;
-    g->hostKeepCap = 0;
-    size_t o = 0;
+    // the slabs' last readers (earlier restores, possibly on other streams) finish first, on the device
+    for (uint32_t i = 0; i < n; i++) CK(cudaStreamWaitEvent(g->stream, g_slabs[ids[i]].lastRead, 0));
+    // the arrays back to back across the slabs
+    uint32_t si = 0;
+    size_t so = 0;
     for (int i = 0; i < k; i++) {
-        cudaError_t e = cudaMemcpyAsync(h + o, *a[i].ptr, a[i].bytes, cudaMemcpyDeviceToHost, g->stream);
-        if (e != cudaSuccess) {
-            cudaStreamSynchronize(g->stream);
-            cudaFreeHost(h);
-            return dn_set_err(DN_CUDA_ERR_LAUNCH, "evict: %s", cudaGetErrorString(e));
+        size_t done = 0;
+        while (done < a[i].bytes) {
+            const size_t len = (a[i].bytes - done) < (HOST_SLAB - so) ? (a[i].bytes - done) : (HOST_SLAB - so);
+            cudaError_t e = cudaMemcpyAsync(g_slabs[ids[si]].p + so, (const unsigned char*)*a[i].ptr + done, len,
+                                            cudaMemcpyDeviceToHost, g->stream);
+            if (e != cudaSuccess) {
+                cudaStreamSynchronize(g->stream);
+                std::lock_guard<std::mutex> lock(g_slabMutex);
+                for (uint32_t j = 0; j < n; j++) g_freeSlabs.push_back(ids[j]);
+                free(ids);
+                return dn_set_err(DN_CUDA_ERR_LAUNCH, "evict: %s", cudaGetErrorString(e));
+            }
+            done += len;
+            so += len;
+            if (so == HOST_SLAB) { so = 0; si++; }
         }
-        o += align16(a[i].bytes);
     }
-    // the frees follow the copies in the stream's order (a cudaFree of an array from cudaMalloc waits anyway)
+    // the frees follow the copies in the stream's order
     free_tiles(g);
     vfree(g, g->rec); vfree(g, g->nsamples); vfree(g, g->vox); vfree(g, g->diff); vfree(g, g->spec);
     vfree(g, g->reqs); vfree(g, g->st); vfree(g, g->dtab);
     vfree(g, g->lightOut); vfree(g, g->dstage); vfree(g, g->dimg); vfree(g, g->dhit); vfree(g, g->dface);
     g->dstageCap = 0; g->dimgCap = 0;
-    g->evicted = h;
-    g->evictedBytes = cap;
+    g->evicted = ids;
+    g->evictedSlabs = n;
     dn_new_generation(g);
-    return DN_CUDA_OK;
-}
-
-extern "C" int dn_cuda_map_reserve_host(DNgpuVolume* g)
-{
-    if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
-    if (g->evicted) return DN_CUDA_OK;
-    CK(cudaSetDevice(g->device));
-    PersistentArray a[16];
-    const int k = persistent_arrays(g, a);
-    size_t total = 0;
-    for (int i = 0; i < k; i++) total += align16(a[i].bytes);
-    if (!total) total = 16;
-    if (g->hostKeep && g->hostKeepCap >= total) {
-        if (!g->hostKeepReserved) {
-            __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
-            g->hostKeepReserved = true;
-        }
-        return DN_CUDA_OK;
-    }
-    if (g->hostKeep) {
-        CK(cudaStreamSynchronize(g->stream));
-        cudaFreeHost(g->hostKeep);
-        if (!g->hostKeepReserved) __atomic_fetch_sub(&g_pinnedRetained, (unsigned long long)g->hostKeepCap, __ATOMIC_RELAXED);
-        g->hostKeep = nullptr;
-        g->hostKeepCap = 0;
-    }
-    // room to grow by a sixteenth before the next eviction needs a new block
-    const size_t cap = total + total / 16 + 4096;
-    COUNT_ALLOC();
-    CK(cudaMallocHost((void**)&g->hostKeep, cap));
-    g->hostKeepCap = cap;
-    g->hostKeepReserved = true;
     return DN_CUDA_OK;
 }
 
@@ -450,27 +459,30 @@ extern "C" int dn_cuda_map_restore(DNgpuVolume* g)
         vfree(g, g->reqs); vfree(g, g->st); vfree(g, g->dtab); vfree(g, g->lightOut);
         return rc;
     }
-    size_t o = 0;
+    uint32_t si = 0;
+    size_t so = 0;
     for (int i = 0; i < k; i++) {
-        CK(cudaMemcpyAsync(*a[i].ptr, g->evicted + o, a[i].bytes, cudaMemcpyHostToDevice, g->stream));
-        o += align16(a[i].bytes);
+        size_t done = 0;
+        while (done < a[i].bytes) {
+            const size_t len = (a[i].bytes - done) < (HOST_SLAB - so) ? (a[i].bytes - done) : (HOST_SLAB - so);
+            CK(cudaMemcpyAsync((unsigned char*)*a[i].ptr + done, g_slabs[g->evicted[si]].p + so, len,
+                               cudaMemcpyHostToDevice, g->stream));
+            done += len;
+            so += len;
+            if (so == HOST_SLAB) { so = 0; si++; }
+        }
     }
-    // keep the pinned block for the next eviction when the retention cap allows it; otherwise free it once
-    // the copies have read it
-    const unsigned long long cap = g->evictedBytes;
-    if (g->hostKeepReserved) {
-        g->hostKeep = g->evicted;
-        g->hostKeepCap = (size_t)cap;
-    } else if (__atomic_add_fetch(&g_pinnedRetained, cap, __ATOMIC_RELAXED) <= g_pinnedRetainMax) {
-        g->hostKeep = g->evicted;
-        g->hostKeepCap = (size_t)cap;
-    } else {
-        __atomic_fetch_sub(&g_pinnedRetained, cap, __ATOMIC_RELAXED);
-        CK(cudaStreamSynchronize(g->stream));
-        cudaFreeHost(g->evicted);
+    // the slabs are free for the next eviction once these copies have read them
+    {
+        std::lock_guard<std::mutex> lock(g_slabMutex);
+        for (uint32_t i = 0; i < g->evictedSlabs; i++) {
+            CK(cudaEventRecord(g_slabs[g->evicted[i]].lastRead, g->stream));
+            g_freeSlabs.push_back(g->evicted[i]);
+        }
     }
+    free(g->evicted);
     g->evicted = nullptr;
-    g->evictedBytes = 0;
+    g->evictedSlabs = 0;
     dn_new_generation(g);
     return DN_CUDA_OK;
 }

@@ -64,11 +64,9 @@ struct DNgpuVolume {
     // device staging for host-memory draws
     float4* dimg; uint32_t* dhit; uint8_t* dface; size_t dimgCap;
     int numSMs;
-    // eviction: every persistent device array copied to one pinned host block, device arrays freed
-    unsigned char* evicted; size_t evictedBytes;
-    // the pinned block of the last restore, kept for the next eviction (within the process-wide retention cap)
-    unsigned char* hostKeep; size_t hostKeepCap;
-    bool hostKeepReserved;              // the block was reserved (dn_cuda_map_reserve_host): never given back early
+    // eviction: every persistent device array copied into slabs of the process-wide pinned host pool
+    // (evicted: the slabs' indices, null while resident), device arrays freed
+    uint32_t* evicted; uint32_t evictedSlabs;
     // arrays allocated from the device's stream-ordered pool (bit per array, vol_array_bit): freed with
     // cudaFreeAsync on the volume's stream instead of cudaFree (which waits for the whole device)
     uint32_t poolMask;

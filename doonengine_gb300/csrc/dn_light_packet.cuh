@@ -51,6 +51,7 @@ enum : uint32_t { PV_VALID = 1u, PV_FIRST = 2u, PV_SPEC = 4u, PV_DIFF = 8u };
 #define DN_PK_POOL_FAN 128
 #endif
 constexpr uint32_t PK_POOL_FAN = DN_PK_POOL_FAN;
+constexpr uint32_t PK_POOL_ALT = PK_POOL_FAN == 64u ? 128u : 64u;   // the batched autotuner's other pool size
 
 template <uint32_t POOL>
 struct PacketWarpT {

@@ -475,10 +475,15 @@ static void* serve_main(void* arg)
 bool DN_server_start(DNserver* s)
 {
 	if (!s || s->started) return false;
-	/* volumes beyond the budget will be evicted: pin each one's host block now, not under load */
-	if (s->cfg.deviceBudgetBytes && resident_bytes(s, NULL) > s->cfg.deviceBudgetBytes)
-		for (unsigned int i = 0; i < s->nslots; i++)
-			if (dn_cuda_map_reserve_host(s->slots[i].vol->gpu) != DN_CUDA_OK) return false;
+	/* volumes beyond the budget will be evicted: pin the host memory they need now, not under load (the
+	 * difference plus a quarter, for growth and slab rounding) */
+	if (s->cfg.deviceBudgetBytes) {
+		const uint64_t used = resident_bytes(s, NULL);
+		if (used > s->cfg.deviceBudgetBytes) {
+			const uint64_t over = used - s->cfg.deviceBudgetBytes;
+			if (dn_cuda_host_reserve(over + over / 4) != DN_CUDA_OK) return false;
+		}
+	}
 	s->stop = 0;
 	if (pthread_create(&s->thread, NULL, serve_main, s) != 0) return false;
 	s->started = 1;

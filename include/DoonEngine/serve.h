@@ -96,9 +96,9 @@ DNserver* DN_server_create(const DNserveConfig* config);
 void DN_server_destroy(DNserver* server);
 /* registers a device volume (it joins the server's batch); returns its index, or -1 */
 int DN_server_add_volume(DNserver* server, DNvolume* vol);
-/* starts the serving thread.  When the volumes' device footprint exceeds the budget, each volume's pinned
- * host block for eviction is reserved here (dn_cuda_map_reserve_host), so that no eviction under load pins
- * host memory; false if that reservation fails */
+/* starts the serving thread.  When the volumes' device footprint exceeds the budget, the pinned host memory
+ * their evictions need (the excess plus a quarter) is reserved here (dn_cuda_host_reserve), so that no
+ * eviction under load pins host memory; false if that reservation fails */
 bool DN_server_start(DNserver* server);
 /* thread-safe; returns the request id (> 0), or 0 for an invalid request */
 uint64_t DN_server_submit(DNserver* server, const DNrequest* request);

@@ -235,10 +235,12 @@ uint64_t dn_cuda_map_footprint(struct DNgpuVolume* g);
 int dn_cuda_map_is_resident(struct DNgpuVolume* g);
 int dn_cuda_map_evict(struct DNgpuVolume* g);
 int dn_cuda_map_restore(struct DNgpuVolume* g);
-/* pins the host block the map's evictions copy into now (its current size plus a sixteenth), so that no
- * later eviction pins memory; the block stays with the map until it is destroyed (a server with a device
- * budget below its volumes' total reserves one for each at start) */
-int dn_cuda_map_reserve_host(struct DNgpuVolume* g);
+/* Evictions copy into a process-wide pool of pinned 64 MiB host slabs, pinned when first needed and reused
+ * by every volume afterwards.  dn_cuda_host_reserve pins slabs until the pool holds 'bytes', so that no
+ * eviction under load has to pin host memory (a server whose volumes exceed its device budget reserves the
+ * difference at start); dn_cuda_host_pinned returns the pool's size in bytes. */
+int dn_cuda_host_reserve(uint64_t bytes);
+uint64_t dn_cuda_host_pinned(void);
 /* 1 when the work recorded by ev has completed, 0 while pending, negative on error */
 int dn_cuda_event_query(void* ev);
 
