@@ -342,10 +342,15 @@ def cpu_baseline_sample(vol, view, proj, W, H, seconds):
     from doonengine_gb300 import _lib
     lib = dn.load()
     ncores = os.cpu_count() or 1
-    st, vis, _, _ = vol.export_tiles()
+    st, vis, _, ns = vol.export_tiles()
     reqs = vol.export_requests()
+    idx, dif, spe = vol.export_lighting()
     om = O.OracleMap(vol.map_size)
     om.import_state(vol.s, st, vis, vol.s.frameNum)
+    # the device's sample counts and lighting too: with zero counts every voxel would trace its first-sample
+    # rays (one shadow ray instead of K), a lighter mix than the GPU's
+    om.import_lighting(idx, dif, spe)
+    om.import_samples(ns)
     om.set_requests(reqs)
     params = om.light_params(vol.s, 1, 1000, float(vol.s.lastTime))
     iv, icv, ip = _lib.DNmat4(), _lib.DNmat4(), _lib.DNmat4()

@@ -557,7 +557,12 @@ static inline uint32_t step_cap(uint32_t sx, uint32_t sy, uint32_t sz)
     return c > (1ull << 23) ? (1u << 23) : (uint32_t)c;
 }
 
-static inline void store_u8(uint8_t* p, uint8_t v) { __atomic_store_n(p, v, __ATOMIC_RELAXED); }
+/* idempotent flag store: written only when it changes, so that threads whose rays cross the same tiles do not
+ * keep invalidating each other's cache lines with stores of the value already there */
+static inline void store_u8(uint8_t* p, uint8_t v)
+{
+    if (__atomic_load_n(p, __ATOMIC_RELAXED) != v) __atomic_store_n(p, v, __ATOMIC_RELAXED);
+}
 static inline uint8_t load_u8(const uint8_t* p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
 
 static inline uint32_t map_index(const dno_map* m, iv3 p)
