@@ -325,13 +325,15 @@ def serving_summary(sv):
     request rate and rays/s, and the highest achieved rate whose p99 stays within 33 ms."""
     rows = [{k: r.get(k) for k in ("offered_rps", "achieved_rps", "p50_ms", "p99_ms", "rays_per_s", "completed",
                                    "drained", "evictions", "restores", "evicted_gb", "restored_gb", "server_admit_s",
-                                   "server_evict_s", "server_restore_s", "server_issue_s", "device_s")}
+                                   "server_evict_s", "server_restore_s", "server_issue_s", "device_s",
+                                   "host_pinned_gb", "host_pinned_grown_gb")}
             for r in sv["sweep"]]
     return {"workload": sv["config"]["workload"], "device_budget_gb": sv["config"]["device_budget_gb"],
             "offered_rps": [r["offered_rps"] for r in rows], "p50_ms": [r["p50_ms"] for r in rows],
             "p99_ms": [r["p99_ms"] for r in rows], "max_rps_p99_le_33ms": sv["max_rps_with_p99_le_33ms"],
             "rays_per_s": sv["value"], "evictions": sv["evictions"], "restores": sv["restores"],
-            "resident_bytes": sv["resident_bytes"], "sweep": rows, "build_s": sv["build_s"]}
+            "resident_bytes": sv["resident_bytes"], "host_pinned_gb": sv["host_pinned_gb"], "sweep": rows,
+            "build_s": sv["build_s"]}
 
 
 def cpu_baseline_sample(vol, view, proj, W, H, seconds):
@@ -672,8 +674,12 @@ def run_streaming(args):
         "chunks_edited_per_step": edited / K, "host_edit_ms_per_step": host_edit_s * 1e3 / K,
         "host_sync_ms_per_step": host_sync[0] * 1e3 / K,
         "host_edit_note": "host_edit: the workload generating its edits (dn_scene_reroll re-rolls the voxels of the "
-                          "chosen chunks through the edit API); host_sync: DN_sync_gpu's host part (packing of the "
-                          "edited chunks, pool ranges, one pinned upload)",
+                          "chosen chunks through the edit API); host_sync: DN_sync_gpu's host part (%s)"
+                          % ("packing of the edited chunks on the host, pool ranges, one pinned upload of the "
+                             "packed voxels" if os.environ.get("DN_HOST_PACKING", "0") not in ("", "0") else
+                             "the surface count of each edited chunk, pool ranges, one pinned upload of the "
+                             "chunks' voxels; the packing itself runs on the device, k_pack_stage"),
+        "packing": "host" if os.environ.get("DN_HOST_PACKING", "0") not in ("", "0") else "device",
         "wall_ms_per_step": wall * 1e3 / K, "build_s": build_s,
         "gpu_launches": int(allreduce_sum(pg, launches)), "clocks": clk,
     }
@@ -873,6 +879,7 @@ def serving_sweep(args, lib, rank, world, nmaps, rates, seconds, budget_gb, stop
         return reqs, offs
 
     server.start()
+    pinned_start = lib.dn_cuda_host_pinned()
     # warm-up: every map drawn once and relit once
     warm = []
     for vi in range(len(vols)):
@@ -884,6 +891,7 @@ def serving_sweep(args, lib, rank, world, nmaps, rates, seconds, budget_gb, stop
         server.submit(q)
     assert server.drain(1800.0), "warm-up did not drain"
     server.poll()
+    pinned_warm = lib.dn_cuda_host_pinned()
     sweep = []
     lib.DN_batch_reset_stats(lib.DN_server_batch(server.ptr))
     tot_rays, tot_s = 0, 0.0
@@ -891,6 +899,7 @@ def serving_sweep(args, lib, rank, world, nmaps, rates, seconds, budget_gb, stop
         reqs, offs = make_requests(rate, seconds)
         st0 = server.stats()
         b0 = server.batch_stats()
+        pin0 = lib.dn_cuda_host_pinned()
         t0 = time.perf_counter()
         server.replay(reqs, offs)
         ok = server.drain(args.drain_timeout)
@@ -921,10 +930,13 @@ def serving_sweep(args, lib, rank, world, nmaps, rates, seconds, budget_gb, stop
                "server_issue_s": st1["issueSeconds"] - st0["issueSeconds"],
                "server_evict_s": st1["evictSeconds"] - st0["evictSeconds"],
                "server_restore_s": st1["restoreSeconds"] - st0["restoreSeconds"],
-               "device_s": st1["deviceSeconds"] - st0["deviceSeconds"]}
+               "device_s": st1["deviceSeconds"] - st0["deviceSeconds"],
+               "host_pinned_gb": lib.dn_cuda_host_pinned() / 2**30,
+               "host_pinned_grown_gb": (lib.dn_cuda_host_pinned() - pin0) / 2**30}
         log("rate %g: %s" % (rate, {k: row[k] for k in ("completed", "achieved_rps", "p50_ms", "p99_ms", "rays_per_s",
                                                        "evictions", "restores", "server_admit_s", "server_evict_s",
-                                                       "server_restore_s", "server_issue_s", "device_s")}))
+                                                       "server_restore_s", "server_issue_s", "device_s",
+                                                       "host_pinned_gb", "host_pinned_grown_gb")}))
         sweep.append(row)
         # past saturation the queue only grows: stop the sweep there
         if not ok or (row["achieved_rps"] or 0.0) < 0.9 * rate:
@@ -949,6 +961,8 @@ def serving_sweep(args, lib, rank, world, nmaps, rates, seconds, budget_gb, stop
         "max_rps_with_p99_le_33ms": best["achieved_rps"] if best else None,
         "resident_bytes": st["residentBytes"], "resident_maps": st["residentVolumes"],
         "evictions": st["evictions"], "restores": st["restores"], "build_s": build_s,
+        "host_pinned_gb": {"after_start": pinned_start / 2**30, "after_warmup": pinned_warm / 2**30,
+                           "end": lib.dn_cuda_host_pinned() / 2**30},
     }
     server.close()
     for imgs in ring.values():

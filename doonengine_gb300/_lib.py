@@ -267,6 +267,7 @@ _SIGS = [
     ("DN_server_batch", c_void_p, [c_void_p]),
     ("DN_server_clock", c_double, []),
     ("dn_pack_chunk", c_uint32, [VOLP, POINTER(DNchunk), c_void_p, c_void_p, c_void_p]),
+    ("dn_count_surface", c_uint32, [VOLP, POINTER(DNchunk)]),
     ("dn_scene_palette", None, [VOLP, c_uint32, c_uint32, c_uint32, c_float, c_float, c_float]),
     ("dn_scene_terrain", None, [VOLP, c_uint32, c_float, c_float, c_uint32, c_uint32]),
     ("dn_scene_shapes", None, [VOLP, c_uint32, c_uint32, c_int32, c_int32, c_uint32, c_float, c_float]),
@@ -310,6 +311,10 @@ _SIGS = [
     ("dn_cuda_device_sync", c_int, []),
     ("dn_cuda_flush_l2", c_int, [c_void_p, c_size_t]),
     ("dn_cuda_sync_stage", c_int, [c_void_p, c_void_p, c_uint32, c_void_p, c_uint32, c_void_p, c_uint64]),
+    ("dn_cuda_sync_chunks", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p, c_uint32, c_void_p]),
+    ("dn_cuda_sync_stage_chunks", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p, c_uint32, c_void_p]),
+    ("dn_cuda_export_chunk", c_int, [c_void_p, c_uint32, c_void_p, c_void_p, c_void_p]),
+    ("dn_cuda_stage_part_limit", c_size_t, [c_size_t]),
     ("dn_cuda_batch_create", c_int, [POINTER(c_void_p)]),
     ("dn_cuda_batch_destroy", None, [c_void_p]),
     ("dn_cuda_batch_add", c_int, [c_void_p, c_void_p]),

@@ -670,6 +670,85 @@ __global__ void k_sync_stage(const dn_tile_op* ops, uint32_t nops, const dn_chun
     }
 }
 
+// Packs and publishes staged chunks from the voxels of the CPU map (one 512-thread block per op); the
+// packing of voxel.c:1397-1461 restated per voxel.  Thread i is voxel i = x + 8*(y + 8*z), which is bit i
+// of the occupancy mask, so warp w's ballot is mask word w; the CPU array is stored [x][y][z].  A solid
+// voxel is kept when one of its six face neighbours is outside the chunk or see-through (voxel.c:1391-1394).
+// Kept voxels go to the record's pool range in mask order (their rank), with linear albedo.  The host
+// counted the kept voxels to size the range; a record whose count differs is not published.
+__global__ void __launch_bounds__(512) k_pack_stage(const dn_tile_op* ops, uint32_t nops, const dn_chunk_record* recs,
+                                                    const uint2* raw, const dn_pack_params* pk, uint32_t* tpend,
+                                                    uint32_t* tpendSlot, ChunkRec* rec, uint32_t* nsamples, uint2* vox,
+                                                    float4* diff, float4* spec, uint32_t slotCap, uint64_t voxCap,
+                                                    uint64_t ntiles, DevState* st)
+{
+    __shared__ uint8_t thru[512];
+    __shared__ uint8_t lin[256];
+    __shared__ uint32_t see[8], maskW[16], mats[8];
+    const uint32_t i = threadIdx.x, lane = i & 31u, warp = i >> 5;
+    const uint32_t x = i & 7u, y = (i >> 3) & 7u, z = i >> 6;
+    const uint32_t r = (x << 6) | (y << 3) | z;
+    if (i < 8) see[i] = pk->seeThrough[i];
+    if (i < 256) lin[i] = pk->linear[i];
+    for (uint32_t o = blockIdx.x; o < nops; o += gridDim.x) {
+        const dn_tile_op op = ops[o];
+        __syncthreads();   // the previous op's shared-memory reads are done (and the tables are written)
+        if (op.tile >= ntiles) { if (i == 0) atomicOr(&st->w[ST_ERR], ERRF_TILE); continue; }
+        if (!(op.flags & DN_PEND_STAGED)) {
+            if (i == 0) { tpend[op.tile] = op.flags; tpendSlot[op.tile] = op.slot; }
+            continue;
+        }
+        const dn_chunk_record* src = &recs[op.recordIndex];
+        const uint2 v = raw[(size_t)op.recordIndex * 512u + r];
+        const uint32_t m = v.x >> 24;
+        thru[i] = (uint8_t)((see[m >> 5] >> (m & 31u)) & 1u);
+        if (i < 8) mats[i] = 0;
+        __syncthreads();
+        const bool keep = m != 255u &&
+            (x == 7u || thru[i + 1] || x == 0u || thru[i - 1] || y == 7u || thru[i + 8] || y == 0u || thru[i - 8] ||
+             z == 7u || thru[i + 64] || z == 0u || thru[i - 64]);
+        const uint32_t ball = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) maskW[warp] = ball;
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+        #pragma unroll
+        for (uint32_t w = 0; w < 16; w++) {
+            const uint32_t c = __popc(maskW[w]);
+            before += w < warp ? c : 0u;
+            total += c;
+        }
+        const uint32_t nvox = src->nvox, base = src->voxBase;
+        const bool bad = op.slot >= slotCap || nvox != total || (uint64_t)base + total > voxCap;
+        if (i == 0) {
+            tpend[op.tile] = bad ? (op.flags & ~DN_PEND_STAGED) : op.flags;
+            tpendSlot[op.tile] = bad ? DN_SLOT_NONE : op.slot;
+            if (bad) atomicOr(&st->w[ST_ERR], ERRF_RECORD);
+        }
+        if (bad) continue;
+        if (keep) {
+            const uint64_t d = (uint64_t)base + before + __popc(ball & ((1u << lane) - 1u));
+            const uint32_t a = v.y;
+            vox[d] = make_uint2(v.x, ((uint32_t)lin[a >> 24] << 24) | ((uint32_t)lin[(a >> 16) & 0xFFu] << 16) |
+                                     ((uint32_t)lin[(a >> 8) & 0xFFu] << 8));
+            diff[d] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            spec[d] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            atomicOr(&mats[m >> 5], 1u << (m & 31u));
+        }
+        __syncthreads();
+        ChunkRec* dst = &rec[op.slot];
+        if (i < 16) dst->mask[i] = maskW[i];
+        else if (i < 19) {
+            uint32_t c = 0;
+            for (uint32_t w = 0; w < 4u * (i - 15u); w++) c += __popc(maskW[w]);
+            dst->partial[i - 16] = c;
+        } else if (i == 19) dst->nvox = total;
+        else if (i < 23) dst->pos[i - 20] = src->pos[i - 20];
+        else if (i == 23) dst->voxBase = base;
+        else if (i < 32) dst->matSet[i - 24] = mats[i - 24];
+        else if (i == 32) nsamples[op.slot] = 0;
+    }
+}
+
 // DN_sync_gpu's per-tile pass (compact_tiles) over every tile of one map
 __global__ void __launch_bounds__(256) k_compact(const __grid_constant__ CompactArgs a)
 {
@@ -681,6 +760,8 @@ __global__ void k_clamp_requests(DevState* st, uint64_t cap)
 {
     if (st->w[ST_REQ] > cap) st->w[ST_REQ] = (uint32_t)cap;
 }
+
+static int stage_reserve(DNgpuVolume* g, size_t total);
 
 int dn_stage_ops(DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops, const dn_chunk_record* records,
                  uint32_t nrecords, const uint32_t* voxelWords, uint64_t nvoxels)
@@ -694,24 +775,8 @@ int dn_stage_ops(DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops, const dn_
         const size_t oRec = (bOps + 15) & ~(size_t)15, oOff = (oRec + bRec + 15) & ~(size_t)15,
                      oVox = (oOff + bOff + 15) & ~(size_t)15, total = oVox + bVox;
         CK(cudaEventSynchronize(g->stageFree));
-        if (total > g->hstageCap) {
-            if (g->hstage) cudaFreeHost(g->hstage);
-            g->hstage = nullptr;
-            size_t nc = total + total / 2 + 4096;
-            COUNT_ALLOC();
-            CK(cudaMallocHost((void**)&g->hstage, nc));
-            g->hstageCap = nc;
-        }
-        if (total > g->dstageCap) {
-            // a pooled buffer is freed in stream order after the kernels that read it; a cudaMalloc one
-            // needs the stream drained first
-            if (!(g->poolMask & vol_array_bit(g, &g->dstage))) CK(cudaStreamSynchronize(g->stream));
-            vfree(g, g->dstage);
-            size_t nc = total + total / 2 + 4096;
-            int rc = valloc(g, g->dstage, nc);
-            if (rc) { g->dstageCap = 0; return rc; }
-            g->dstageCap = nc;
-        }
+        int rc = stage_reserve(g, total);
+        if (rc) return rc;
         memcpy(g->hstage, ops, bOps);
         if (bRec) memcpy(g->hstage + oRec, records, bRec);
         uint64_t* off = (uint64_t*)(g->hstage + oOff);
@@ -734,6 +799,168 @@ int dn_stage_ops(DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops, const dn_
     return DN_CUDA_OK;
 }
 
+static const size_t STAGE_PART_DEFAULT = (size_t)16 << 20;
+static const size_t CHUNK_VOXEL_BYTES = 512u * 8u;
+static size_t g_stagePart = STAGE_PART_DEFAULT;
+
+extern "C" size_t dn_cuda_stage_part_limit(size_t bytes)
+{
+    const size_t prev = g_stagePart;
+    g_stagePart = bytes ? bytes : STAGE_PART_DEFAULT;
+    return prev;
+}
+
+// grows the volume's pinned and device staging buffers to 'total' bytes (the host buffer must be free)
+static int stage_reserve(DNgpuVolume* g, size_t total)
+{
+    if (total > g->hstageCap) {
+        if (g->hstage) cudaFreeHost(g->hstage);
+        g->hstage = nullptr;
+        g->hstageCap = 0;
+        size_t nc = total + total / 2 + 4096;
+        COUNT_ALLOC();
+        CK(cudaMallocHost((void**)&g->hstage, nc));
+        g->hstageCap = nc;
+    }
+    if (total > g->dstageCap) {
+        if (!(g->poolMask & vol_array_bit(g, &g->dstage))) CK(cudaStreamSynchronize(g->stream));
+        vfree(g, g->dstage);
+        size_t nc = total + total / 2 + 4096;
+        int rc = valloc(g, g->dstage, nc);
+        if (rc) { g->dstageCap = 0; return rc; }
+        g->dstageCap = nc;
+    }
+    return DN_CUDA_OK;
+}
+
+// Staging with packing on the device: params | ops | records | chunk voxels, in parts of at most
+// g_stagePart bytes (or one op); each part's ops name its own records (recordIndex rebased to the part)
+static int dn_stage_chunks(DNgpuVolume* g, const dn_pack_params* pk, const dn_tile_op* ops, uint32_t nops,
+                           const dn_chunk_record* records, uint32_t nrecords, const void* const* chunkVoxels)
+{
+    for (uint32_t o = 0; o < nops; o++)
+        if ((ops[o].flags & DN_PEND_STAGED) && ops[o].recordIndex >= nrecords)
+            return dn_set_err(DN_CUDA_ERR_ARG, "op %u references record %u of %u", o, ops[o].recordIndex, nrecords);
+    for (uint32_t r = 0; r < nrecords; r++)
+        if (!chunkVoxels[r] || records[r].nvox > 512u)
+            return dn_set_err(DN_CUDA_ERR_ARG, "record %u: %s", r, chunkVoxels[r] ? "more than 512 voxels" : "no voxels");
+    const size_t perOp = sizeof(dn_tile_op) + sizeof(dn_chunk_record) + CHUNK_VOXEL_BYTES;
+    const size_t oOps = (sizeof(dn_pack_params) + 15) & ~(size_t)15;
+    uint32_t o0 = 0;
+    while (o0 < nops) {
+        // the part: ops o0 .. o1-1, at most g_stagePart bytes (at least one op)
+        uint32_t o1 = o0, nrec = 0;
+        size_t bytes = oOps + 64;
+        while (o1 < nops) {
+            const bool staged = (ops[o1].flags & DN_PEND_STAGED) != 0;
+            const size_t add = staged ? perOp : sizeof(dn_tile_op);
+            if (o1 > o0 && bytes + add > g_stagePart) break;
+            bytes += add;
+            nrec += staged;
+            o1++;
+        }
+        const uint32_t n = o1 - o0;
+        const size_t oRec = (oOps + (size_t)n * sizeof(dn_tile_op) + 15) & ~(size_t)15;
+        const size_t oVox = (oRec + (size_t)nrec * sizeof(dn_chunk_record) + 15) & ~(size_t)15;
+        const size_t total = oVox + (size_t)nrec * CHUNK_VOXEL_BYTES;
+        CK(cudaEventSynchronize(g->stageFree));
+        int rc = stage_reserve(g, total);
+        if (rc) return rc;
+        memcpy(g->hstage, pk, sizeof(dn_pack_params));
+        dn_tile_op* hops = (dn_tile_op*)(g->hstage + oOps);
+        dn_chunk_record* hrec = (dn_chunk_record*)(g->hstage + oRec);
+        unsigned char* hvox = g->hstage + oVox;
+        uint32_t k = 0;
+        for (uint32_t j = 0; j < n; j++) {
+            dn_tile_op op = ops[o0 + j];
+            if (op.flags & DN_PEND_STAGED) {
+                hrec[k] = records[op.recordIndex];
+                memcpy(hvox + (size_t)k * CHUNK_VOXEL_BYTES, chunkVoxels[op.recordIndex], CHUNK_VOXEL_BYTES);
+                op.recordIndex = k++;
+            }
+            hops[j] = op;
+        }
+        CK(cudaMemcpyAsync(g->dstage, g->hstage, total, cudaMemcpyHostToDevice, g->stream));
+        CK(cudaEventRecord(g->stageFree, g->stream));
+        COUNT_LAUNCH();
+        k_pack_stage<<<n < 65535u ? n : 65535u, 512, 0, g->stream>>>(
+            (const dn_tile_op*)(g->dstage + oOps), n, (const dn_chunk_record*)(g->dstage + oRec),
+            (const uint2*)(g->dstage + oVox), (const dn_pack_params*)g->dstage, g->tpend, g->tpendSlot, g->rec,
+            g->nsamples, g->vox, g->diff, g->spec, g->slotCap, g->voxCap, g->ntiles, g->st);
+        CK(cudaGetLastError());
+        o0 = o1;
+    }
+    return DN_CUDA_OK;
+}
+
+// the per-tile pass of a sync after its staging (compact_tiles), then the request count's clamp
+static int sync_tiles(DNgpuVolume* g, const dn_sync_params* p)
+{
+    CK(cudaMemsetAsync(&g->st->w[ST_REQ], 0, 4, g->stream));
+    CompactArgs a;
+    a.tword = g->tword; a.tbits = g->tbits; a.treq = g->treq; a.tvis = g->tvis; a.ttouch = g->ttouch; a.tlast = g->tlast;
+    a.tpend = g->tpend; a.tpendSlot = g->tpendSlot; a.rec = g->rec;
+    a.reqs = g->reqs; a.reqCap = g->reqCap; a.st = g->st; a.ntiles = g->ntiles;
+    a.op = p->op; a.split = p->split; a.frameNum = p->frameNum;
+    uint64_t blocks = (g->ntiles + 255) / 256;
+    uint32_t maxBlocks = (uint32_t)(g->numSMs > 0 ? g->numSMs * 8 : 1024);
+    COUNT_LAUNCH();
+    k_compact<<<(uint32_t)(blocks < maxBlocks ? blocks : maxBlocks), 256, 0, g->stream>>>(a);
+    CK(cudaGetLastError());
+    COUNT_LAUNCH();
+    k_clamp_requests<<<1, 1, 0, g->stream>>>(g->st, g->reqCap);
+    CK(cudaGetLastError());
+    return DN_CUDA_OK;
+}
+
+extern "C" int dn_cuda_sync_stage_chunks(DNgpuVolume* g, const dn_pack_params* pk, const dn_tile_op* ops, uint32_t nops,
+                                         const dn_chunk_record* records, uint32_t nrecords, const void* const* chunkVoxels)
+{
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (!g || !pk || (nops && !ops) || (nrecords && (!records || !chunkVoxels))) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
+    CK(cudaSetDevice(g->device));
+    return dn_stage_chunks(g, pk, ops, nops, records, nrecords, chunkVoxels);
+}
+
+extern "C" int dn_cuda_sync_chunks(DNgpuVolume* g, const dn_sync_params* p, const dn_pack_params* pk, const dn_tile_op* ops,
+                                   uint32_t nops, const dn_chunk_record* records, uint32_t nrecords,
+                                   const void* const* chunkVoxels)
+{
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (!g || !p || !pk || (nops && !ops) || (nrecords && (!records || !chunkVoxels))) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
+    if (p->split == 0 || p->op > 2) return dn_set_err(DN_CUDA_ERR_ARG, "bad sync parameters");
+    CK(cudaSetDevice(g->device));
+    int rc = dn_stage_chunks(g, pk, ops, nops, records, nrecords, chunkVoxels);
+    if (rc) return rc;
+    return sync_tiles(g, p);
+}
+
+extern "C" int dn_cuda_export_chunk(DNgpuVolume* g, uint32_t tile, dn_chunk_record* recOut, uint32_t matSet[8],
+                                    uint32_t* words)
+{
+    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (!g || !recOut) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
+    if (tile >= g->ntiles) return dn_set_err(DN_CUDA_ERR_ARG, "tile %u of %llu", tile, (unsigned long long)g->ntiles);
+    CK(cudaSetDevice(g->device));
+    CK(cudaStreamSynchronize(g->stream));
+    uint32_t w = 0;
+    CK(cudaMemcpy(&w, &g->tword[tile], 4, cudaMemcpyDeviceToHost));
+    const uint32_t slot = w & dn::SLOT_MASK;
+    if (slot == DN_SLOT_NONE || slot >= g->slotCap) return dn_set_err(DN_CUDA_ERR_ARG, "tile %u has no record", tile);
+    ChunkRec r;
+    CK(cudaMemcpy(&r, &g->rec[slot], sizeof(ChunkRec), cudaMemcpyDeviceToHost));
+    if (r.nvox > 512u || (uint64_t)r.voxBase + r.nvox > g->voxCap)
+        return dn_set_err(DN_CUDA_ERR_ARG, "tile %u: record out of range", tile);
+    memcpy(recOut->mask, r.mask, sizeof(r.mask));
+    memcpy(recOut->partial, r.partial, sizeof(r.partial));
+    recOut->nvox = r.nvox;
+    memcpy(recOut->pos, r.pos, sizeof(r.pos));
+    recOut->voxBase = r.voxBase;
+    if (matSet) memcpy(matSet, r.matSet, sizeof(r.matSet));
+    if (words && r.nvox) CK(cudaMemcpy(words, &g->vox[r.voxBase], (size_t)r.nvox * 8u, cudaMemcpyDeviceToHost));
+    return DN_CUDA_OK;
+}
+
 extern "C" int dn_cuda_sync_stage(DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops, const dn_chunk_record* records,
                                   uint32_t nrecords, const uint32_t* voxelWords, uint64_t nvoxels)
 {
@@ -753,21 +980,7 @@ extern "C" int dn_cuda_sync(DNgpuVolume* g, const dn_sync_params* p, const dn_ti
     CK(cudaSetDevice(g->device));
     int rc = dn_stage_ops(g, ops, nops, records, nrecords, voxelWords, nvoxels);
     if (rc) return rc;
-    CK(cudaMemsetAsync(&g->st->w[ST_REQ], 0, 4, g->stream));
-    CompactArgs a;
-    a.tword = g->tword; a.tbits = g->tbits; a.treq = g->treq; a.tvis = g->tvis; a.ttouch = g->ttouch; a.tlast = g->tlast;
-    a.tpend = g->tpend; a.tpendSlot = g->tpendSlot; a.rec = g->rec;
-    a.reqs = g->reqs; a.reqCap = g->reqCap; a.st = g->st; a.ntiles = g->ntiles;
-    a.op = p->op; a.split = p->split; a.frameNum = p->frameNum;
-    uint64_t blocks = (g->ntiles + 255) / 256;
-    uint32_t maxBlocks = (uint32_t)(g->numSMs > 0 ? g->numSMs * 8 : 1024);
-    COUNT_LAUNCH();
-    k_compact<<<(uint32_t)(blocks < maxBlocks ? blocks : maxBlocks), 256, 0, g->stream>>>(a);
-    CK(cudaGetLastError());
-    COUNT_LAUNCH();
-    k_clamp_requests<<<1, 1, 0, g->stream>>>(g->st, g->reqCap);
-    CK(cudaGetLastError());
-    return DN_CUDA_OK;
+    return sync_tiles(g, p);
 }
 
 extern "C" int dn_cuda_light(DNgpuVolume* g, const dn_light_params* p, const dn_material* materials)
@@ -1185,7 +1398,7 @@ extern "C" int dn_cuda_flush_l2(void* stream, size_t bytes)
 
 extern "C" const char* dn_cuda_kernel_names(void)
 {
-    return "k_draw;k_light_stream;k_light_packet;k_light_diffuse;k_light_tables;k_mark_opaque;k_commit;k_sync_stage;k_compact;k_clamp_requests;k_flush;"
+    return "k_draw;k_light_stream;k_light_packet;k_light_diffuse;k_light_tables;k_mark_opaque;k_commit;k_sync_stage;k_pack_stage;k_compact;k_clamp_requests;k_flush;"
            "k_draw_batch;k_compact_batch;k_batch_reset;k_batch_prep;k_mark_opaque_batch;k_light_stream_batch;k_light_packet_batch;"
            "k_light_diffuse_batch;k_commit_batch;k_batch_gather;"
            "k_shape_count;k_shape_write";

@@ -66,6 +66,7 @@ struct DNserver
 	pthread_t thread;
 	int started, stop;
 	int cancel;                      /* stop serving queued requests: they complete with ok = 0 */
+	int settled;                     /* the thread is idle with the resident set within the budget */
 	Tick ticks[2];
 	unsigned int tickHead, tickCount;
 	uint64_t tickNo;
@@ -166,6 +167,7 @@ uint64_t DN_server_submit(DNserver* s, const DNrequest* r)
 	s->inTail = p;
 	s->outstanding++;
 	s->stats.submitted++;
+	s->settled = 0;
 	pthread_cond_signal(&s->cond);
 	pthread_mutex_unlock(&s->lock);
 	return p->id;
@@ -458,6 +460,16 @@ static void* serve_main(void* arg)
 		for (unsigned int i = 0; i < s->nslots && !queued; i++) queued = s->slots[i].head != NULL;
 		if (stop && !queued && !s->tickCount) break;
 		if (s->tickCount) { sleep_us(20); continue; }
+		if (!queued && !s->settled) {
+			/* idle: volumes grow when their syncs stage chunks, so a busy period can end above the budget;
+			 * evict down to it now, while no request waits (DN_server_drain waits for this too) */
+			enforce_budget(s, 0, NULL);
+			pthread_mutex_lock(&s->lock);
+			if (!s->inHead) s->settled = 1;
+			pthread_cond_broadcast(&s->cond);
+			pthread_mutex_unlock(&s->lock);
+			continue;
+		}
 		/* idle: wait for a submission */
 		pthread_mutex_lock(&s->lock);
 		if (!s->inHead && !s->stop) {
@@ -469,6 +481,10 @@ static void* serve_main(void* arg)
 		}
 		pthread_mutex_unlock(&s->lock);
 	}
+	pthread_mutex_lock(&s->lock);
+	s->settled = 1;
+	pthread_cond_broadcast(&s->cond);
+	pthread_mutex_unlock(&s->lock);
 	return NULL;
 }
 
@@ -482,6 +498,9 @@ bool DN_server_start(DNserver* s)
 		if (used > s->cfg.deviceBudgetBytes) {
 			const uint64_t over = used - s->cfg.deviceBudgetBytes;
 			if (dn_cuda_host_reserve(over + over / 4) != DN_CUDA_OK) return false;
+			/* and evict down to the budget before the first request arrives, so that no request waits on
+			 * the start's evictions (counted in the stats like any other) */
+			if (!enforce_budget(s, 0, NULL)) return false;
 		}
 	}
 	s->stop = 0;
@@ -495,7 +514,7 @@ bool DN_server_drain(DNserver* s, double timeout)
 	if (!s) return false;
 	const double end = DN_server_clock() + timeout;
 	pthread_mutex_lock(&s->lock);
-	while (s->outstanding) {
+	while (s->outstanding || (s->started && !s->settled)) {
 		if (DN_server_clock() > end) { pthread_mutex_unlock(&s->lock); return false; }
 		struct timespec ts;
 		clock_gettime(CLOCK_REALTIME, &ts);

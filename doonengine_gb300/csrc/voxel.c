@@ -27,6 +27,7 @@
 #include "dn_cuda.h"
 #include "dn_residency.h"
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 #include <stdarg.h>
 #include <pthread.h>
@@ -103,7 +104,10 @@ typedef struct DNvolumePriv
 	/* sync scratch */
 	dn_tile_op* ops; size_t opsCap;
 	dn_chunk_record* recs; size_t recsCap;
-	uint32_t* vwords; size_t vwordsCap;   /* in uint32 units */
+	uint32_t* vwords; size_t vwordsCap;   /* in uint32 units; DN_HOST_PACKING only */
+	const void** chunkVox; size_t chunkVoxCap;   /* per staged record: its chunk's voxels (packed on the device) */
+	dn_pack_params pack;       /* the packing parameters of the sync being prepared */
+	int hostPack;              /* DN_HOST_PACKING=1 at creation: records are packed on the host */
 	u32vec deferredSlots;
 	/* the last view/projection passed to DN_draw */
 	float sphereK; float spherePts[64][3]; uint32_t sphereValid;
@@ -189,7 +193,7 @@ static void free_priv_arrays(DNvolumePriv* p)
 	DN_FREE(p->dirty); DN_FREE(p->dirtyList.v); DN_FREE(p->tileSlot);
 	DN_FREE(p->freeSlots.v); DN_FREE(p->slotBase); DN_FREE(p->slotClass); DN_FREE(p->slotGroups);
 	for (int c = 0; c < NUM_CLASSES; c++) DN_FREE(p->freeRanges[c].v);
-	DN_FREE(p->ops); DN_FREE(p->recs); DN_FREE(p->vwords); DN_FREE(p->deferredSlots.v);
+	DN_FREE(p->ops); DN_FREE(p->recs); DN_FREE(p->vwords); DN_FREE(p->chunkVox); DN_FREE(p->deferredSlots.v);
 }
 
 static bool alloc_tile_arrays(DNvolumePriv* p, size_t tiles)
@@ -240,6 +244,10 @@ static DNvolume* create_volume(DNuvec3 mapSize, unsigned int minChunks, int with
 	}
 	memset(p, 0, sizeof(*p));
 	DNvolume* vol = &p->pub;
+	{
+		const char* hp = getenv("DN_HOST_PACKING");
+		p->hostPack = hp && atoi(hp) != 0;
+	}
 
 	/* sized from x*y*z (the reference sizes its GPU buffers from x*y*x, voxel.c:173, 184) */
 	size_t numChunks = tiles < minChunks ? tiles : (size_t)minChunks;
@@ -803,6 +811,47 @@ static uint32_t pack_chunk(const DNvolume* vol, const DNchunk* c, dn_chunk_recor
 	return n;
 }
 
+/* the materials a face is seen through at this sync (voxel.c:1391-1394): empty, or opacity < 1 */
+static void pack_params(const DNvolume* vol, dn_pack_params* pk)
+{
+	memset(pk->seeThrough, 0, sizeof(pk->seeThrough));
+	for (uint32_t m = 0; m < DN_MAX_MATERIALS; m++)
+		if (m == DN_MATERIAL_EMPTY || vol->materials[m].opacity < 1.0f) pk->seeThrough[m >> 5] |= 1u << (m & 31);
+	memcpy(pk->linear, s_linear, sizeof(pk->linear));
+}
+
+/* The number of voxels pack_chunk keeps: the same cull on 64-bit boards of the chunk's [x][y][z] storage,
+ * word x holding bit 8*y + z, so one shift tests a face neighbour of 64 voxels at once.  The device packs
+ * the chunk itself (dn_cuda_sync_chunks); the host needs only this count to size the chunk's pool range. */
+static uint32_t count_kept(const DNchunk* c, const uint32_t see[8])
+{
+	uint64_t solid[8], thru[8];
+	for (int x = 0; x < 8; x++) {
+		const DNcompressedVoxel* v = &c->voxels[x][0][0];
+		uint64_t sb = 0, tb = 0;
+		for (int i = 0; i < 64; i++) {
+			const uint32_t m = GET_MATERIAL_ID(v[i].normal);
+			sb |= (uint64_t)(m != DN_MATERIAL_EMPTY) << i;
+			tb |= (uint64_t)((see[m >> 5] >> (m & 31)) & 1u) << i;
+		}
+		solid[x] = sb; thru[x] = tb;
+	}
+	uint32_t n = 0;
+	for (int x = 0; x < 8; x++) {
+		const uint64_t t = thru[x];
+		/* a neighbour outside the chunk counts as see-through: z = 7 and z = 0 are bits 7 and 0 of each
+		 * byte, y = 7 and y = 0 the top and bottom byte, x = 7 and x = 0 the last and first word */
+		uint64_t nb = (t >> 1) | 0x8080808080808080ull;   /* z + 1 */
+		nb |= (t << 1) | 0x0101010101010101ull;           /* z - 1 */
+		nb |= (t >> 8) | 0xFF00000000000000ull;           /* y + 1 */
+		nb |= (t << 8) | 0x00000000000000FFull;           /* y - 1 */
+		nb |= x < 7 ? thru[x + 1] : ~0ull;
+		nb |= x > 0 ? thru[x - 1] : ~0ull;
+		n += (uint32_t)__builtin_popcountll(solid[x] & nb);
+	}
+	return n;
+}
+
 /* ---------------------------------------------------- slot / range allocator */
 
 static uint32_t class_of(uint32_t nvox)
@@ -864,6 +913,38 @@ static bool grow_scratch(void** buf, size_t* cap, size_t need, size_t elem)
 }
 
 /* ---------------------------------------------------------------- sync */
+
+/* room for one more staged record: record 'nrecs', with its words from vwords[nvw] when packed here */
+static bool grow_stage(DNvolumePriv* p, size_t nrecs, uint64_t nvw)
+{
+	if (!grow_scratch((void**)&p->recs, &p->recsCap, nrecs + 1, sizeof(dn_chunk_record))) return false;
+	if (p->hostPack) return grow_scratch((void**)&p->vwords, &p->vwordsCap, (size_t)nvw + 1024, sizeof(uint32_t));
+	return grow_scratch((void**)&p->chunkVox, &p->chunkVoxCap, nrecs + 1, sizeof(void*));
+}
+
+/* record 'ri' of the sync for chunk c: packed here with DN_HOST_PACKING (its words to vwords[nvw]), else only
+ * counted here and packed on the device from the chunk's voxels.  Returns the kept-voxel count. */
+static uint32_t stage_record(DNvolume* vol, const DNchunk* c, uint32_t ri, uint64_t nvw)
+{
+	DNvolumePriv* p = priv(vol);
+	dn_chunk_record* r = &p->recs[ri];
+	if (p->hostPack) return pack_chunk(vol, c, r, &p->vwords[nvw]);
+	memset(r, 0, sizeof(*r));
+	r->nvox = count_kept(c, p->pack.seeThrough);
+	p->chunkVox[ri] = &c->voxels[0][0][0];
+	return r->nvox;
+}
+
+/* the device half of a sync prepared by sync_prepare (per-tile pass included unless stageOnly) */
+static int sync_issue(DNvolume* vol, const dn_sync_params* sp, uint32_t nops, uint32_t nrecs, uint64_t nvw, int stageOnly)
+{
+	DNvolumePriv* p = priv(vol);
+	if (p->hostPack)
+		return stageOnly ? dn_cuda_sync_stage(vol->gpu, p->ops, nops, p->recs, nrecs, p->vwords, nvw / 2)
+		                 : dn_cuda_sync(vol->gpu, sp, p->ops, nops, p->recs, nrecs, p->vwords, nvw / 2);
+	return stageOnly ? dn_cuda_sync_stage_chunks(vol->gpu, &p->pack, p->ops, nops, p->recs, nrecs, p->chunkVox)
+	                 : dn_cuda_sync_chunks(vol->gpu, sp, &p->pack, p->ops, nops, p->recs, nrecs, p->chunkVox);
+}
 
 /* the op of tile t in the sync being prepared, appended (with 'flags') when the tile has none; -1 when
  * the scratch cannot grow */
@@ -929,13 +1010,12 @@ static bool lru_pass(DNvolume* vol, DNmemOp op, uint32_t* nops, uint32_t* nrecs,
 				staged = false;
 				long oi = lru_op(p, t, nops, DN_PEND_VALID | DN_PEND_EXISTS);
 				uint32_t slot;
-				if (oi < 0 || !grow_scratch((void**)&p->recs, &p->recsCap, (size_t)*nrecs + 1, sizeof(dn_chunk_record)) ||
-				    !grow_scratch((void**)&p->vwords, &p->vwordsCap, (size_t)*nvw + 1024, sizeof(uint32_t))) {
+				if (oi < 0 || !grow_stage(p, *nrecs, *nvw)) {
 					dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to allocate sync scratch");
 					ok = false;
 				} else {
 					dn_chunk_record* rec = &p->recs[*nrecs];
-					uint32_t n = pack_chunk(vol, c, rec, &p->vwords[*nvw]);
+					uint32_t n = stage_record(vol, c, *nrecs, *nvw);
 					if (!alloc_slot(p, n, &slot)) {
 						dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "failed to stage a chunk on the device");
 					} else {
@@ -996,10 +1076,12 @@ static bool sync_prepare(DNvolume* vol, DNmemOp op, int lightingSplit, dn_sync_p
 	size_t nd = p->dirtyList.n;
 	if (!grow_scratch((void**)&p->ops, &p->opsCap, nd ? nd : 1, sizeof(dn_tile_op)) ||
 	    !grow_scratch((void**)&p->recs, &p->recsCap, nd ? nd : 1, sizeof(dn_chunk_record)) ||
-	    !grow_scratch((void**)&p->vwords, &p->vwordsCap, (nd ? nd : 1) * 1024, sizeof(uint32_t))) {
+	    !(p->hostPack ? grow_scratch((void**)&p->vwords, &p->vwordsCap, (nd ? nd : 1) * 1024, sizeof(uint32_t))
+	                  : grow_scratch((void**)&p->chunkVox, &p->chunkVoxCap, nd ? nd : 1, sizeof(void*)))) {
 		dn_msg(DN_MESSAGE_CPU_MEMORY, DN_MESSAGE_ERROR, "failed to allocate sync scratch");
 		return false;
 	}
+	pack_params(vol, &p->pack);
 	uint32_t nops = 0, nrecs = 0;
 	uint64_t nvw = 0;
 	p->deferredSlots.n = 0;
@@ -1017,7 +1099,7 @@ static bool sync_prepare(DNvolume* vol, DNmemOp op, int lightingSplit, dn_sync_p
 			if (vol->map[t].flag) {
 				DNchunk* c = &vol->chunks[vol->map[t].chunkIndex];
 				dn_chunk_record* r = &p->recs[nrecs];
-				uint32_t n = pack_chunk(vol, c, r, &p->vwords[nvw]);
+				uint32_t n = stage_record(vol, c, nrecs, nvw);
 				uint32_t slot;
 				if (!alloc_slot(p, n, &slot)) {
 					dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "failed to stage a chunk on the device");
@@ -1079,7 +1161,7 @@ void DN_sync_gpu(DNvolume* vol, DNmemOp op, int lightingSplit)
 	uint32_t nops = 0, nrecs = 0;
 	uint64_t nvw = 0;
 	if (!sync_prepare(vol, op, lightingSplit, &sp, &nops, &nrecs, &nvw)) return;
-	int rc = dn_cuda_sync(vol->gpu, &sp, p->ops, nops, p->recs, nrecs, p->vwords, nvw / 2);
+	int rc = sync_issue(vol, &sp, nops, nrecs, nvw, 0);
 	if (rc != DN_CUDA_OK)
 		dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "device sync failed: %s", dn_cuda_last_error());
 	sync_done(vol);
@@ -1469,6 +1551,13 @@ uint32_t dn_pack_chunk(const DNvolume* vol, const DNchunk* chunk, uint32_t mask[
 	return n;
 }
 
+uint32_t dn_count_surface(const DNvolume* vol, const DNchunk* chunk)
+{
+	dn_pack_params pk;
+	pack_params(vol, &pk);
+	return count_kept(chunk, pk.seeThrough);
+}
+
 /* ---------------------------------------------------------------- batches */
 
 struct DNbatch
@@ -1588,7 +1677,7 @@ bool DN_batch_run(DNbatch* b, const DNbatchItem* items, unsigned int count)
 			uint32_t nops = 0, nrecs = 0;
 			uint64_t nvw = 0;
 			if (!sync_prepare(vol, it->op, it->lightingSplit, &d->sync, &nops, &nrecs, &nvw)) return false;
-			int rc = dn_cuda_sync_stage(vol->gpu, p->ops, nops, p->recs, nrecs, p->vwords, nvw / 2);
+			int rc = sync_issue(vol, NULL, nops, nrecs, nvw, 1);
 			sync_done(vol);
 			if (rc != DN_CUDA_OK) {
 				dn_msg(DN_MESSAGE_GPU_MEMORY, DN_MESSAGE_ERROR, "device sync failed: %s", dn_cuda_last_error());

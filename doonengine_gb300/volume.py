@@ -323,6 +323,25 @@ class Volume:
         fn, rest = args[k]
         fn(self.ptr, vox, bool(flip), *rest, q, func, user)
 
+    def export_chunk(self, tile):
+        """The device record of a loaded tile (dn_cuda_export_chunk): dict of mask (16 words), partial (3),
+        nvox, pos, voxBase, matSet (8 words) and words (nvox x 2: normal word, linear albedo word), or None
+        when the tile has no record"""
+        rec = np.zeros(24, np.uint32)
+        mats = np.zeros(8, np.uint32)
+        words = np.zeros(1024, np.uint32)
+        rc = self.lib.dn_cuda_export_chunk(self.s.gpu, int(tile), rec.ctypes.data, mats.ctypes.data, words.ctypes.data)
+        if rc != 0:
+            return None
+        n = int(rec[19])
+        return {"mask": rec[:16].copy(), "partial": rec[16:19].copy(), "nvox": n, "pos": rec[20:23].view(np.int32).copy(),
+                "voxBase": int(rec[23]), "matSet": mats, "words": words[: 2 * n].reshape(n, 2).copy()}
+
+    def cpu_chunk(self, tile):
+        """The CPU map's chunk of a tile (a DNchunk), or None when the tile has none"""
+        h = self.s.map[int(tile)]
+        return self.s.chunks[h.chunkIndex] if h.flag else None
+
     def export_voxels(self):
         """(normal words, albedo words, tile flags) of the CPU map, dense"""
         sx, sy, sz = self.map_size

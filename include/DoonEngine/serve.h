@@ -98,13 +98,17 @@ void DN_server_destroy(DNserver* server);
 int DN_server_add_volume(DNserver* server, DNvolume* vol);
 /* starts the serving thread.  When the volumes' device footprint exceeds the budget, the pinned host memory
  * their evictions need (the excess plus a quarter) is reserved here (dn_cuda_host_reserve), so that no
- * eviction under load pins host memory; false if that reservation fails */
+ * eviction under load pins host memory, and volumes are evicted down to the budget (least recently used
+ * first; volumes not used yet in the order they were added) before the thread takes requests; false if the
+ * reservation or an eviction fails */
 bool DN_server_start(DNserver* server);
 /* thread-safe; returns the request id (> 0), or 0 for an invalid request */
 uint64_t DN_server_submit(DNserver* server, const DNrequest* request);
 /* submits requests[i] at offsets[i] seconds after the call (non-decreasing) from the calling thread */
 size_t DN_server_replay(DNserver* server, const DNrequest* requests, const double* offsets, size_t count);
-/* waits until every submitted request has completed (false on timeout) */
+/* waits until every submitted request has completed and the serving thread is idle with its resident set
+ * within the budget: volumes grow when their syncs stage chunks, and the idle thread evicts (least recently
+ * used first) down to the budget before it waits for more work (false on timeout) */
 bool DN_server_drain(DNserver* server, double timeoutSeconds);
 /* moves up to capacity completions out of the server; returns how many */
 size_t DN_server_poll(DNserver* server, DNcompletion* out, size_t capacity);

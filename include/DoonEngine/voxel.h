@@ -309,6 +309,9 @@ int DN_decompress_chunk(const DNvolume* vol, const uint8_t* mem, size_t size, DN
  * counts at 128/256/384, linearised albedo; voxel.c:1397-1461).  words: 2 per surface voxel (normal
  * word, linear albedo word), room for 512 voxels.  Returns the surface voxel count. */
 uint32_t dn_pack_chunk(const DNvolume* vol, const DNchunk* chunk, uint32_t mask[16], uint32_t partial[3], uint32_t* words);
+/* The surface voxel count of dn_pack_chunk computed the way DN_sync_gpu sizes a chunk's pool range before
+ * the device packs it (64-bit occupancy boards; no words written).  Equal to dn_pack_chunk's return value. */
+uint32_t dn_count_surface(const DNvolume* vol, const DNchunk* chunk);
 
 /* Struct sizes and field offsets for language bindings; returns the number of entries. */
 size_t DN_abi_layout(uint64_t* out, size_t n);

@@ -166,6 +166,37 @@ int dn_cuda_sync_stage(struct DNgpuVolume* g, const dn_tile_op* ops, uint32_t no
                        const dn_chunk_record* records, uint32_t nrecords,
                        const uint32_t* voxelWords, uint64_t nvoxels);
 
+/* --- sync with packing on the device (no counterpart in the reference, which packs on the host,
+ *     voxel.c:1397-1461).  Each staged record comes with its chunk's 512 voxels as the CPU map stores them
+ *     (DNcompressedVoxel voxels[8][8][8]: normal word, sRGB albedo word; x outermost).  The device does the
+ *     packing: the surface cull (a solid voxel is kept when a face neighbour is outside the chunk, empty or
+ *     of a see-through material), the occupancy mask and partial counts, the compaction in mask order and
+ *     the albedo linearisation.  The host supplies, per record, pos, voxBase and nvox: the kept-voxel
+ *     count, which sizes the record's pool range before the upload; the device counts again and a record
+ *     whose count differs is not published (its tile stays unloaded; dn_cuda_finish reports
+ *     DN_CUDA_ERR_KERNEL).  mask and partial of the records are not read. --- */
+typedef struct dn_pack_params {
+    uint32_t seeThrough[8];  /* bit m: material m is empty (255) or has opacity < 1 */
+    uint8_t linear[256];     /* sRGB albedo byte -> linear byte (voxel.c:1441-1447) */
+} dn_pack_params;
+/* chunkVoxels[r]: the 4096-byte voxel array of record r; copied before the call returns.  A sync whose
+ * chunks exceed the volume's staging buffer (16 MiB) is uploaded in parts, and the call then waits for
+ * each part's upload before it fills the buffer again. */
+int dn_cuda_sync_chunks(struct DNgpuVolume* g, const dn_sync_params* p, const dn_pack_params* pk,
+                        const dn_tile_op* ops, uint32_t nops,
+                        const dn_chunk_record* records, uint32_t nrecords, const void* const* chunkVoxels);
+/* Sets the size of one staging part of dn_cuda_sync_chunks (0: back to 16 MiB); returns the previous size.
+ * Process-wide; for tests of the multi-part upload. */
+size_t dn_cuda_stage_part_limit(size_t bytes);
+/* the staging half of dn_cuda_sync_chunks (DN_BATCH_SYNC maps; see dn_cuda_sync_stage) */
+int dn_cuda_sync_stage_chunks(struct DNgpuVolume* g, const dn_pack_params* pk,
+                              const dn_tile_op* ops, uint32_t nops,
+                              const dn_chunk_record* records, uint32_t nrecords, const void* const* chunkVoxels);
+/* the device record of a loaded tile and its voxel words (2 per voxel: normal, linear albedo; room for 512
+ * voxels); waits for the map's stream.  Returns DN_CUDA_ERR_ARG when the tile has no record. */
+int dn_cuda_export_chunk(struct DNgpuVolume* g, uint32_t tile, dn_chunk_record* rec, uint32_t matSet[8],
+                         uint32_t* words);
+
 /* --- batches (no counterpart in the reference, which issues one GL dispatch sequence per volume) ---
  * A batch runs the frame work of many maps as kernels that each cover every map of the frame: one draw
  * launch over all maps' pixels, one launch of the per-tile sync pass over all maps' tiles, one persistent

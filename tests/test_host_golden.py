@@ -32,7 +32,8 @@ def olib():
 
 def chunk_from_bytes(b):
     c = L.DNchunk()
-    ctypes.memmove(ctypes.byref(c), np.ascontiguousarray(b, np.uint8).ctypes.data, ctypes.sizeof(c))
+    a = np.ascontiguousarray(b, np.uint8)   # kept alive while memmove reads it
+    ctypes.memmove(ctypes.byref(c), a.ctypes.data, ctypes.sizeof(c))
     return c
 
 
@@ -78,7 +79,8 @@ def test_voxel_codec_oracle(olib):
 
 
 def _materials_into(vol, table):
-    ctypes.memmove(vol.s.materials, np.ascontiguousarray(table, np.uint32).ctypes.data, 256 * 32)
+    a = np.ascontiguousarray(table, np.uint32)   # kept alive while memmove reads it
+    ctypes.memmove(vol.s.materials, a.ctypes.data, 256 * 32)
 
 
 def test_chunk_packing_product(lib):
@@ -113,6 +115,49 @@ def test_chunk_packing_oracle(olib):
         if n:
             assert list(p.partial) == G["pack_partial"][k].tolist(), k
         assert list(p.vox)[: 2 * n] == G["pack_vox"][k].reshape(-1)[: 2 * n].tolist(), k
+
+
+def test_surface_count_sizes_like_packing(lib):
+    """The bit-board count that sizes a chunk's pool range before the device packs it (dn_count_surface)
+    equals the reference's packed voxel count on every golden chunk, and the host packing's count on random
+    chunks: opaque, see-through and empty materials, full, hollow and single-voxel chunks, every face."""
+    vol = dn.Volume((2, 2, 2), 4, cpu_only=True)
+    _materials_into(vol, G["pack_materials"])
+    for k in range(len(G["pack_chunks"])):
+        ch = chunk_from_bytes(G["pack_chunks"][k])
+        assert lib.dn_count_surface(vol.ptr, ctypes.byref(ch)) == G["pack_nvox"][k], k
+    rng = np.random.default_rng(7)
+    mats = np.zeros((256, 8), np.uint32)
+    opac = np.ones(256, np.float32)
+    opac[rng.choice(255, 40, replace=False)] = rng.uniform(0.0, 0.999, 40).astype(np.float32)
+    mats[:, 3] = opac.view(np.uint32)
+    _materials_into(vol, mats)
+    words = np.zeros(1024, np.uint32)
+    mask = np.zeros(16, np.uint32)
+    part = np.zeros(3, np.uint32)
+    for k in range(400):
+        ch = L.DNchunk()
+        m = rng.integers(0, 255, 512).astype(np.uint32)
+        kind = k % 5
+        if kind == 0:
+            m[rng.random(512) < rng.random()] = 255            # random density
+        elif kind == 1:
+            pass                                               # full (only the faces show, plus see-through)
+        elif kind == 2:
+            m[:] = 255
+            m[rng.integers(0, 512)] = rng.integers(0, 255)     # one voxel
+        elif kind == 3:
+            g = np.indices((8, 8, 8)).reshape(3, -1)           # [x][y][z] order: a hollow shell
+            m[((g > 0) & (g < 7)).all(0)] = 255
+        else:
+            m[:] = 255                                         # empty
+        raw = np.zeros((512, 2), np.uint32)
+        raw[:, 0] = (m << 24) | rng.integers(0, 1 << 24, 512).astype(np.uint32)
+        raw[:, 1] = rng.integers(0, 1 << 32, 512, dtype=np.uint64).astype(np.uint32)
+        ctypes.memmove(ctypes.addressof(ch.voxels), raw.ctypes.data, 4096)
+        n = lib.dn_pack_chunk(vol.ptr, ctypes.byref(ch), mask.ctypes.data, part.ctypes.data, words.ctypes.data)
+        assert lib.dn_count_surface(vol.ptr, ctypes.byref(ch)) == n, (k, kind)
+    vol.close()
 
 
 def _mat_np(m):
