@@ -367,6 +367,24 @@ extern "C" uint64_t dn_cuda_host_pinned(void)
     return (uint64_t)g_slabs.size() * HOST_SLAB;
 }
 
+extern "C" uint64_t dn_cuda_host_pinned_free(void)
+{
+    std::lock_guard<std::mutex> lock(g_slabMutex);
+    return (uint64_t)g_freeSlabs.size() * HOST_SLAB;
+}
+
+extern "C" int dn_cuda_host_headroom(uint64_t bytes)
+{
+    if (g_device < 0) return dn_set_err(DN_CUDA_ERR_DEVICE, "dn_cuda_init was not called");
+    CK(cudaSetDevice(g_device));
+    std::lock_guard<std::mutex> lock(g_slabMutex);
+    const size_t want = (size_t)((bytes + HOST_SLAB - 1) / HOST_SLAB);
+    if (g_freeSlabs.size() >= want) return DN_CUDA_OK;
+    if (!slabs_grow_to((g_slabs.size() + want - g_freeSlabs.size()) * HOST_SLAB))
+        return dn_set_err(DN_CUDA_ERR_NOMEM, "pinning %llu more bytes of host memory failed", (unsigned long long)bytes);
+    return DN_CUDA_OK;
+}
+
 // Eviction and restore never wait for the device.  Both run in the volume's stream order (the batch's
 // stream while the volume is a member): eviction queues the copies of the persistent arrays into slabs of
 // the pinned pool and then frees the arrays (stream-ordered: they come from the device's pool), and restore

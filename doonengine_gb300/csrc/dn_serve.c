@@ -464,6 +464,12 @@ static void* serve_main(void* arg)
 			/* idle: volumes grow when their syncs stage chunks, so a busy period can end above the budget;
 			 * evict down to it now, while no request waits (DN_server_drain waits for this too) */
 			enforce_budget(s, 0, NULL);
+			if (s->cfg.deviceBudgetBytes) {
+				/* which maps are evicted changes under load, and small maps round up to whole slabs: keep a
+				 * quarter of the pinned memory in use free, pinned now rather than by an eviction in a tick */
+				const uint64_t pinned = dn_cuda_host_pinned(), spare = dn_cuda_host_pinned_free();
+				if (pinned > spare) dn_cuda_host_headroom((pinned - spare) / 4);
+			}
 			pthread_mutex_lock(&s->lock);
 			if (!s->inHead) s->settled = 1;
 			pthread_cond_broadcast(&s->cond);

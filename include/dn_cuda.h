@@ -272,6 +272,10 @@ int dn_cuda_map_restore(struct DNgpuVolume* g);
  * difference at start); dn_cuda_host_pinned returns the pool's size in bytes. */
 int dn_cuda_host_reserve(uint64_t bytes);
 uint64_t dn_cuda_host_pinned(void);
+/* the pool's free bytes (slabs no evicted volume holds), and pinning until at least 'bytes' are free (a
+ * server pins ahead while idle: evictions of smaller maps take more slabs for the same bytes) */
+uint64_t dn_cuda_host_pinned_free(void);
+int dn_cuda_host_headroom(uint64_t bytes);
 /* 1 when the work recorded by ev has completed, 0 while pending, negative on error */
 int dn_cuda_event_query(void* ev);
 
