@@ -179,7 +179,6 @@ __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLi
         const float (*sdir)[3] = MANY ? e->sdir : one->gtab->sdir;
         const float (*sinv)[3] = MANY ? e->sinv : one->gtab->sinv;
         float4* out = MANY ? e->out : one->out;
-        const bool rngSin = p.rngMode == 1u;
         const f3 sun = mk(p.sunStrength[0], p.sunStrength[1], p.sunStrength[2]);
         const f3 sunDir = mk(p.sunDir[0], p.sunDir[1], p.sunDir[2]);
         const uint32_t K = p.K;

@@ -112,7 +112,7 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
     // D16: every visited cell (each outer or inner iteration of step_map / step_chunk) counts; a segment
     // that reached the cap ends as a miss
     if (inb) {
-        if ((s.flags >> 8) >= m.stepCap) return 2u;
+        if (s.flags >= (m.stepCap << 8)) return 2u;   // (flags >> 8) >= stepCap: the low byte holds state bits
         s.flags += 256u;
     }
     const uint32_t idx = (uint32_t)s.cpos.x + bx * ((uint32_t)s.cpos.y + by * (uint32_t)s.cpos.z);
@@ -137,15 +137,17 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
             const f3 up = add(s.pos, muls(s.dir, tt));
             f3 cp = mk((up.x - (float)s.cpos.x) * 8.0f, (up.y - (float)s.cpos.y) * 8.0f, (up.z - (float)s.cpos.z) * 8.0f);
             const float lo = EPS, hi_ = 8.0f - EPS;
-            cp.x = gmin(gmax(cp.x, lo), hi_); cp.y = gmin(gmax(cp.y, lo), hi_); cp.z = gmin(gmax(cp.z, lo), hi_);
+            // cp is finite here (a finite origin and direction, D16), so fminf / fmaxf give GLSL clamp's
+            // values and the floors below are 0..7: a plain conversion, and fl itself for (float)cpos
+            cp.x = fminf(fmaxf(cp.x, lo), hi_); cp.y = fminf(fmaxf(cp.y, lo), hi_); cp.z = fminf(fmaxf(cp.z, lo), hi_);
             s.cp = cp;
             s.opos = s.cpos; s.oside = s.cside; s.olastMin = s.clastMin;
             const f3 fl = vfloor(cp);
-            s.cpos.x = f2i(fl.x); s.cpos.y = f2i(fl.y); s.cpos.z = f2i(fl.z);
+            s.cpos.x = (int32_t)fl.x; s.cpos.y = (int32_t)fl.y; s.cpos.z = (int32_t)fl.z;
             const f3 sg = mk((float)step.x, (float)step.y, (float)step.z);
-            s.cside.x = (sg.x * ((float)s.cpos.x - cp.x) + sg.x * 0.5f + 0.5f) * delta.x;
-            s.cside.y = (sg.y * ((float)s.cpos.y - cp.y) + sg.y * 0.5f + 0.5f) * delta.y;
-            s.cside.z = (sg.z * ((float)s.cpos.z - cp.z) + sg.z * 0.5f + 0.5f) * delta.z;
+            s.cside.x = (sg.x * (fl.x - cp.x) + sg.x * 0.5f + 0.5f) * delta.x;
+            s.cside.y = (sg.y * (fl.y - cp.y) + sg.y * 0.5f + 0.5f) * delta.y;
+            s.cside.z = (sg.z * (fl.z - cp.z) + sg.z * 0.5f + 0.5f) * delta.z;
             s.clastMin = 0.0f;
             s.rec = &m.rec[__ldg(&m.tword[idx]) & SLOT_MASK];
             // inner level; the chunk inherits ignoreFirst; bit5: the chunk is marked opaque
@@ -191,12 +193,15 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
                 s.ts.lastVoxRefract = mat.refractIndex;
             }
         }
-    } else if (inner) {
-        c.inner++;
-        if (s.ts.lastVoxID != 255u) { s.ts.lastVoxID = 255u; s.ts.lastVoxRefract = 1.0f; }
     } else {
-        c.outer++;
-        if (!(s.flags & 8u) && cst != 0u) {
+        // an empty cell, either level, without branches: the counters, and at the voxel level the end of a
+        // run of transparent voxels (lastVoxID 255 always comes with refract 1, so writing both is the
+        // reference's reset); an unloaded chunk cell requests its chunk once per ray
+        c.inner += inner ? 1u : 0u;
+        c.outer += inner ? 0u : 1u;
+        s.ts.lastVoxID = inner ? 255u : s.ts.lastVoxID;
+        s.ts.lastVoxRefract = inner ? 1.0f : s.ts.lastVoxRefract;
+        if (!inner && !(s.flags & 8u) && cst != 0u) {
             if (m.treq[idx] == 0) m.treq[idx] = 1;
             s.flags |= 8u;
         }
