@@ -313,7 +313,7 @@ def run_ours(args):
         if args.pressure_budget_gb > 0:
             t1 = time.perf_counter()
             rates = [float(x) for x in args.pressure_rates.split(",")]
-            sv = serving_sweep(args, lib, rank, world, 256, rates, args.serving_seconds, args.pressure_budget_gb)
+            sv = serving_sweep(args, lib, rank, world, 256, rates, args.pressure_seconds, args.pressure_budget_gb)
             result["serving_under_eviction"] = serving_summary(sv)
             log("serving under eviction: %.1f s" % (time.perf_counter() - t1))
     if rank == 0:
@@ -1104,6 +1104,9 @@ def main():
                     help="plain workload: a second serving sweep under this device budget (below the resident "
                          "set, so whole maps are evicted to pinned host memory under load); 0 skips it")
     ap.add_argument("--pressure-rates", default="300,600,900", help="offered req/s of the eviction sweep")
+    ap.add_argument("--pressure-seconds", type=float, default=4.0,
+                    help="plain workload's eviction sweep: s per rate (which maps are evicted depends on timing, "
+                         "so its tail latency needs more requests than the resident sweep's)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3 (at least three untimed steps)")

@@ -72,6 +72,13 @@ struct HostSlab { unsigned char* p; cudaEvent_t lastRead; };
 static std::mutex g_slabMutex;
 static std::vector<HostSlab> g_slabs;
 static std::vector<uint32_t> g_freeSlabs;
+// Evictions and restores copy on streams of their own, so that their copies overlap the kernels of other
+// maps; evictions (device to host) and restores (host to device) on separate streams, so that a restore
+// never queues behind evictions and the two directions overlap.  Pool memory an eviction frees becomes
+// reusable by a restore once the eviction's frees have run (the stream-ordered allocator tracks that).
+static cudaStream_t g_copyStream = nullptr;      // evictions
+static cudaStream_t g_restoreStream = nullptr;   // restores
+static int g_copyStreamDevice = -1;
 unsigned long long g_launches = 0;
 unsigned long long g_allocs = 0;
 static unsigned long long g_generation = 0;
@@ -164,10 +171,10 @@ static int alloc_tiles(DNgpuVolume* g)
     return DN_CUDA_OK;
 }
 
-static void free_tiles(DNgpuVolume* g)
+static void free_tiles(DNgpuVolume* g, cudaStream_t s = nullptr)
 {
-    vfree(g, g->tword); vfree(g, g->tbits); vfree(g, g->treq); vfree(g, g->tvis); vfree(g, g->ttouch); vfree(g, g->tlast);
-    vfree(g, g->tpend); vfree(g, g->tpendSlot);
+    vfree(g, g->tword, s); vfree(g, g->tbits, s); vfree(g, g->treq, s); vfree(g, g->tvis, s); vfree(g, g->ttouch, s);
+    vfree(g, g->tlast, s); vfree(g, g->tpend, s); vfree(g, g->tpendSlot, s);
 }
 
 extern "C" void dn_cuda_map_destroy(DNgpuVolume* g)
@@ -190,6 +197,7 @@ extern "C" void dn_cuda_map_destroy(DNgpuVolume* g)
         free(g->evicted);
     }
     if (g->stageFree) cudaEventDestroy(g->stageFree);
+    if (g->copyDone) cudaEventDestroy(g->copyDone);
     if (g->ownStream) cudaStreamDestroy(g->ownStream);
     delete g;
 }
@@ -229,6 +237,7 @@ extern "C" int dn_cuda_map_create(uint32_t sx, uint32_t sy, uint32_t sz, uint32_
     if (e != cudaSuccess) { delete g; return dn_set_err(DN_CUDA_ERR_LAUNCH, "stream: %s", cudaGetErrorString(e)); }
     g->ownStream = g->stream;
     e = cudaEventCreateWithFlags(&g->stageFree, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->copyDone, cudaEventDisableTiming);
     if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "event: %s", cudaGetErrorString(e));
     if (!rc) rc = alloc_tiles(g);
     if (!rc) rc = valloc(g, g->rec, slotCap);
@@ -385,11 +394,26 @@ extern "C" int dn_cuda_host_headroom(uint64_t bytes)
     return DN_CUDA_OK;
 }
 
-// Eviction and restore never wait for the device.  Both run in the volume's stream order (the batch's
-// stream while the volume is a member): eviction queues the copies of the persistent arrays into slabs of
-// the pinned pool and then frees the arrays (stream-ordered: they come from the device's pool), and restore
-// queues the allocations and the copies back, then returns the slabs with an event after the copies.  Only
-// slabs the pool does not hold yet are pinned (dn_cuda_host_reserve pins them ahead).
+// the eviction (restore = false) or restore copy stream of the current device (created on first use)
+static int copy_stream(cudaStream_t* out, bool restore)
+{
+    std::lock_guard<std::mutex> lock(g_slabMutex);
+    if (!g_copyStream || g_copyStreamDevice != g_device) {
+        CK(cudaStreamCreateWithFlags(&g_copyStream, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&g_restoreStream, cudaStreamNonBlocking));
+        g_copyStreamDevice = g_device;
+    }
+    *out = restore ? g_restoreStream : g_copyStream;
+    return DN_CUDA_OK;
+}
+
+// Eviction and restore never wait for the device.  Eviction waits (on the device, on the eviction stream)
+// for the work queued on the volume's stream (the batch's stream while the volume is a member), then queues
+// the copies of the persistent arrays into slabs of the pinned pool and the stream-ordered frees of the
+// arrays; restore waits (on the restore stream) for the volume's eviction, queues the allocations and the
+// copies back, returns the slabs with an event after the copies, and makes the volume's stream wait for
+// them.  The copies so run beside the kernels of other maps.  Only slabs the pool does not hold yet are
+// pinned (dn_cuda_host_reserve pins them ahead).
 extern "C" int dn_cuda_map_evict(DNgpuVolume* g)
 {
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
@@ -400,6 +424,9 @@ extern "C" int dn_cuda_map_evict(DNgpuVolume* g)
     size_t total = 0;
     for (int i = 0; i < k; i++) total += a[i].bytes;
     const uint32_t n = (uint32_t)((total + HOST_SLAB - 1) / HOST_SLAB);
+    cudaStream_t cs;
+    int rc0 = copy_stream(&cs, false);
+    if (rc0) return rc0;
     uint32_t* ids = (uint32_t*)malloc(sizeof(uint32_t) * (n ? n : 1));
     if (!ids) return dn_set_err(DN_CUDA_ERR_NOMEM, "host");
     {
@@ -410,8 +437,10 @@ extern "C" int dn_cuda_map_evict(DNgpuVolume* g)
         }
         for (uint32_t i = 0; i < n; i++) { ids[i] = g_freeSlabs.back(); g_freeSlabs.pop_back(); }
     }
-    // the slabs' last readers (earlier restores, possibly on other streams) finish first, on the device
-    for (uint32_t i = 0; i < n; i++) CK(cudaStreamWaitEvent(g->stream, g_slabs[ids[i]].lastRead, 0));
+    // the volume's queued work, and the slabs' last readers (earlier restores), finish first, on the device
+    CK(cudaEventRecord(g->copyDone, g->stream));
+    CK(cudaStreamWaitEvent(cs, g->copyDone, 0));
+    for (uint32_t i = 0; i < n; i++) CK(cudaStreamWaitEvent(cs, g_slabs[ids[i]].lastRead, 0));
     // the arrays back to back across the slabs
     uint32_t si = 0;
     size_t so = 0;
@@ -420,9 +449,9 @@ extern "C" int dn_cuda_map_evict(DNgpuVolume* g)
         while (done < a[i].bytes) {
             const size_t len = (a[i].bytes - done) < (HOST_SLAB - so) ? (a[i].bytes - done) : (HOST_SLAB - so);
             cudaError_t e = cudaMemcpyAsync(g_slabs[ids[si]].p + so, (const unsigned char*)*a[i].ptr + done, len,
-                                            cudaMemcpyDeviceToHost, g->stream);
+                                            cudaMemcpyDeviceToHost, cs);
             if (e != cudaSuccess) {
-                cudaStreamSynchronize(g->stream);
+                cudaStreamSynchronize(cs);
                 std::lock_guard<std::mutex> lock(g_slabMutex);
                 for (uint32_t j = 0; j < n; j++) g_freeSlabs.push_back(ids[j]);
                 free(ids);
@@ -433,12 +462,14 @@ extern "C" int dn_cuda_map_evict(DNgpuVolume* g)
             if (so == HOST_SLAB) { so = 0; si++; }
         }
     }
-    // the frees follow the copies in the stream's order
-    free_tiles(g);
-    vfree(g, g->rec); vfree(g, g->nsamples); vfree(g, g->vox); vfree(g, g->diff); vfree(g, g->spec);
-    vfree(g, g->reqs); vfree(g, g->st); vfree(g, g->dtab);
-    vfree(g, g->lightOut); vfree(g, g->dstage); vfree(g, g->dimg); vfree(g, g->dhit); vfree(g, g->dface);
+    // the frees follow the copies in the copy stream's order; the arrays that are not copied (scratch) were
+    // last used on the volume's stream, which the copy stream waited for
+    free_tiles(g, cs);
+    vfree(g, g->rec, cs); vfree(g, g->nsamples, cs); vfree(g, g->vox, cs); vfree(g, g->diff, cs); vfree(g, g->spec, cs);
+    vfree(g, g->reqs, cs); vfree(g, g->st, cs); vfree(g, g->dtab, cs);
+    vfree(g, g->lightOut, cs); vfree(g, g->dstage, cs); vfree(g, g->dimg, cs); vfree(g, g->dhit, cs); vfree(g, g->dface, cs);
     g->dstageCap = 0; g->dimgCap = 0;
+    CK(cudaEventRecord(g->copyDone, cs));
     g->evicted = ids;
     g->evictedSlabs = n;
     dn_new_generation(g);
@@ -452,29 +483,32 @@ extern "C" int dn_cuda_map_restore(DNgpuVolume* g)
     CK(cudaSetDevice(g->device));
     PersistentArray a[16];
     const int k = persistent_arrays(g, a);
-    int rc = DN_CUDA_OK;
-    // the arrays in persistent_arrays' order, each from the pool on the volume's stream
-    rc = valloc(g, g->tword, g->ntiles);
-    if (!rc) rc = valloc(g, g->treq, g->ntiles);
-    if (!rc) rc = valloc(g, g->tvis, g->ntiles);
-    if (!rc) rc = valloc(g, g->ttouch, g->ntiles);
-    if (!rc) rc = valloc(g, g->tbits, (g->ntiles + 31) / 32 * 2);
-    if (!rc) rc = valloc(g, g->tlast, g->ntiles);
-    if (!rc) rc = valloc(g, g->tpend, g->ntiles);
-    if (!rc) rc = valloc(g, g->tpendSlot, g->ntiles);
-    if (!rc) rc = valloc(g, g->rec, g->slotCap);
-    if (!rc) rc = valloc(g, g->nsamples, g->slotCap);
-    if (!rc) rc = valloc(g, g->vox, g->voxCap);
-    if (!rc) rc = valloc(g, g->diff, g->voxCap);
-    if (!rc) rc = valloc(g, g->spec, g->voxCap);
-    if (!rc) rc = valloc(g, g->reqs, g->reqCap);
-    if (!rc) rc = valloc(g, g->st, 1);
-    if (!rc) rc = valloc(g, g->dtab, 1);
-    if (!rc) rc = valloc(g, g->lightOut, (size_t)g->reqCap * 64);
+    cudaStream_t cs;
+    int rc = copy_stream(&cs, true);
+    if (rc) return rc;
+    CK(cudaStreamWaitEvent(cs, g->copyDone, 0));   // the eviction's copies into the slabs, and its frees
+    // the arrays in persistent_arrays' order, each from the pool on the restore stream
+    rc = valloc(g, g->tword, g->ntiles, cs);
+    if (!rc) rc = valloc(g, g->treq, g->ntiles, cs);
+    if (!rc) rc = valloc(g, g->tvis, g->ntiles, cs);
+    if (!rc) rc = valloc(g, g->ttouch, g->ntiles, cs);
+    if (!rc) rc = valloc(g, g->tbits, (g->ntiles + 31) / 32 * 2, cs);
+    if (!rc) rc = valloc(g, g->tlast, g->ntiles, cs);
+    if (!rc) rc = valloc(g, g->tpend, g->ntiles, cs);
+    if (!rc) rc = valloc(g, g->tpendSlot, g->ntiles, cs);
+    if (!rc) rc = valloc(g, g->rec, g->slotCap, cs);
+    if (!rc) rc = valloc(g, g->nsamples, g->slotCap, cs);
+    if (!rc) rc = valloc(g, g->vox, g->voxCap, cs);
+    if (!rc) rc = valloc(g, g->diff, g->voxCap, cs);
+    if (!rc) rc = valloc(g, g->spec, g->voxCap, cs);
+    if (!rc) rc = valloc(g, g->reqs, g->reqCap, cs);
+    if (!rc) rc = valloc(g, g->st, 1, cs);
+    if (!rc) rc = valloc(g, g->dtab, 1, cs);
+    if (!rc) rc = valloc(g, g->lightOut, (size_t)g->reqCap * 64, cs);
     if (rc) {
-        free_tiles(g);
-        vfree(g, g->rec); vfree(g, g->nsamples); vfree(g, g->vox); vfree(g, g->diff); vfree(g, g->spec);
-        vfree(g, g->reqs); vfree(g, g->st); vfree(g, g->dtab); vfree(g, g->lightOut);
+        free_tiles(g, cs);
+        vfree(g, g->rec, cs); vfree(g, g->nsamples, cs); vfree(g, g->vox, cs); vfree(g, g->diff, cs); vfree(g, g->spec, cs);
+        vfree(g, g->reqs, cs); vfree(g, g->st, cs); vfree(g, g->dtab, cs); vfree(g, g->lightOut, cs);
         return rc;
     }
     uint32_t si = 0;
@@ -484,7 +518,7 @@ extern "C" int dn_cuda_map_restore(DNgpuVolume* g)
         while (done < a[i].bytes) {
             const size_t len = (a[i].bytes - done) < (HOST_SLAB - so) ? (a[i].bytes - done) : (HOST_SLAB - so);
             CK(cudaMemcpyAsync((unsigned char*)*a[i].ptr + done, g_slabs[g->evicted[si]].p + so, len,
-                               cudaMemcpyHostToDevice, g->stream));
+                               cudaMemcpyHostToDevice, cs));
             done += len;
             so += len;
             if (so == HOST_SLAB) { so = 0; si++; }
@@ -494,10 +528,13 @@ extern "C" int dn_cuda_map_restore(DNgpuVolume* g)
     {
         std::lock_guard<std::mutex> lock(g_slabMutex);
         for (uint32_t i = 0; i < g->evictedSlabs; i++) {
-            CK(cudaEventRecord(g_slabs[g->evicted[i]].lastRead, g->stream));
+            CK(cudaEventRecord(g_slabs[g->evicted[i]].lastRead, cs));
             g_freeSlabs.push_back(g->evicted[i]);
         }
     }
+    // the volume's later work waits for its arrays
+    CK(cudaEventRecord(g->copyDone, cs));
+    CK(cudaStreamWaitEvent(g->stream, g->copyDone, 0));
     free(g->evicted);
     g->evicted = nullptr;
     g->evictedSlabs = 0;

@@ -60,6 +60,7 @@ struct DNgpuVolume {
     unsigned char* hstage; size_t hstageCap;
     unsigned char* dstage; size_t dstageCap;
     cudaEvent_t stageFree;
+    cudaEvent_t copyDone;       // eviction / restore: the volume's queued work, then its last copy on the copy stream
     DevState* hst;                      // pinned copy of DevState
     // device staging for host-memory draws
     float4* dimg; uint32_t* dhit; uint8_t* dface; size_t dimgCap;
@@ -98,26 +99,27 @@ template <class T> static void dfree(T*& p) { if (p) cudaFree(p); p = nullptr; }
 uint32_t vol_array_bit(DNgpuVolume* g, const void* field);
 extern bool g_asyncAlloc;               // the device supports stream-ordered allocation (cudaMallocAsync)
 
-// frees one of the volume's device arrays: stream-ordered on the volume's stream when it came from the pool
-template <class T> static void vfree(DNgpuVolume* g, T*& p)
+// frees one of the volume's device arrays: stream-ordered on stream s (the volume's stream by default) when
+// it came from the pool
+template <class T> static void vfree(DNgpuVolume* g, T*& p, cudaStream_t s = nullptr)
 {
     if (!p) return;
     const uint32_t bit = vol_array_bit(g, &p);
-    if (bit && (g->poolMask & bit)) cudaFreeAsync(p, g->stream);
+    if (bit && (g->poolMask & bit)) cudaFreeAsync(p, s ? s : g->stream);
     else cudaFree(p);
     g->poolMask &= ~bit;
     p = nullptr;
 }
-// allocates one of the volume's device arrays from the stream-ordered pool, ordered on the volume's stream
-// (work issued afterwards on that stream may use it)
-template <class T> static int valloc(DNgpuVolume* g, T*& p, size_t count)
+// allocates one of the volume's device arrays from the stream-ordered pool, ordered on stream s (the
+// volume's stream by default: work issued afterwards on that stream may use it)
+template <class T> static int valloc(DNgpuVolume* g, T*& p, size_t count, cudaStream_t s = nullptr)
 {
     p = nullptr;
     if (count == 0) count = 1;
     const uint32_t bit = vol_array_bit(g, &p);
     COUNT_ALLOC();
     if (g_asyncAlloc && bit) {
-        CK(cudaMallocAsync((void**)&p, count * sizeof(T), g->stream));
+        CK(cudaMallocAsync((void**)&p, count * sizeof(T), s ? s : g->stream));
         g->poolMask |= bit;
     } else {
         CK(cudaMalloc((void**)&p, count * sizeof(T)));

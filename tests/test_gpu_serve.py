@@ -223,3 +223,46 @@ def test_submit_rejects_bad_requests(gpu_ready):
         server.close()
         for v in vols:
             v.close()
+
+
+def test_direct_eviction_behind_queued_work_is_exact(gpu_ready):
+    """dn_cuda_map_evict and dn_cuda_map_restore called right behind queued draws, syncs and lighting
+    launches, without waiting for them: the copies run on their own stream, ordered after the volume's work
+    and before its next work.  Eviction after every phase and a twin that never leaves the device give the
+    same images, tile state and lighting, bit for bit."""
+    lib = dn.load()
+    sp = dict(SPECS[2])
+    twins = []
+    for _ in range(2):
+        v, _ = configs.build_volume("tiny", **sp)
+        v.s.mapId = sp["seed"]
+        twins.append(v)
+    W, H = sp["res"]
+    images = [[dn.Image(W, H, on_device=True) for _ in range(6)] for _ in twins]
+    try:
+        for f in range(6):
+            for which, vol in enumerate(twins):
+                roundtrip = (lambda: (lib.dn_cuda_map_evict(vol.s.gpu) == 0 and
+                                      lib.dn_cuda_map_restore(vol.s.gpu) == 0)) if which == 1 else (lambda: True)
+                v, p = vol.view_proj(H / W)
+                vol.draw(images[which][f], v, p)
+                assert roundtrip()
+                vol.sync(dn.DN_READ_WRITE, 1)
+                assert roundtrip()
+                vol.update_lighting(1, 1000, 0.75 + 0.5 * f)
+                assert roundtrip()
+                if f == 3:
+                    # an evicted volume stays evicted across other work, then comes back
+                    if which == 1:
+                        assert lib.dn_cuda_map_evict(vol.s.gpu) == 0
+                        assert lib.dn_cuda_map_is_resident(vol.s.gpu) == 0
+                        assert lib.dn_cuda_map_restore(vol.s.gpu) == 0
+        for vol in twins:
+            assert vol.finish(), lib.dn_cuda_last_error().decode()
+        same(snapshot(twins[0], images[0]), snapshot(twins[1], images[1]), "evicted twin")
+    finally:
+        for imgs in images:
+            for im in imgs:
+                im.close()
+        for vol in twins:
+            vol.close()
