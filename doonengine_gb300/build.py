@@ -23,7 +23,7 @@ CUDA_FLAGS = ARCH + ["-lineinfo", "-O3", "--fmad=false", "-prec-div=true", "-pre
                      "-ftz=false", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 # extra nvcc defines for tuning experiments, e.g. DN_NVCC_EXTRA="-DDN_STREAM_MIN_BLOCKS=5"
 CUDA_FLAGS += [f for f in os.environ.get("DN_NVCC_EXTRA", "").split() if f.startswith("-D")]
-C_FLAGS = ["-O2", "-fPIC", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", "-Wall",
+C_FLAGS = ["-O2", "-fPIC", "-fno-semantic-interposition", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", "-Wall",
            "-Wno-unused-function", "-I" + INCLUDE]
 
 CU_SOURCES = ["dn_cuda.cu", "dn_batch.cu", "dn_shapes.cu"]
