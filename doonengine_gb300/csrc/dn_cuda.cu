@@ -5,11 +5,12 @@
  *   tiles   tword[t] = state << 30 | record slot   (state 0 absent, 1 unloaded, 2 loaded)
  *           treq / tvis / ttouch (bytes), tlast (lastUsed), tpend / tpendSlot (host ops of a sync)
  *   records rec[slot]: 128-B ChunkRec (512-bit occupancy mask, partial counts, voxel count,
- *           position, pool base), nsamples[slot]
+ *           position, pool base, material set), nsamples[slot]
  *   pool    vox[i] (uint2: normal word, linear albedo word), diff[i] / spec[i] (float4, FP32)
  *   frame   reqs[] ((tile << 4) | group), lightOut[] (scratch: new lighting per request lane)
- * Kernels per frame: k_draw (primary rays), k_sync_stage + k_compact (DN_sync_gpu),
- * k_light_packet (or k_light_stream) + k_commit (DN_update_lighting).
+ * Kernels per frame: k_draw (primary rays); k_pack_stage (or k_sync_stage for records packed on the host)
+ * + k_compact (DN_sync_gpu); k_mark_opaque + k_light_tables + k_light_packet + k_light_diffuse (or
+ * k_light_stream) + k_commit (DN_update_lighting).
  */
 #include "dn_internal.cuh"
 #include "dn_light_stream.cuh"

@@ -39,7 +39,8 @@ typedef struct dn_material {
     uint32_t reflectType, shininess;
 } dn_material;
 
-/* one packed chunk (output of the host packing, voxel.c:1397-1461) */
+/* one packed chunk (the packing of voxel.c:1397-1461): the input of dn_cuda_sync; dn_cuda_sync_chunks reads
+ * only pos, nvox and voxBase and packs the rest on the device */
 typedef struct dn_chunk_record {
     uint32_t mask[16];      /* bit x + 8*(y + 8*z) */
     uint32_t partial[3];    /* set bits before 128, 256, 384 */
