@@ -332,6 +332,8 @@ _SIGS = [
     ("dn_cuda_map_is_resident", c_int, [c_void_p]),
     ("dn_cuda_map_evict", c_int, [c_void_p]),
     ("dn_cuda_map_restore", c_int, [c_void_p]),
+    ("dn_cuda_map_restore_async", c_int, [c_void_p]),
+    ("dn_cuda_map_restore_query", c_int, [c_void_p]),
     ("dn_cuda_host_reserve", c_int, [c_uint64]),
     ("dn_cuda_host_pinned", c_uint64, []),
     ("dn_cuda_host_pinned_free", c_uint64, []),

@@ -463,7 +463,7 @@ extern "C" int dn_cuda_batch_frame(DNgpuBatch* b, const dn_batch_item* items, ui
         const dn_batch_item& it = items[i];
         DNgpuVolume* g = it.map;
         if (!g || g->batch != b) return dn_set_err(DN_CUDA_ERR_ARG, "item %u: the map is not a member of the batch", i);
-        if (g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "item %u: the map is evicted", i);
+        if (map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "item %u: the map is evicted", i);
         if (!it.phases || (it.phases & ~(DN_BATCH_DRAW | DN_BATCH_SYNC | DN_BATCH_LIGHT)))
             return dn_set_err(DN_CUDA_ERR_ARG, "item %u: phases 0x%x", i, it.phases);
         seen.push_back(g);

@@ -267,7 +267,7 @@ extern "C" int dn_cuda_map_create(uint32_t sx, uint32_t sy, uint32_t sz, uint32_
 
 extern "C" int dn_cuda_map_resize(DNgpuVolume* g, uint32_t sx, uint32_t sy, uint32_t sz)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
     uint64_t n = (uint64_t)sx * sy * sz;
     if (n == 0 || n >= (1ull << 28)) return dn_set_err(DN_CUDA_ERR_ARG, "map size %ux%ux%u", sx, sy, sz);
@@ -420,6 +420,7 @@ extern "C" int dn_cuda_map_evict(DNgpuVolume* g)
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
     if (g->evicted) return DN_CUDA_OK;
     CK(cudaSetDevice(g->device));
+    map_evicted(g);   // a restore still copying: the volume's stream (and so this eviction) waits for it
     PersistentArray a[16];
     const int k = persistent_arrays(g, a);
     size_t total = 0;
@@ -477,11 +478,47 @@ extern "C" int dn_cuda_map_evict(DNgpuVolume* g)
     return DN_CUDA_OK;
 }
 
+// the allocations and copies of a restore, on the restore stream; copyDone marks their end
+static int restore_copies(DNgpuVolume* g);
+
 extern "C" int dn_cuda_map_restore(DNgpuVolume* g)
+{
+    if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
+    CK(cudaSetDevice(g->device));
+    if (!g->evicted) { map_evicted(g); return DN_CUDA_OK; }
+    int rc = restore_copies(g);
+    if (rc) return rc;
+    // the volume's later work waits for its arrays
+    CK(cudaStreamWaitEvent(g->stream, g->copyDone, 0));
+    return DN_CUDA_OK;
+}
+
+extern "C" int dn_cuda_map_restore_async(DNgpuVolume* g)
 {
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
     if (!g->evicted) return DN_CUDA_OK;
     CK(cudaSetDevice(g->device));
+    int rc = restore_copies(g);
+    if (rc) return rc;
+    g->restorePending = 1;
+    return DN_CUDA_OK;
+}
+
+extern "C" int dn_cuda_map_restore_query(DNgpuVolume* g)
+{
+    if (!g) { dn_set_err(DN_CUDA_ERR_ARG, "null volume"); return -1; }
+    if (g->evicted) return 0;
+    if (!g->restorePending) return 1;
+    CK(cudaSetDevice(g->device));
+    const cudaError_t e = cudaEventQuery(g->copyDone);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    dn_set_err(DN_CUDA_ERR_LAUNCH, "restore: %s", cudaGetErrorString(e));
+    return -1;
+}
+
+static int restore_copies(DNgpuVolume* g)
+{
     PersistentArray a[16];
     const int k = persistent_arrays(g, a);
     cudaStream_t cs;
@@ -533,9 +570,7 @@ extern "C" int dn_cuda_map_restore(DNgpuVolume* g)
             g_freeSlabs.push_back(g->evicted[i]);
         }
     }
-    // the volume's later work waits for its arrays
     CK(cudaEventRecord(g->copyDone, cs));
-    CK(cudaStreamWaitEvent(g->stream, g->copyDone, 0));
     free(g->evicted);
     g->evicted = nullptr;
     g->evictedSlabs = 0;
@@ -545,7 +580,7 @@ extern "C" int dn_cuda_map_restore(DNgpuVolume* g)
 
 extern "C" int dn_cuda_reserve(DNgpuVolume* g, uint32_t slotCap, uint64_t voxelCap, uint64_t requestCap)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
     CK(cudaSetDevice(g->device));
     int rc;
@@ -972,7 +1007,7 @@ static int sync_tiles(DNgpuVolume* g, const dn_sync_params* p)
 extern "C" int dn_cuda_sync_stage_chunks(DNgpuVolume* g, const dn_pack_params* pk, const dn_tile_op* ops, uint32_t nops,
                                          const dn_chunk_record* records, uint32_t nrecords, const void* const* chunkVoxels)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !pk || (nops && !ops) || (nrecords && (!records || !chunkVoxels))) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     CK(cudaSetDevice(g->device));
     return dn_stage_chunks(g, pk, ops, nops, records, nrecords, chunkVoxels);
@@ -982,7 +1017,7 @@ extern "C" int dn_cuda_sync_chunks(DNgpuVolume* g, const dn_sync_params* p, cons
                                    uint32_t nops, const dn_chunk_record* records, uint32_t nrecords,
                                    const void* const* chunkVoxels)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !p || !pk || (nops && !ops) || (nrecords && (!records || !chunkVoxels))) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (p->split == 0 || p->op > 2) return dn_set_err(DN_CUDA_ERR_ARG, "bad sync parameters");
     CK(cudaSetDevice(g->device));
@@ -994,7 +1029,7 @@ extern "C" int dn_cuda_sync_chunks(DNgpuVolume* g, const dn_sync_params* p, cons
 extern "C" int dn_cuda_export_chunk(DNgpuVolume* g, uint32_t tile, dn_chunk_record* recOut, uint32_t matSet[8],
                                     uint32_t* words)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !recOut) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (tile >= g->ntiles) return dn_set_err(DN_CUDA_ERR_ARG, "tile %u of %llu", tile, (unsigned long long)g->ntiles);
     CK(cudaSetDevice(g->device));
@@ -1020,7 +1055,7 @@ extern "C" int dn_cuda_export_chunk(DNgpuVolume* g, uint32_t tile, dn_chunk_reco
 extern "C" int dn_cuda_sync_stage(DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops, const dn_chunk_record* records,
                                   uint32_t nrecords, const uint32_t* voxelWords, uint64_t nvoxels)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     CK(cudaSetDevice(g->device));
     return dn_stage_ops(g, ops, nops, records, nrecords, voxelWords, nvoxels);
@@ -1030,7 +1065,7 @@ extern "C" int dn_cuda_sync(DNgpuVolume* g, const dn_sync_params* p, const dn_ti
                             const dn_chunk_record* records, uint32_t nrecords, const uint32_t* voxelWords,
                             uint64_t nvoxels)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !p) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (p->split == 0 || p->op > 2) return dn_set_err(DN_CUDA_ERR_ARG, "bad sync parameters");
     CK(cudaSetDevice(g->device));
@@ -1041,7 +1076,7 @@ extern "C" int dn_cuda_sync(DNgpuVolume* g, const dn_sync_params* p, const dn_ti
 
 extern "C" int dn_cuda_light(DNgpuVolume* g, const dn_light_params* p, const dn_material* materials)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !p || !materials) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (p->K < 1 || p->K > 64) return dn_set_err(DN_CUDA_ERR_ARG, "K = %u", p->K);
     CK(cudaSetDevice(g->device));
@@ -1137,7 +1172,7 @@ extern "C" uint32_t dn_cuda_light_noalloc_set_limit(uint32_t groups)
 
 extern "C" int dn_cuda_light_noalloc(DNgpuVolume* g, const dn_light_params* p, const dn_material* materials)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !p || !materials) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (p->K < 1 || p->K > 64) return dn_set_err(DN_CUDA_ERR_ARG, "K = %u", p->K);
     CK(cudaSetDevice(g->device));
@@ -1225,7 +1260,7 @@ static int launch_draw(DNgpuVolume* g, const dn_draw_params* p, const dn_materia
 extern "C" int dn_cuda_draw(DNgpuVolume* g, const dn_draw_params* p, const dn_material* materials, float* colorOut,
                             uint32_t* hitOut, uint8_t* faceOut)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !p || !materials || !colorOut) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (p->width == 0 || p->height == 0) return dn_set_err(DN_CUDA_ERR_ARG, "empty image");
     CK(cudaSetDevice(g->device));
@@ -1235,7 +1270,7 @@ extern "C" int dn_cuda_draw(DNgpuVolume* g, const dn_draw_params* p, const dn_ma
 extern "C" int dn_cuda_draw_host(DNgpuVolume* g, const dn_draw_params* p, const dn_material* materials,
                                  float* colorOut, uint32_t* hitOut, uint8_t* faceOut)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !p || !materials || !colorOut) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     if (p->width == 0 || p->height == 0) return dn_set_err(DN_CUDA_ERR_ARG, "empty image");
     CK(cudaSetDevice(g->device));
@@ -1254,7 +1289,7 @@ extern "C" int dn_cuda_draw_host(DNgpuVolume* g, const dn_draw_params* p, const 
 
 extern "C" int dn_cuda_finish(DNgpuVolume* g, uint64_t* numRequests)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
     CK(cudaSetDevice(g->device));
     CK(cudaMemcpyAsync(g->hst, g->st, sizeof(DevState), cudaMemcpyDeviceToHost, g->stream));
@@ -1276,7 +1311,7 @@ extern "C" int dn_cuda_finish(DNgpuVolume* g, uint64_t* numRequests)
 
 extern "C" int dn_cuda_stats_kind(DNgpuVolume* g, int kind, dn_stats* out)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !out || kind < 0 || kind > 2) return dn_set_err(DN_CUDA_ERR_ARG, "bad argument");
     int rc = dn_cuda_finish(g, nullptr);
     if (rc && rc != DN_CUDA_ERR_KERNEL) return rc;
@@ -1293,7 +1328,7 @@ extern "C" int dn_cuda_stats(DNgpuVolume* g, dn_stats* out) { return dn_cuda_sta
 
 extern "C" int dn_cuda_reset_stats(DNgpuVolume* g)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
     CK(cudaSetDevice(g->device));
     CK(cudaMemsetAsync(g->st->stats, 0, sizeof(g->st->stats) + sizeof(g->st->lstats), g->stream));
@@ -1305,7 +1340,7 @@ extern "C" void* dn_cuda_stream(DNgpuVolume* g) { return g ? (void*)g->stream : 
 extern "C" int dn_cuda_read_tile_flags(DNgpuVolume* g, uint8_t* requested, uint8_t* touched)
 {
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
-    if (g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     CK(cudaSetDevice(g->device));
     CK(cudaMemcpyAsync(requested, g->treq, g->ntiles, cudaMemcpyDeviceToHost, g->stream));
     CK(cudaMemcpyAsync(touched, g->ttouch, g->ntiles, cudaMemcpyDeviceToHost, g->stream));
@@ -1315,7 +1350,7 @@ extern "C" int dn_cuda_read_tile_flags(DNgpuVolume* g, uint8_t* requested, uint8
 
 extern "C" int dn_cuda_export_tiles(DNgpuVolume* g, uint8_t* state, uint8_t* vis, uint32_t* lastUsed, uint32_t* samples)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g) return dn_set_err(DN_CUDA_ERR_ARG, "null volume");
     CK(cudaSetDevice(g->device));
     CK(cudaStreamSynchronize(g->stream));
@@ -1341,7 +1376,7 @@ extern "C" int dn_cuda_export_tiles(DNgpuVolume* g, uint8_t* state, uint8_t* vis
 
 extern "C" int dn_cuda_export_requests(DNgpuVolume* g, uint32_t* out, uint64_t capacity, uint64_t* count)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !count) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     uint64_t n = 0;
     int rc = dn_cuda_finish(g, &n);
@@ -1354,7 +1389,7 @@ extern "C" int dn_cuda_export_requests(DNgpuVolume* g, uint32_t* out, uint64_t c
 extern "C" int dn_cuda_export_lighting(DNgpuVolume* g, uint32_t* index, float* diff, float* spec, uint64_t capacity,
                                        uint64_t* count)
 {
-    if (g && g->evicted) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
+    if (g && map_evicted(g)) return dn_set_err(DN_CUDA_ERR_ARG, "the map is evicted; restore it first");
     if (!g || !count) return dn_set_err(DN_CUDA_ERR_ARG, "null argument");
     CK(cudaSetDevice(g->device));
     CK(cudaStreamSynchronize(g->stream));

@@ -61,6 +61,7 @@ struct DNgpuVolume {
     unsigned char* dstage; size_t dstageCap;
     cudaEvent_t stageFree;
     cudaEvent_t copyDone;       // eviction / restore: the volume's queued work, then its last copy on the copy stream
+    int restorePending;         // restored by dn_cuda_map_restore_async: the volume's stream has not waited yet
     DevState* hst;                      // pinned copy of DevState
     // device staging for host-memory draws
     float4* dimg; uint32_t* dhit; uint8_t* dface; size_t dimgCap;
@@ -125,6 +126,18 @@ template <class T> static int valloc(DNgpuVolume* g, T*& p, size_t count, cudaSt
         CK(cudaMalloc((void**)&p, count * sizeof(T)));
     }
     return DN_CUDA_OK;
+}
+
+// An evicted map cannot be used.  A map restored by dn_cuda_map_restore_async gets its stream's wait for the
+// restore copies here, so that the work an entry point queues next sees its arrays.
+static inline bool map_evicted(DNgpuVolume* g)
+{
+    if (g->evicted) return true;
+    if (g->restorePending) {
+        cudaStreamWaitEvent(g->stream, g->copyDone, 0);
+        g->restorePending = 0;
+    }
+    return false;
 }
 
 static inline dn::DevMap dev_map(const DNgpuVolume* g)

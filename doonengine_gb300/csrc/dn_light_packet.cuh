@@ -284,6 +284,7 @@ __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLi
                     bool more = false, add_ = false;
                     f3 sc = mk(0.0f, 0.0f, 0.0f);
                     if (hs == 1u) {
+                        hit_position(s);
                         Voxel hv;
                         decompress(m, hit_index(s, hitIdx), hv);
                         const i3 hp{f2i(truncf(s.pos.x)), f2i(truncf(s.pos.y)), f2i(truncf(s.pos.z))};

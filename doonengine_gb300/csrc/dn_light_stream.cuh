@@ -72,6 +72,7 @@ struct Seg {
     uint32_t flags;      // bit0 inner level, bit1 ignore (current level), bit2 saved outer ignore, bit3 requested,
                          // bit4 degenerate direction (D16), bit5 the current chunk's materials are all opaque,
                          // bit6 the segment ended on a voxel of such a chunk (hitIdx holds its local index),
+                         // bit7 the segment ended on a voxel and pos is not yet its hit position,
                          // bits 8-31 cells visited by the segment (D16 cell cap)
     f3 cadd;
     float cmul;
@@ -94,9 +95,9 @@ __device__ __forceinline__ void seg_begin(Seg& s, f3 pos, f3 dir, f3 inv)
     if (!finite_dir(inv)) { s.cpos.x = -1; s.flags = 2u | 16u; }
 }
 
-// Advances one traversal step.  Returns 0 while the segment continues, 1 on an opaque hit (s.pos moved to
-// the hit; hitIdx = pool index of the voxel, or its local index in s.rec when flags bit 6 is set -- hit_index()
-// gives the pool index), 2 when it leaves the map.  The common case (a chunk cell that is not loaded, or a
+// Advances one traversal step.  Returns 0 while the segment continues, 1 on an opaque hit (hit_position()
+// moves s.pos to the hit; hitIdx = pool index of the voxel, or its local index in s.rec when flags bit 6 is
+// set -- hit_index() gives the pool index), 2 when it leaves the map.  The common case (a chunk cell that is not loaded, or a
 // voxel cell that is empty) runs one code path for both levels; entering a chunk, leaving it, reaching a voxel
 // and leaving the map are the divergent events.  In a chunk marked 3 in the tile map (every material of its
 // voxels opaque under the launch's materials, mark_opaque_word) the first occupied voxel ends the ray without
@@ -162,11 +163,8 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
             c.inner++;
             c.hits++;
             if (s.flags & 32u) {
-                const float t = s.clastMin + EPS;
-                const f3 cp = add(s.cp, muls(s.dir, t));
-                s.pos = add(mk((float)s.opos.x, (float)s.opos.y, (float)s.opos.z), muls(cp, INV_CHUNK));
                 hitIdx = idx;
-                s.flags |= 64u;
+                s.flags |= 64u | 128u;   // the hit position is formed when shading needs it (hit_position)
                 return 1u;
             }
             const uint32_t vi = __ldg(&s.rec->voxBase) + vox_rank(s.rec, idx);
@@ -174,10 +172,8 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
             const uint32_t material = vw.x >> 24;
             const Material& mat = mats[material];
             if (mat.opacity == 1.0f) {
-                const float t = s.clastMin + EPS;
-                const f3 cp = add(s.cp, muls(s.dir, t));
-                s.pos = add(mk((float)s.opos.x, (float)s.opos.y, (float)s.opos.z), muls(cp, INV_CHUNK));
                 hitIdx = vi;
+                s.flags |= 128u;
                 return 1u;
             }
             const uint32_t thisID = (vw.y & 0xFFFFFF00u) | material;
@@ -228,6 +224,18 @@ __device__ __forceinline__ f3 rcp3(f3 d) { return mk(__frcp_rn(d.x), __frcp_rn(d
 __device__ __forceinline__ uint32_t hit_index(const Seg& s, uint32_t hitIdx)
 {
     return (s.flags & 64u) ? __ldg(&s.rec->voxBase) + vox_rank(s.rec, hitIdx) : hitIdx;
+}
+
+// the hit position of a segment that ended on a voxel (voxelShared.comp:362-364), formed when shading needs
+// it: shadow rays never do.  The segment's state is unchanged since the hit.
+__device__ __forceinline__ void hit_position(Seg& s)
+{
+    if (s.flags & 128u) {
+        const float t = s.clastMin + EPS;
+        const f3 cp = add(s.cp, muls(s.dir, t));
+        s.pos = add(mk((float)s.opos.x, (float)s.opos.y, (float)s.opos.z), muls(cp, INV_CHUNK));
+        s.flags &= ~128u;
+    }
 }
 
 // per-lane job state of the voxel being lit
@@ -299,6 +307,7 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
         const bool hit = hitState == 1u;
         hitState = 0;
         Voxel hv;
+        if (hit) hit_position(s);
         if (hit) decompress(m, hit_index(s, hitIdx), hv);
         if (j.phase == PH_SPEC) {
             // specular_ray body after step_map (voxelLighting.comp:98-144)

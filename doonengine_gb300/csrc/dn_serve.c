@@ -36,6 +36,7 @@ typedef struct VolumeSlot
 	uint64_t lastTick;               /* last tick that used the volume (LRU) */
 	unsigned int inFlight;           /* ticks in flight that use the volume */
 	int resident;
+	int restoring;                   /* resident, its restore copies possibly still running */
 } VolumeSlot;
 
 typedef struct Tick
@@ -211,7 +212,7 @@ static bool enforce_budget(DNserver* s, uint64_t extra, const uint8_t* inTick)
 		int victim = -1;
 		for (unsigned int i = 0; i < s->nslots; i++) {
 			VolumeSlot* c = &s->slots[i];
-			if (!c->resident || c->inFlight || (inTick && inTick[i])) continue;
+			if (!c->resident || c->inFlight || c->restoring || (inTick && inTick[i])) continue;
 			if (victim < 0 || c->lastTick < s->slots[victim].lastTick) victim = (int)i;
 		}
 		if (victim < 0) return false;
@@ -227,24 +228,40 @@ static bool enforce_budget(DNserver* s, uint64_t extra, const uint8_t* inTick)
 	return true;
 }
 
-/* makes volume v resident within the budget; false when that is impossible now.  A volume larger than
- * the whole budget still runs once nothing else is resident. */
+/* true when volume v can join the tick being built: resident with its restore copies done.  An evicted
+ * volume is restored within the budget without any stream waiting for it (dn_cuda_map_restore_async), and
+ * joins a later tick once the copies are done, so the other volumes' requests never wait for them.  False
+ * also when the budget cannot make room now; a volume larger than the whole budget still runs once nothing
+ * else is resident. */
 static bool admit(DNserver* s, unsigned int v, const uint8_t* inTick)
 {
 	VolumeSlot* slot = &s->slots[v];
-	if (slot->resident) return true;
+	if (slot->resident) {
+		if (!slot->restoring) return true;
+		if (dn_cuda_map_restore_query(slot->vol->gpu) == 0) return false;
+		slot->restoring = 0;   /* done (an error shows at the volume's next use) */
+		return true;
+	}
 	if (!enforce_budget(s, dn_cuda_map_footprint(slot->vol->gpu), inTick)) {
 		unsigned int n = 0;
 		resident_bytes(s, &n);
 		if (n) return false;
 	}
 	const double r0 = DN_server_clock();
-	if (dn_cuda_map_restore(slot->vol->gpu) != DN_CUDA_OK) return false;
+	if (dn_cuda_map_restore_async(slot->vol->gpu) != DN_CUDA_OK) return false;
 	s->stats.restoreSeconds += DN_server_clock() - r0;
 	slot->resident = 1;
+	slot->restoring = 1;
 	s->stats.restores++;
 	s->stats.restoredBytes += dn_cuda_map_footprint(slot->vol->gpu);
-	return true;
+	return false;
+}
+
+static bool any_restoring(const DNserver* s)
+{
+	for (unsigned int i = 0; i < s->nslots; i++)
+		if (s->slots[i].restoring) return true;
+	return false;
 }
 
 /* ----------------------------------------------------------------- ticks */
@@ -459,16 +476,18 @@ static void* serve_main(void* arg)
 		int queued = 0;
 		for (unsigned int i = 0; i < s->nslots && !queued; i++) queued = s->slots[i].head != NULL;
 		if (stop && !queued && !s->tickCount) break;
-		if (s->tickCount) { sleep_us(20); continue; }
+		if (s->tickCount || (queued && any_restoring(s))) { sleep_us(20); continue; }
 		if (!queued && !s->settled) {
 			/* idle: volumes grow when their syncs stage chunks, so a busy period can end above the budget;
 			 * evict down to it now, while no request waits (DN_server_drain waits for this too) */
 			enforce_budget(s, 0, NULL);
 			if (s->cfg.deviceBudgetBytes) {
-				/* which maps are evicted changes under load, and small maps round up to whole slabs: keep a
-				 * quarter of the pinned memory in use free, pinned now rather than by an eviction in a tick */
+				/* which maps are evicted changes under load, and small maps round up to whole slabs: keep as
+				 * much pinned memory free as is in use, pinned now rather than by an eviction in a tick
+				 * (pinning a 64 MiB slab takes milliseconds, and the serving thread would hold every request
+				 * for it; measured, a quarter and a half of it still left slabs to pin under load) */
 				const uint64_t pinned = dn_cuda_host_pinned(), spare = dn_cuda_host_pinned_free();
-				if (pinned > spare) dn_cuda_host_headroom((pinned - spare) / 4);
+				if (pinned > spare) dn_cuda_host_headroom(pinned - spare);
 			}
 			pthread_mutex_lock(&s->lock);
 			if (!s->inHead) s->settled = 1;
@@ -581,7 +600,8 @@ void DN_server_destroy(DNserver* s)
 	}
 	for (unsigned int i = 0; i < s->nslots; i++) {
 		/* volumes go back to the caller resident and out of the server's batch */
-		if (!s->slots[i].resident) dn_cuda_map_restore(s->slots[i].vol->gpu);
+		if (!s->slots[i].resident || s->slots[i].restoring) dn_cuda_map_restore(s->slots[i].vol->gpu);
+		s->slots[i].restoring = 0;
 		DN_batch_remove(s->batch, s->slots[i].vol);
 	}
 	DN_batch_destroy(s->batch);

@@ -267,6 +267,14 @@ uint64_t dn_cuda_map_footprint(struct DNgpuVolume* g);
 int dn_cuda_map_is_resident(struct DNgpuVolume* g);
 int dn_cuda_map_evict(struct DNgpuVolume* g);
 int dn_cuda_map_restore(struct DNgpuVolume* g);
+/* Restore without making the volume's stream wait: the allocations and copies are queued on the restore
+ * stream and the call returns at once.  dn_cuda_map_restore_query returns 1 once the copies are done (and
+ * for a resident volume with nothing pending), 0 while they run or the volume is evicted, -1 on error.  A
+ * server admits the volume to its next tick only then, so its other volumes' work never waits for the
+ * copies.  Any other entry point (dn_cuda_map_restore included) used on the volume first makes its stream
+ * wait for them. */
+int dn_cuda_map_restore_async(struct DNgpuVolume* g);
+int dn_cuda_map_restore_query(struct DNgpuVolume* g);
 /* Evictions copy into a process-wide pool of pinned 64 MiB host slabs, pinned when first needed and reused
  * by every volume afterwards.  dn_cuda_host_reserve pins slabs until the pool holds 'bytes', so that no
  * eviction under load has to pin host memory (a server whose volumes exceed its device budget reserves the

@@ -227,10 +227,19 @@ def test_submit_rejects_bad_requests(gpu_ready):
 
 def test_direct_eviction_behind_queued_work_is_exact(gpu_ready):
     """dn_cuda_map_evict and dn_cuda_map_restore called right behind queued draws, syncs and lighting
-    launches, without waiting for them: the copies run on their own stream, ordered after the volume's work
-    and before its next work.  Eviction after every phase and a twin that never leaves the device give the
-    same images, tile state and lighting, bit for bit."""
+    launches, without waiting for them: the copies run on their own streams, ordered after the volume's work
+    and before its next work.  Every other round trip restores with dn_cuda_map_restore_async and is never
+    polled, so the next entry point must make the volume's stream wait by itself.  Eviction after every
+    phase and a twin that never leaves the device give the same images, tile state and lighting, bit for
+    bit."""
     lib = dn.load()
+    trips = [0]
+
+    def restore(g):
+        trips[0] += 1
+        if trips[0] % 2:
+            return lib.dn_cuda_map_restore(g) == 0
+        return lib.dn_cuda_map_restore_async(g) == 0 and lib.dn_cuda_map_restore_query(g) in (0, 1)
     sp = dict(SPECS[2])
     twins = []
     for _ in range(2):
@@ -243,7 +252,7 @@ def test_direct_eviction_behind_queued_work_is_exact(gpu_ready):
         for f in range(6):
             for which, vol in enumerate(twins):
                 roundtrip = (lambda: (lib.dn_cuda_map_evict(vol.s.gpu) == 0 and
-                                      lib.dn_cuda_map_restore(vol.s.gpu) == 0)) if which == 1 else (lambda: True)
+                                      restore(vol.s.gpu))) if which == 1 else (lambda: True)
                 v, p = vol.view_proj(H / W)
                 vol.draw(images[which][f], v, p)
                 assert roundtrip()
@@ -256,7 +265,15 @@ def test_direct_eviction_behind_queued_work_is_exact(gpu_ready):
                     if which == 1:
                         assert lib.dn_cuda_map_evict(vol.s.gpu) == 0
                         assert lib.dn_cuda_map_is_resident(vol.s.gpu) == 0
-                        assert lib.dn_cuda_map_restore(vol.s.gpu) == 0
+                        assert lib.dn_cuda_map_restore_query(vol.s.gpu) == 0
+                        assert lib.dn_cuda_map_restore_async(vol.s.gpu) == 0
+                        import time
+                        for _ in range(10000):
+                            q = lib.dn_cuda_map_restore_query(vol.s.gpu)
+                            if q != 0:
+                                break
+                            time.sleep(0.0001)
+                        assert q == 1
         for vol in twins:
             assert vol.finish(), lib.dn_cuda_last_error().decode()
         same(snapshot(twins[0], images[0]), snapshot(twins[1], images[1]), "evicted twin")
