@@ -189,7 +189,8 @@ extern "C" void dn_cuda_map_destroy(DNgpuVolume* g)
     vfree(g, g->reqs); vfree(g, g->lightOut); vfree(g, g->st); vfree(g, g->dtab); vfree(g, g->dstage);
     vfree(g, g->dimg); vfree(g, g->dhit); vfree(g, g->dface);
     if (g->stream) cudaStreamSynchronize(g->stream);
-    if (g->hstage) cudaFreeHost(g->hstage);
+    for (int k = 0; k < 2; k++)
+        if (g->hstage[k]) cudaFreeHost(g->hstage[k]);
     if (g->hst) cudaFreeHost(g->hst);
     if (g->evicted) {
         // an evicted volume's slabs go back to the pool (no copy reads them any more)
@@ -197,7 +198,8 @@ extern "C" void dn_cuda_map_destroy(DNgpuVolume* g)
         for (uint32_t i = 0; i < g->evictedSlabs; i++) g_freeSlabs.push_back(g->evicted[i]);
         free(g->evicted);
     }
-    if (g->stageFree) cudaEventDestroy(g->stageFree);
+    for (int k = 0; k < 2; k++)
+        if (g->stageFree[k]) cudaEventDestroy(g->stageFree[k]);
     if (g->copyDone) cudaEventDestroy(g->copyDone);
     if (g->ownStream) cudaStreamDestroy(g->ownStream);
     delete g;
@@ -237,7 +239,8 @@ extern "C" int dn_cuda_map_create(uint32_t sx, uint32_t sy, uint32_t sz, uint32_
     cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete g; return dn_set_err(DN_CUDA_ERR_LAUNCH, "stream: %s", cudaGetErrorString(e)); }
     g->ownStream = g->stream;
-    e = cudaEventCreateWithFlags(&g->stageFree, cudaEventDisableTiming);
+    e = cudaEventCreateWithFlags(&g->stageFree[0], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->stageFree[1], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->copyDone, cudaEventDisableTiming);
     if (e != cudaSuccess) rc = dn_set_err(DN_CUDA_ERR_LAUNCH, "event: %s", cudaGetErrorString(e));
     if (!rc) rc = alloc_tiles(g);
@@ -852,7 +855,7 @@ __global__ void k_clamp_requests(DevState* st, uint64_t cap)
     if (st->w[ST_REQ] > cap) st->w[ST_REQ] = (uint32_t)cap;
 }
 
-static int stage_reserve(DNgpuVolume* g, size_t total);
+static int stage_reserve(DNgpuVolume* g, size_t total, unsigned char** host, int* which);
 
 int dn_stage_ops(DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops, const dn_chunk_record* records,
                  uint32_t nrecords, const uint32_t* voxelWords, uint64_t nvoxels)
@@ -865,21 +868,22 @@ int dn_stage_ops(DNgpuVolume* g, const dn_tile_op* ops, uint32_t nops, const dn_
         const size_t bVox = (size_t)nvoxels * 8u;
         const size_t oRec = (bOps + 15) & ~(size_t)15, oOff = (oRec + bRec + 15) & ~(size_t)15,
                      oVox = (oOff + bOff + 15) & ~(size_t)15, total = oVox + bVox;
-        CK(cudaEventSynchronize(g->stageFree));
-        int rc = stage_reserve(g, total);
+        unsigned char* hs = nullptr;
+        int which = 0;
+        int rc = stage_reserve(g, total, &hs, &which);
         if (rc) return rc;
-        memcpy(g->hstage, ops, bOps);
-        if (bRec) memcpy(g->hstage + oRec, records, bRec);
-        uint64_t* off = (uint64_t*)(g->hstage + oOff);
+        memcpy(hs, ops, bOps);
+        if (bRec) memcpy(hs + oRec, records, bRec);
+        uint64_t* off = (uint64_t*)(hs + oOff);
         uint64_t acc = 0;
         for (uint32_t r = 0; r < nrecords; r++) { off[r] = acc; acc += records[r].nvox; }
         if (acc != nvoxels) return dn_set_err(DN_CUDA_ERR_ARG, "voxel word count %llu != %llu", (unsigned long long)acc, (unsigned long long)nvoxels);
         for (uint32_t o = 0; o < nops; o++)
             if ((ops[o].flags & DN_PEND_STAGED) && ops[o].recordIndex >= nrecords)
                 return dn_set_err(DN_CUDA_ERR_ARG, "op %u references record %u of %u", o, ops[o].recordIndex, nrecords);
-        if (bVox) memcpy(g->hstage + oVox, voxelWords, bVox);
-        CK(cudaMemcpyAsync(g->dstage, g->hstage, total, cudaMemcpyHostToDevice, g->stream));
-        CK(cudaEventRecord(g->stageFree, g->stream));
+        if (bVox) memcpy(hs + oVox, voxelWords, bVox);
+        CK(cudaMemcpyAsync(g->dstage, hs, total, cudaMemcpyHostToDevice, g->stream));
+        CK(cudaEventRecord(g->stageFree[which], g->stream));
         COUNT_LAUNCH();
         k_sync_stage<<<nops < 65535u ? nops : 65535u, 128, 0, g->stream>>>(
             (const dn_tile_op*)g->dstage, nops, (const dn_chunk_record*)(g->dstage + oRec),
@@ -901,18 +905,31 @@ extern "C" size_t dn_cuda_stage_part_limit(size_t bytes)
     return prev;
 }
 
-// grows the volume's pinned and device staging buffers to 'total' bytes (the host buffer must be free)
-static int stage_reserve(DNgpuVolume* g, size_t total)
+// the pinned upload buffer for the next upload, grown to 'total' bytes, and the device staging buffer
+// grown likewise: the last buffer when its upload is done, else the other one (waiting only for its older
+// upload, normally long done)
+static int stage_reserve(DNgpuVolume* g, size_t total, unsigned char** host, int* which)
 {
-    if (total > g->hstageCap) {
-        if (g->hstage) cudaFreeHost(g->hstage);
-        g->hstage = nullptr;
-        g->hstageCap = 0;
+    int k = g->stageCur;
+    const cudaError_t q = cudaEventQuery(g->stageFree[k]);
+    if (q == cudaErrorNotReady) {
+        k ^= 1;
+        CK(cudaEventSynchronize(g->stageFree[k]));
+    } else if (q != cudaSuccess) {
+        CK(q);
+    }
+    if (total > g->hstageCap[k]) {
+        if (g->hstage[k]) cudaFreeHost(g->hstage[k]);
+        g->hstage[k] = nullptr;
+        g->hstageCap[k] = 0;
         size_t nc = total + total / 2 + 4096;
         COUNT_ALLOC();
-        CK(cudaMallocHost((void**)&g->hstage, nc));
-        g->hstageCap = nc;
+        CK(cudaMallocHost((void**)&g->hstage[k], nc));
+        g->hstageCap[k] = nc;
     }
+    g->stageCur = k;
+    *host = g->hstage[k];
+    *which = k;
     if (total > g->dstageCap) {
         if (!(g->poolMask & vol_array_bit(g, &g->dstage))) CK(cudaStreamSynchronize(g->stream));
         vfree(g, g->dstage);
@@ -954,13 +971,14 @@ static int dn_stage_chunks(DNgpuVolume* g, const dn_pack_params* pk, const dn_ti
         const size_t oRec = (oOps + (size_t)n * sizeof(dn_tile_op) + 15) & ~(size_t)15;
         const size_t oVox = (oRec + (size_t)nrec * sizeof(dn_chunk_record) + 15) & ~(size_t)15;
         const size_t total = oVox + (size_t)nrec * CHUNK_VOXEL_BYTES;
-        CK(cudaEventSynchronize(g->stageFree));
-        int rc = stage_reserve(g, total);
+        unsigned char* hs = nullptr;
+        int which = 0;
+        int rc = stage_reserve(g, total, &hs, &which);
         if (rc) return rc;
-        memcpy(g->hstage, pk, sizeof(dn_pack_params));
-        dn_tile_op* hops = (dn_tile_op*)(g->hstage + oOps);
-        dn_chunk_record* hrec = (dn_chunk_record*)(g->hstage + oRec);
-        unsigned char* hvox = g->hstage + oVox;
+        memcpy(hs, pk, sizeof(dn_pack_params));
+        dn_tile_op* hops = (dn_tile_op*)(hs + oOps);
+        dn_chunk_record* hrec = (dn_chunk_record*)(hs + oRec);
+        unsigned char* hvox = hs + oVox;
         uint32_t k = 0;
         for (uint32_t j = 0; j < n; j++) {
             dn_tile_op op = ops[o0 + j];
@@ -971,8 +989,8 @@ static int dn_stage_chunks(DNgpuVolume* g, const dn_pack_params* pk, const dn_ti
             }
             hops[j] = op;
         }
-        CK(cudaMemcpyAsync(g->dstage, g->hstage, total, cudaMemcpyHostToDevice, g->stream));
-        CK(cudaEventRecord(g->stageFree, g->stream));
+        CK(cudaMemcpyAsync(g->dstage, hs, total, cudaMemcpyHostToDevice, g->stream));
+        CK(cudaEventRecord(g->stageFree[which], g->stream));
         COUNT_LAUNCH();
         k_pack_stage<<<n < 65535u ? n : 65535u, 512, 0, g->stream>>>(
             (const dn_tile_op*)(g->dstage + oOps), n, (const dn_chunk_record*)(g->dstage + oRec),

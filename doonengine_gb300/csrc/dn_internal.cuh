@@ -57,9 +57,12 @@ struct DNgpuVolume {
     DevState* st;
     dn::LightTables* dtab;              // materials and shadow directions of the last lighting launch (k_light_packet)
     // pinned staging for sync uploads and small readbacks
-    unsigned char* hstage; size_t hstageCap;
+    // two pinned upload buffers: a sync takes one whose last upload is done, so the host does not wait for
+    // the previous sync's upload while that sync's work is still queued (a tick in flight)
+    unsigned char* hstage[2]; size_t hstageCap[2];
     unsigned char* dstage; size_t dstageCap;
-    cudaEvent_t stageFree;
+    cudaEvent_t stageFree[2];   // after each buffer's last upload
+    int stageCur;               // the buffer of the last upload
     cudaEvent_t copyDone;       // eviction / restore: the volume's queued work, then its last copy on the copy stream
     int restorePending;         // restored by dn_cuda_map_restore_async: the volume's stream has not waited yet
     DevState* hst;                      // pinned copy of DevState
