@@ -338,6 +338,7 @@ _SIGS = [
     ("dn_cuda_host_pinned", c_uint64, []),
     ("dn_cuda_host_pinned_free", c_uint64, []),
     ("dn_cuda_host_headroom", c_int, [c_uint64]),
+    ("dn_cuda_host_slab_bytes", c_uint64, []),
     ("dn_cuda_event_query", c_int, [c_void_p]),
     ("dn_cuda_kernel_names", c_char_p, []),
     ("dn_cuda_launch_count", c_uint64, []),

@@ -380,6 +380,8 @@ extern "C" uint64_t dn_cuda_host_pinned(void)
     return (uint64_t)g_slabs.size() * HOST_SLAB;
 }
 
+extern "C" uint64_t dn_cuda_host_slab_bytes(void) { return (uint64_t)HOST_SLAB; }
+
 extern "C" uint64_t dn_cuda_host_pinned_free(void)
 {
     std::lock_guard<std::mutex> lock(g_slabMutex);

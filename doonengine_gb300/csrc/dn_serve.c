@@ -476,7 +476,17 @@ static void* serve_main(void* arg)
 		int queued = 0;
 		for (unsigned int i = 0; i < s->nslots && !queued; i++) queued = s->slots[i].head != NULL;
 		if (stop && !queued && !s->tickCount) break;
-		if (s->tickCount || (queued && any_restoring(s))) { sleep_us(20); continue; }
+		if (s->tickCount || (queued && any_restoring(s))) {
+			/* the GPU is busy: pin one more slab if fewer are free than in use (evictions under load then
+			 * find them pinned; volumes keep growing as their chunks stream in, so the evicted set does) */
+			if (s->cfg.deviceBudgetBytes) {
+				const uint64_t pinned = dn_cuda_host_pinned(), spare = dn_cuda_host_pinned_free();
+				if (pinned - spare > spare && dn_cuda_host_headroom(spare + dn_cuda_host_slab_bytes()) == DN_CUDA_OK)
+					continue;
+			}
+			sleep_us(20);
+			continue;
+		}
 		if (!queued && !s->settled) {
 			/* idle: volumes grow when their syncs stage chunks, so a busy period can end above the budget;
 			 * evict down to it now, while no request waits (DN_server_drain waits for this too) */

@@ -285,6 +285,8 @@ uint64_t dn_cuda_host_pinned(void);
  * server pins ahead while idle: evictions of smaller maps take more slabs for the same bytes) */
 uint64_t dn_cuda_host_pinned_free(void);
 int dn_cuda_host_headroom(uint64_t bytes);
+/* the size of one slab of the pool (64 MiB) */
+uint64_t dn_cuda_host_slab_bytes(void);
 /* 1 when the work recorded by ev has completed, 0 while pending, negative on error */
 int dn_cuda_event_query(void* ev);
 
