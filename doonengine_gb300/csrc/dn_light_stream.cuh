@@ -95,6 +95,35 @@ __device__ __forceinline__ void seg_begin(Seg& s, f3 pos, f3 dir, f3 inv)
     if (!finite_dir(inv)) { s.cpos.x = -1; s.flags = 2u | 16u; }
 }
 
+// Enters the loaded chunk of chunk cell idx (tile state cst >= 2) from the chunk level
+// (voxelShared.comp:441-449): saves the chunk-level DDA state and starts the voxel-level DDA at the entry point.
+__device__ __forceinline__ void seg_enter(Seg& s, const DevMap& m, Counters& c, uint32_t idx, uint32_t cst, f3 delta,
+                                          i3 step)
+{
+    c.outer++;
+    c.entered++;
+    if (m.ttouch[idx] == 0) m.ttouch[idx] = 1;
+    const float tt = s.clastMin - EPS;
+    const f3 up = add(s.pos, muls(s.dir, tt));
+    f3 cp = mk((up.x - (float)s.cpos.x) * 8.0f, (up.y - (float)s.cpos.y) * 8.0f, (up.z - (float)s.cpos.z) * 8.0f);
+    const float lo = EPS, hi_ = 8.0f - EPS;
+    // cp is finite here (a finite origin and direction, D16), so fminf / fmaxf give GLSL clamp's values and
+    // the floors below are 0..7: a plain conversion, and fl itself for (float)cpos
+    cp.x = fminf(fmaxf(cp.x, lo), hi_); cp.y = fminf(fmaxf(cp.y, lo), hi_); cp.z = fminf(fmaxf(cp.z, lo), hi_);
+    s.cp = cp;
+    s.opos = s.cpos; s.oside = s.cside; s.olastMin = s.clastMin;
+    const f3 fl = vfloor(cp);
+    s.cpos.x = (int32_t)fl.x; s.cpos.y = (int32_t)fl.y; s.cpos.z = (int32_t)fl.z;
+    const f3 sg = mk((float)step.x, (float)step.y, (float)step.z);
+    s.cside.x = (sg.x * (fl.x - cp.x) + sg.x * 0.5f + 0.5f) * delta.x;
+    s.cside.y = (sg.y * (fl.y - cp.y) + sg.y * 0.5f + 0.5f) * delta.y;
+    s.cside.z = (sg.z * (fl.z - cp.z) + sg.z * 0.5f + 0.5f) * delta.z;
+    s.clastMin = 0.0f;
+    s.rec = &m.rec[__ldg(&m.tword[idx]) & SLOT_MASK];
+    // inner level; the chunk inherits ignoreFirst; bit5: the chunk is marked opaque
+    s.flags = (s.flags & ~(4u | 32u)) | 1u | ((s.flags & 2u) << 1) | (cst == 3u ? 32u : 0u);
+}
+
 // Advances one traversal step.  Returns 0 while the segment continues, 1 on an opaque hit (hit_position()
 // moves s.pos to the hit; hitIdx = pool index of the voxel, or its local index in s.rec when flags bit 6 is
 // set -- hit_index() gives the pool index), 2 when it leaves the map.  The common case (a chunk cell that is not loaded, or a
@@ -130,29 +159,7 @@ __device__ __forceinline__ uint32_t seg_step(Seg& s, const DevMap& m, const Mate
                 if (s.flags & 16u) count_degenerate(m);
                 return 2u;
             }
-            // a loaded chunk: enter it (voxelShared.comp:441-449)
-            c.outer++;
-            c.entered++;
-            if (m.ttouch[idx] == 0) m.ttouch[idx] = 1;
-            const float tt = s.clastMin - EPS;
-            const f3 up = add(s.pos, muls(s.dir, tt));
-            f3 cp = mk((up.x - (float)s.cpos.x) * 8.0f, (up.y - (float)s.cpos.y) * 8.0f, (up.z - (float)s.cpos.z) * 8.0f);
-            const float lo = EPS, hi_ = 8.0f - EPS;
-            // cp is finite here (a finite origin and direction, D16), so fminf / fmaxf give GLSL clamp's
-            // values and the floors below are 0..7: a plain conversion, and fl itself for (float)cpos
-            cp.x = fminf(fmaxf(cp.x, lo), hi_); cp.y = fminf(fmaxf(cp.y, lo), hi_); cp.z = fminf(fmaxf(cp.z, lo), hi_);
-            s.cp = cp;
-            s.opos = s.cpos; s.oside = s.cside; s.olastMin = s.clastMin;
-            const f3 fl = vfloor(cp);
-            s.cpos.x = (int32_t)fl.x; s.cpos.y = (int32_t)fl.y; s.cpos.z = (int32_t)fl.z;
-            const f3 sg = mk((float)step.x, (float)step.y, (float)step.z);
-            s.cside.x = (sg.x * (fl.x - cp.x) + sg.x * 0.5f + 0.5f) * delta.x;
-            s.cside.y = (sg.y * (fl.y - cp.y) + sg.y * 0.5f + 0.5f) * delta.y;
-            s.cside.z = (sg.z * (fl.z - cp.z) + sg.z * 0.5f + 0.5f) * delta.z;
-            s.clastMin = 0.0f;
-            s.rec = &m.rec[__ldg(&m.tword[idx]) & SLOT_MASK];
-            // inner level; the chunk inherits ignoreFirst; bit5: the chunk is marked opaque
-            s.flags = (s.flags & ~(4u | 32u)) | 1u | ((s.flags & 2u) << 1) | (cst == 3u ? 32u : 0u);
+            seg_enter(s, m, c, idx, cst, delta, step);
             return 0u;
         }
         if (!inb) {
