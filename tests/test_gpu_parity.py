@@ -337,7 +337,19 @@ def test_raster_composition(gpu_ready, tex_scale, transparent):
 @pytest.mark.parametrize("K", [1, 2, 3, 5])
 def test_small_fan_counts(gpu_ready, K):
     """Few direct / specular rays per voxel: the packet kernel's pools then hold more than 16 voxels
-    (96 / K), so its per-pool sums take more than one round of lanes."""
+    (128 / K), so its per-pool sums take more than one round of lanes."""
+    pair = Pair("tiny", K=K)
+    try:
+        for _ in range(3):
+            pair.step()
+    finally:
+        pair.close()
+
+
+@pytest.mark.parametrize("K", [32, 33, 48, 64])
+def test_large_fan_counts(gpu_ready, K):
+    """A fan of exactly one warp, just over one, and up to the maximum of 64 rays per voxel: a pool then
+    holds 4, 3, 2 or 2 voxels, and a fan's rays span lanes of more than one refill."""
     pair = Pair("tiny", K=K)
     try:
         for _ in range(3):
