@@ -316,7 +316,9 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
         Voxel hv;
         if (hit) hit_position(s);
         if (hit) decompress(m, hit_index(s, hitIdx), hv);
-        if (j.phase == PH_SPEC) {
+        // the diffuse-only kernel's jobs never reach the specular and shadow phases: with DIFFONLY their
+        // code is left out of it (a smaller kernel: fewer instruction-fetch stalls)
+        if (!DIFFONLY && j.phase == PH_SPEC) {
             // specular_ray body after step_map (voxelLighting.comp:98-144)
             bool done = true;
             if (hit) {
@@ -368,7 +370,7 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
                 j.spec.z = j.spec.z + (sc.z * s.cmul + s.cadd.z) * j.jA.z;
             }
             if (done) { j.k++; j.b = 0; }
-        } else if (j.phase == PH_SHADOW) {
+        } else if (!DIFFONLY && j.phase == PH_SHADOW) {
             if (!hit) {
                 j.acc.x = j.acc.x + (sun.x * s.cmul + s.cadd.x);
                 j.acc.y = j.acc.y + (sun.y * s.cmul + s.cadd.y);
@@ -415,7 +417,7 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
     }
     // start the next segment of this voxel
     for (int guard = 0; guard < 8; guard++) {
-        if (j.phase == PH_SPEC) {
+        if (!DIFFONLY && j.phase == PH_SPEC) {
             if (j.k < p.K) {
                 if (p.specBounceLimit == 0u) { j.k++; continue; }
                 const Material& tm = mats[j.tmat];
@@ -431,7 +433,7 @@ __device__ __forceinline__ bool advance(Job& j, Seg& s, uint32_t& hitState, uint
             j.k = 0;
             continue;
         }
-        if (j.phase == PH_SHADOW) {
+        if (!DIFFONLY && j.phase == PH_SHADOW) {
             const uint32_t n = j.firstSample ? 1u : p.K;
             if (j.k < n) {
                 const uint32_t q = j.firstSample ? 64u : j.k;
