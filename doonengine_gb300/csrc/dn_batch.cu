@@ -83,7 +83,7 @@ __global__ void k_batch_reset(const CompactArgs* s, uint32_t ns)
     if (i < ns) s[i].st->w[ST_REQ] = 0;
 }
 
-__global__ void __launch_bounds__(256) k_draw_batch(const BatchDrawEntry* d, const uint32_t* start, uint32_t nd,
+__global__ void __launch_bounds__(256, DN_DRAW_MIN_BLOCKS) k_draw_batch(const BatchDrawEntry* d, const uint32_t* start, uint32_t nd,
                                                     unsigned long long* stats)
 {
     __shared__ Material smat[256];

@@ -605,7 +605,7 @@ extern "C" int dn_cuda_reserve(DNgpuVolume* g, uint32_t slotCap, uint64_t voxelC
 
 // ------------------------------------------------------------------ draw
 
-__global__ void __launch_bounds__(256) k_draw(const __grid_constant__ DrawArgs a)
+__global__ void __launch_bounds__(256, DN_DRAW_MIN_BLOCKS) k_draw(const __grid_constant__ DrawArgs a)
 {
     __shared__ Material smat[256];
     for (int i = threadIdx.x + threadIdx.y * blockDim.x; i < 256; i += blockDim.x * blockDim.y) smat[i] = a.mats[i];
