@@ -53,6 +53,19 @@ enum : uint32_t { PV_VALID = 1u, PV_FIRST = 2u, PV_SPEC = 4u, PV_DIFF = 8u };
 constexpr uint32_t PK_POOL_FAN = DN_PK_POOL_FAN;
 constexpr uint32_t PK_POOL_ALT = PK_POOL_FAN == 64u ? 128u : 64u;   // the batched autotuner's other pool size
 
+// Work units per request group in a one-map launch: a warp takes 32 / PK_PARTS voxels of a group at a time,
+// so that the launch does not end with a few warps finishing whole groups while the others have left.  Per
+// warp exit times on the large map's frame 11 with whole groups: the last warp left 2.7 ms after 90 % of
+// them had, 16 % of the warps' time idle; units of 16, 8 and 4 voxels measured +8 %, +12 % and +13 %.  A
+// many-map launch keeps whole groups: its queue is long enough that the tail is small, and smaller units
+// measured slower there (the setup of a unit runs on a fraction of the lanes).
+#ifndef DN_PK_PARTS
+#define DN_PK_PARTS 8
+#endif
+constexpr uint32_t PK_PARTS = DN_PK_PARTS;
+static_assert(PK_PARTS == 1u || PK_PARTS == 2u || PK_PARTS == 4u || PK_PARTS == 8u,
+              "a unit is 32, 16, 8 or 4 voxels of a group");
+
 template <uint32_t POOL>
 struct PacketWarpT {
     PacketVoxel v[32];
@@ -157,10 +170,14 @@ __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLi
     Counters c{0, 0, 0, 0, 0};
     uint32_t lit = 0;
     for (;;) {
-        uint32_t r = 0;
-        if (lane == 0) r = atomicAdd(counter, 1u);
-        r = __shfl_sync(0xFFFFFFFFu, r, 0);
-        if (r >= nreq) break;
+        uint32_t u = 0;
+        if (lane == 0) u = atomicAdd(counter, 1u);
+        u = __shfl_sync(0xFFFFFFFFu, u, 0);
+        constexpr uint32_t parts = MANY ? 1u : PK_PARTS;
+        if (u >= nreq * parts) break;
+        // unit u: lanes [part * 32 / parts, (part + 1) * 32 / parts) of request group r
+        const uint32_t r = u / parts;
+        const bool mine = lane / (32u / parts) == u % parts;
         // the group's map (warp-uniform)
         const BatchLightMap* e = nullptr;
         uint32_t req = r;
@@ -183,7 +200,8 @@ __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLi
         const f3 sunDir = mk(p.sunDir[0], p.sunDir[1], p.sunDir[2]);
         const uint32_t K = p.K;
 
-        packet_setup(W.v[lane], req, lane, m, p, mats, MANY ? e->reqs : one->reqs, MANY ? e->nsamples : one->nsamples, out);
+        if (mine) packet_setup(W.v[lane], req, lane, m, p, mats, MANY ? e->reqs : one->reqs, MANY ? e->nsamples : one->nsamples, out);
+        else W.v[lane].flags = 0;   // another unit's voxel: its warp sets it up and writes it
         __syncwarp();
         const uint32_t myFlags = W.v[lane].flags;
         const uint32_t specAll = __ballot_sync(0xFFFFFFFFu, (myFlags & (PV_VALID | PV_SPEC)) == (PV_VALID | PV_SPEC));
