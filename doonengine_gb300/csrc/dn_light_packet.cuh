@@ -169,31 +169,15 @@ __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLi
     const uint32_t batch = MANY ? many->batch : one->batch;
     Counters c{0, 0, 0, 0, 0};
     uint32_t lit = 0;
-#ifdef DN_PK_ADAPT
-    // voxels per unit: the largest power of two whose fans fit one pool, at least 32 / PK_PARTS
-    uint32_t ushift = 5u;
-    if constexpr (!MANY) {
-        const uint32_t fit = 31u - (uint32_t)__clz((int)(POOL / one->p.K));
-        const uint32_t lo = 5u - (31u - (uint32_t)__clz((int)PK_PARTS));
-        ushift = fit < lo ? lo : (fit > 5u ? 5u : fit);
-    }
-    const uint32_t parts = 32u >> ushift;
-#endif
     for (;;) {
         uint32_t u = 0;
         if (lane == 0) u = atomicAdd(counter, 1u);
         u = __shfl_sync(0xFFFFFFFFu, u, 0);
-#ifdef DN_PK_ADAPT
-        if (u >= nreq * parts) break;
-        const uint32_t r = u >> (5u - ushift);
-        const bool mine = (lane >> ushift) == (u & (parts - 1u));
-#else
         constexpr uint32_t parts = MANY ? 1u : PK_PARTS;
         if (u >= nreq * parts) break;
         // unit u: lanes [part * 32 / parts, (part + 1) * 32 / parts) of request group r
         const uint32_t r = u / parts;
         const bool mine = lane / (32u / parts) == u % parts;
-#endif
         // the group's map (warp-uniform)
         const BatchLightMap* e = nullptr;
         uint32_t req = r;
