@@ -3,7 +3,8 @@
  *
  * Every lit voxel casts two fans of K rays from one point: K specular rays around its reflection
  * direction (voxelLighting.comp:83-146, each up to specBounceLimit segments) and K shadow rays around the
- * sun direction (D8).  A warp takes one request group (32 voxels of one chunk) and traces the fans of
+ * sun direction (D8).  A warp takes one work unit -- 32 / PK_PARTS voxels of a request group (a group is 32
+ * voxels of one chunk) in a one-map launch, a whole group in a many-map launch -- and traces the fans of
  * PK_POOL_FAN / K of its voxels at a time as one pool: the pool's rays are numbered (specular fans first,
  * then the shadow rays), and a lane whose ray has ended takes the pool's next ray, so consecutive rays of
  * a fan run side by side and the lanes of a warp walk nearly the same cells (a fan's shadow rays are
