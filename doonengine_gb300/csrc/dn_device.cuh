@@ -215,20 +215,25 @@ __device__ __forceinline__ void init_dda(f3 dir, f3 inv, f3 p, i3& pos, f3& delt
     side.z = (s.z * ((float)pos.z - p.z) + s.z * 0.5f + 0.5f) * delta.z;
 }
 
-// iterate_DDA, voxelShared.comp:309-317 (branchless <= step; ties step several axes)
-__device__ __forceinline__ void iter_dda(f3 delta, i3 step, f3& side, i3& pos, f3& normal)
+// iterate_DDA, voxelShared.comp:309-317 (<= steps; ties step several axes), for finite, non-negative side
+// distances (every caller has a finite direction, D16, and the side distances start at +0 or above):
+// fminf then gives GLSL min's value, and adding delta only on the stepped axes gives exactly
+// side + (mask ? 1 : 0) * delta.  Returns min3 of the side distances before the step, the only use the
+// reference makes of lastSideDist.  (Measured on the draw against the literal form, bit-identical:
+// streaming edits +1.2-2.1 %, batched workload +0.9 %, 148 bytes of spills down to 40.)
+__device__ __forceinline__ float iter_dda_min(f3 delta, i3 step, f3& side, i3& pos, f3& normal)
 {
-    bool mx = side.x <= gmin(side.y, side.z);
-    bool my = side.y <= gmin(side.z, side.x);
-    bool mz = side.z <= gmin(side.x, side.y);
-    float fx = mx ? 1.0f : 0.0f, fy = my ? 1.0f : 0.0f, fz = mz ? 1.0f : 0.0f;
-    side.x = side.x + fx * delta.x;
-    side.y = side.y + fy * delta.y;
-    side.z = side.z + fz * delta.z;
+    const float gyz = fminf(side.y, side.z), gzx = fminf(side.z, side.x), gxy = fminf(side.x, side.y);
+    const float lastMin = fminf(gxy, side.z);
+    const bool mx = side.x <= gyz, my = side.y <= gzx, mz = side.z <= gxy;
+    if (mx) side.x = side.x + delta.x;
+    if (my) side.y = side.y + delta.y;
+    if (mz) side.z = side.z + delta.z;
     pos.x += (int32_t)mx * step.x; pos.y += (int32_t)my * step.y; pos.z += (int32_t)mz * step.z;
-    normal.x = fx * (float)(-step.x);
-    normal.y = fy * (float)(-step.y);
-    normal.z = fz * (float)(-step.z);
+    normal.x = (mx ? 1.0f : 0.0f) * (float)(-step.x);
+    normal.y = (my ? 1.0f : 0.0f) * (float)(-step.y);
+    normal.z = (mz ? 1.0f : 0.0f) * (float)(-step.z);
+    return lastMin;
 }
 
 struct RayCtx {
@@ -268,7 +273,8 @@ static __device__ __forceinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapP
     const ChunkRec* r = &m.rec[slot];
     const uint32_t base = __ldg(&r->voxBase);
     refracted = false;
-    i3 pos, step; f3 delta, side, lastSide = mk(0.0f, 0.0f, 0.0f);
+    i3 pos, step; f3 delta, side;
+    float lastMin = 0.0f;   // min3(lastSideDist)
     init_dda(rayDir, inv, rayPos, pos, delta, step, side);
     const uint32_t cap = step_cap(m.sx, m.sy, m.sz);
     while (in_chunk(pos)) {
@@ -285,12 +291,12 @@ static __device__ __forceinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapP
             uint2 w = __ldg(&m.vox[idx]);
             uint32_t thisID = (w.y & 0xFFFFFF00u) | (w.x >> 24);
             if (mat.opacity == 1.0f) {
-                float t = min3(lastSide) + EPS;
+                float t = lastMin + EPS;
                 rayPos = add(rayPos, muls(rayDir, t));
                 hi.tile = tile; hi.local = pos;
                 return true;
             } else if (ts.lastVoxID != thisID) {
-                f3 cur = add(rayPos, muls(rayDir, min3(lastSide)));
+                f3 cur = add(rayPos, muls(rayDir, lastMin));
                 cur = add(mk((float)mapPos.x, (float)mapPos.y, (float)mapPos.z), muls(cur, INV_CHUNK));
                 f3 to = sub(cur, c.orgRayPos);
                 if (maxDepth < 0.0f || dot(to, to) < maxDepth * maxDepth) {
@@ -300,7 +306,7 @@ static __device__ __forceinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapP
                     colorAdd.z = colorAdd.z + k * vox.albedo.z * c.sunStrength.z;
                     colorMult = colorMult * (1.0f - mat.opacity);
                 }
-                float rd = min3(lastSide);
+                float rd = lastMin;
                 if (c.refraction && rd > 0.0f) {
                     refracted = true;
                     rayPos = add(rayPos, muls(rayDir, rd + EPS));
@@ -309,7 +315,7 @@ static __device__ __forceinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapP
                     inv = mk(1.0f / rayDir.x, 1.0f / rayDir.y, 1.0f / rayDir.z);
                     if (!finite_dir(inv)) { count_degenerate(m); c.capped = true; return false; }
                     init_dda(rayDir, inv, rayPos, pos, delta, step, side);
-                    lastSide = mk(0.0f, 0.0f, 0.0f);
+                    lastMin = 0.0f;
                 }
                 ts.lastVoxID = thisID;
                 ts.lastVoxRefract = mat.refractIndex;
@@ -317,7 +323,7 @@ static __device__ __forceinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapP
         } else if (ts.lastVoxID != 255u) {
             if (c.refraction) {
                 refracted = true;
-                rayPos = add(rayPos, muls(rayDir, min3(lastSide) + EPS));
+                rayPos = add(rayPos, muls(rayDir, lastMin + EPS));
                 f3 old = rayDir;
                 f3 nn = mk(-vox.normal.x, -vox.normal.y, -vox.normal.z);
                 f3 n = (dot(nn, rayDir) < 0.0f) ? normalize(nn) : hitNormal;
@@ -326,13 +332,12 @@ static __device__ __forceinline__ bool step_chunk(RayCtx& c, TState& ts, i3 mapP
                 inv = mk(1.0f / rayDir.x, 1.0f / rayDir.y, 1.0f / rayDir.z);
                 if (!finite_dir(inv)) { count_degenerate(m); c.capped = true; return false; }
                 init_dda(rayDir, inv, rayPos, pos, delta, step, side);
-                lastSide = mk(0.0f, 0.0f, 0.0f);
+                lastMin = 0.0f;
             }
             ts.lastVoxID = 255u;
             ts.lastVoxRefract = 1.0f;
         }
-        lastSide = side;
-        iter_dda(delta, step, side, pos, hitNormal);
+        lastMin = iter_dda_min(delta, step, side, pos, hitNormal);
         ignoreFirst = false;
     }
     return false;
@@ -352,7 +357,8 @@ static __device__ __forceinline__ bool step_map(RayCtx& c, TState& ts, f3& rayDi
     c.capped = false;
     if (!finite_dir(inv)) { count_degenerate(m); return false; }
     const uint32_t cap = step_cap(m.sx, m.sy, m.sz);
-    i3 pos, step; f3 delta, side, lastSide = mk(0.0f, 0.0f, 0.0f);
+    i3 pos, step; f3 delta, side;
+    float lastMin = 0.0f;   // min3(lastSideDist)
     init_dda(rayDir, inv, rayPos, pos, delta, step, side);
     while (in_map(m, pos)) {
         if (c.segSteps >= cap) return false;
@@ -364,7 +370,7 @@ static __device__ __forceinline__ bool step_map(RayCtx& c, TState& ts, f3& rayDi
         if (st == 2u) {
             c.c.entered++;
             if (m.ttouch[t] == 0) m.ttouch[t] = 1;
-            float tt = min3(lastSide) - EPS;
+            float tt = lastMin - EPS;
             f3 up = add(rayPos, muls(rayDir, tt));
             f3 cp = mk((up.x - (float)pos.x) * 8.0f, (up.y - (float)pos.y) * 8.0f, (up.z - (float)pos.z) * 8.0f);
             const float lo = EPS, hi_ = 8.0f - EPS;
@@ -379,14 +385,13 @@ static __device__ __forceinline__ bool step_map(RayCtx& c, TState& ts, f3& rayDi
             if (refracted) {
                 rayPos = add(mk((float)pos.x, (float)pos.y, (float)pos.z), muls(cp, INV_CHUNK));
                 init_dda(rayDir, inv, rayPos, pos, delta, step, side);
-                lastSide = mk(0.0f, 0.0f, 0.0f);
+                lastMin = 0.0f;
             }
         } else if (!requested && st != 0u) {
             if (m.treq[t] == 0) m.treq[t] = 1;
             requested = true;
         }
-        lastSide = side;
-        iter_dda(delta, step, side, pos, hitNormal);
+        lastMin = iter_dda_min(delta, step, side, pos, hitNormal);
         ignoreFirst = false;
     }
     return false;
