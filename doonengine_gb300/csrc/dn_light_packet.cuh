@@ -125,40 +125,13 @@ __device__ __forceinline__ void packet_setup(PacketVoxel& pv, uint32_t req, uint
     pv.flags = PV_VALID | (first ? PV_FIRST : 0u) | (doSpec ? PV_SPEC : 0u) | (doDiff ? PV_DIFF : 0u);
 }
 
-// steps every lane's current segment until all of them ended (hs: 1 hit, 2 miss)
-__device__ __forceinline__ void packet_trace(bool stepping, Seg& s, const DevMap& m, const Material* mats,
-                                             const float* sun, Counters& c, uint32_t& hs, uint32_t& hitIdx)
-{
-    while (__any_sync(0xFFFFFFFFu, stepping)) {
-        if (stepping) {
-            const uint32_t r = seg_step(s, m, mats, sun, c, hitIdx);
-            if (r) { stepping = false; hs = r; }
-        }
-    }
-}
-
-// the k-th lane of segment sg of a pass over the voxels of 'mask': voxel index (or -1) and ray index
-__device__ __forceinline__ int pass_voxel(uint32_t mask, uint32_t base, uint32_t K, uint32_t lane, uint32_t round,
-                                          uint32_t& kk, uint32_t& sg)
-{
-    const uint32_t vpp = K <= 32u ? 32u / K : 1u;
-    sg = K <= 32u ? lane / K : 0u;
-    kk = K <= 32u ? lane - sg * K : lane + 32u * round;
-    const uint32_t n = (uint32_t)__popc(mask);
-    if (sg >= vpp || base + sg >= n || kk >= K) return -1;
-    // the (base + sg)-th set bit of mask
-    uint32_t mm = mask;
-    for (uint32_t t = 0; t < base + sg; t++) mm &= mm - 1u;
-    return __ffs(mm) - 1;
-}
-
-// The request groups of one launch.  Per group: (1) pools of PK_POOL_FAN/K voxels (at least one): every ray of their
-// specular fans, first-sample shadow rays and shadow fans is traced by whichever lane is free -- a lane
-// takes the pool's next ray as soon as its own ended, and the shading of ended segments runs once `batch`
-// lanes have one, so no lane waits for the slowest ray of a fan; each ray's contributions go to shared
-// memory, and when the pool is empty every voxel's sums are formed in the reference's order; (2) the
-// diffuse paths, one lane per voxel; (3) the running average and the write-out.  One stepping loop
-// serves both traced phases.
+// The work units of one launch (a part of a request group, or a whole group in a many-map launch).  Per
+// unit: (1) pools of PK_POOL_FAN/K voxels (at least one): every ray of their specular fans, first-sample
+// shadow rays and shadow fans is traced by whichever lane is free -- a lane takes the pool's next ray as
+// soon as its own ended, and the shading of ended segments runs once `batch` lanes have one, so no lane
+// waits for the slowest ray of a fan; each ray's contributions go to shared memory, and when the pool is
+// empty every voxel's sums are formed in the reference's order; (2) the write-out of each voxel's
+// specular lighting and direct light (its diffuse paths run in k_light_diffuse).
 template <bool MANY, uint32_t POOL = PK_POOL_FAN>
 __device__ __forceinline__ void packet_loop(const StreamArgs* one, const BatchLightArgs* many, PacketWarpT<POOL>& W)
 {
