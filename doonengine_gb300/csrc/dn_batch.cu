@@ -505,11 +505,16 @@ extern "C" int dn_cuda_batch_frame(DNgpuBatch* b, const dn_batch_item* items, ui
     f.packets = b->tuning.kernel == 2u && maxSpec <= PK_MAX_SPEC_SEGMENTS;
     b->lastPackets = f.packets;
     if (f.t.size > b->tabCap) {
+        // growing waits for the stream, frees pinned memory (which waits for the device) and renews the
+        // graph, a stall of up to two frames: the first table is large enough for about 370 maps per frame
+        // (about 11 KB each, 8 KB of it materials), so a server whose ticks grow from a few maps to dozens
+        // never grows it
         CK(cudaStreamSynchronize(b->stream));
         if (b->htab) cudaFreeHost(b->htab);
         b->htab = nullptr;
         dfree(b->dtab);
-        const size_t nc = f.t.size + f.t.size / 2;
+        const size_t minTable = (size_t)4 << 20;
+        const size_t nc = f.t.size + f.t.size / 2 > minTable ? f.t.size + f.t.size / 2 : minTable;
         COUNT_ALLOC();
         CK(cudaMallocHost((void**)&b->htab, nc));
         int rc = dalloc(&b->dtab, nc);
