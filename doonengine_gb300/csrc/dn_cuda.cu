@@ -291,7 +291,11 @@ template <class T> static int grow_copy(DNgpuVolume* g, T** p, uint64_t oldCount
     if (g_asyncAlloc && bit) CK(cudaMallocAsync((void**)&np, (newCount ? newCount : 1) * sizeof(T), g->stream));
     else CK(cudaMalloc((void**)&np, (newCount ? newCount : 1) * sizeof(T)));
     if (*p && oldCount) CK(cudaMemcpyAsync(np, *p, oldCount * sizeof(T), cudaMemcpyDeviceToDevice, g->stream));
-    CK(cudaStreamSynchronize(g->stream));
+    // an array from the stream-ordered pool is freed after the copy and after every earlier use on the
+    // volume's stream (a batch member's stream is the batch's: the frames in flight that still read it come
+    // first), so the host does not wait; the host reads of these arrays synchronise the stream first, and
+    // eviction orders its copies after it by an event.  Only a plain cudaFree needs the wait.
+    if (!(bit && (g->poolMask & bit))) CK(cudaStreamSynchronize(g->stream));
     vfree(g, *p);
     *p = np;
     if (g_asyncAlloc && bit) g->poolMask |= bit;
